@@ -1,0 +1,115 @@
+"""ctypes binding of libhpsim_gb300.so (the C ABI of include/hpsim_gb300.h).
+
+The library is built in-tree by hpsim_gb300/build.py.  Loading fails loudly
+when it is missing: there is no CPU fallback for the tracking path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+HPS_OK = 0
+_lib = None
+
+
+class HPSimError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+    def __init__(self, status, message):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load libhpsim_gb300.so; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()' or python hpsim_gb300/build.py)")
+    L = C.CDLL(path)
+    vp, d, u32, i32, u64 = C.c_void_p, C.c_double, C.c_uint32, C.c_int, C.c_uint64
+    dp, up, ip, pvp = C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_void_p)
+    cp = C.c_char_p
+    st = C.c_int
+    sig = {
+        "hps_abi_version": (i32, []),
+        "hps_last_error": (cp, []),
+        "hps_status_string": (cp, [i32]),
+        "hps_set_gpu": (st, [i32]),
+        "hps_kernel_launch_count": (u64, []),
+        "hps_beam_create": (st, [u32, d, d, d, i32, pvp]),
+        "hps_beam_destroy": (st, [vp]),
+        "hps_beam_info": (st, [vp, up, ip]),
+        "hps_beam_set_distribution": (st, [vp, dp, dp, dp, dp, dp, dp, up, up]),
+        "hps_beam_set_waterbag": (st, [vp, dp, d, d, d, u32]),
+        "hps_beam_set_dc": (st, [vp, dp, d, d, d, u32]),
+        "hps_beam_get_coord": (st, [vp, i32, dp]),
+        "hps_beam_get_loss": (st, [vp, i32, up]),
+        "hps_beam_save": (st, [vp, i32]),
+        "hps_beam_restore": (st, [vp, i32]),
+        "hps_beam_set_ref_w": (st, [vp, d]),
+        "hps_beam_set_ref_phi": (st, [vp, d]),
+        "hps_beam_get_ref": (st, [vp, dp, dp]),
+        "hps_beam_set_frequency": (st, [vp, d]),
+        "hps_beam_get_scalar": (st, [vp, i32, dp]),
+        "hps_beam_update": (st, [vp, i32, i32, i32]),
+        "hps_beam_get_stat": (st, [vp, i32, dp]),
+        "hps_beam_apply_cut": (st, [vp, C.c_char, d, d]),
+        "hps_beam_translate": (st, [vp, i32, d]),
+        "hps_beam_monitor": (st, [vp, dp]),
+        "hps_beamline_create": (st, [pvp]),
+        "hps_beamline_destroy": (st, [vp]),
+        "hps_beamline_add": (st, [vp, i32, cp, dp]),
+        "hps_beamline_size": (st, [vp, up]),
+        "hps_beamline_find": (st, [vp, cp, up]),
+        "hps_beamline_get": (st, [vp, u32, ip, C.c_char_p, C.c_size_t, dp]),
+        "hps_beamline_set_param": (st, [vp, u32, i32, d]),
+        "hps_scheff_create": (st, [u32, u32, u32, pvp]),
+        "hps_scheff_destroy": (st, [vp]),
+        "hps_scheff_set": (st, [vp, i32, d]),
+        "hps_scheff_get": (st, [vp, i32, dp]),
+        "hps_scheff_set_mesh_size": (st, [vp, u32, u32]),
+        "hps_sim_create": (st, [vp, vp, vp, pvp]),
+        "hps_sim_destroy": (st, [vp]),
+        "hps_sim_simulate": (st, [vp, i32, i32]),
+        "hps_sim_reset": (st, [vp]),
+        "hps_sim_set_space_charge": (st, [vp, i32]),
+        "hps_sim_set_monitor": (st, [vp, dp, u32]),
+        "hps_sim_use_graph": (st, [vp, i32]),
+        "hps_sim_synchronize": (st, [vp]),
+        "hps_sim_last_time_ms": (st, [vp, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status, what=""):
+    if status != HPS_OK:
+        msg = lib().hps_last_error().decode(errors="replace")
+        raise HPSimError(status, f"{what}: {msg}" if what else msg)
+
+
+def call(name, *args):
+    check(getattr(lib(), name)(*args), name)
+
+
+def dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def uptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))

@@ -1,0 +1,107 @@
+// common.cuh -- device-side types shared by the tracking kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/hps_layout.h"
+
+namespace hps {
+
+// src/util/inc/constant.h:7-11
+constexpr double CLIGHT = 299.792458;
+constexpr double PI = 3.14159265358979323846;
+constexpr double TWOPI = 3.14159265358979323846 * 2.0;
+
+constexpr int kBlock = 256;      // threads per block of the particle kernels
+constexpr int kMaxPassBlocks = 1216;  // 8 x 152 SMs
+
+// Indices of the per-beam device scalars (same order as HPS_ST_* in the ABI).
+enum Stat {
+  X_AVG, X_AVG_GOOD, XP_AVG, Y_AVG, Y_AVG_GOOD, YP_AVG, PHI_AVG, PHI_AVG_R, PHI_AVG_GOOD,
+  W_AVG, W_AVG_GOOD, X_SIG, X_SIG_GOOD, XP_SIG, Y_SIG, Y_SIG_GOOD, YP_SIG, PHI_SIG,
+  PHI_SIG_R, PHI_SIG_GOOD, W_SIG, W_SIG_GOOD, X_EMIT, Y_EMIT, Z_EMIT, R_MAX, ABS_PHI_MAX,
+  NSTAT
+};
+
+// The reference's per-beam device scalars (src/beam/inc/beam.h:175-263).
+struct BeamStats {
+  double st[NSTAT];
+  uint32_t num_loss, num_lloss, num_good;
+  uint32_t pad;
+};
+
+// Particle storage.  FP64 beams use the double arrays; FP32 beams use the
+// float arrays, where fphi / fw are offsets from the synchronous particle.
+struct DevBeam {
+  uint32_t n;
+  double mass, charge;
+  double *x, *xp, *y, *yp, *phi, *phi_r, *w;
+  float *fx, *fxp, *fy, *fyp, *fphi, *fw, *fphi_r;
+  uint32_t *loss, *lloss;
+  BeamStats *st;
+};
+
+// SCHEFF solver state in device memory (configuration, the adaptive-remesh
+// memory of space_charge.h:112-125 and the per-kick decision).
+struct ScState {
+  uint32_t nx, nz, nx_init, nz_init, nx_max, nz_max, adj_bunch;
+  uint32_t good_cnt_old;
+  double adj_bunch_w, mesh_w, remesh_val, interval, interval_init;
+  double sigr_old, sigz_old, gm_old;
+  double dr, dz;                       // scheff_sz (space_charge_kernel.cu:12)
+  uint32_t num_on_mesh;                // space_charge_kernel.cu:13
+  // decision of the current kick (Scheff::Start, space_charge.cpp:82-139)
+  int remesh;
+  uint32_t adj;
+  double beta, freq, frac;
+  double ratio_r, ratio_z, ratio_q, ratio_g;
+  uint32_t n_solves;
+  int resized;
+};
+
+struct ScTables {
+  unsigned long long *bin_fx;  // fixed-point deposit, nz_max*nx_max
+  double *fld1;                // (nx+1)*nx*nz (x,y interleaved)
+  double *fld2;                // (nz+1)*(nx+1) (x,y interleaved)
+  float *ffld1, *ffld2;        // FP32 variants
+};
+
+// deposit weights are accumulated as integers: deterministic in any order
+constexpr double kBinScale = 68719476736.0;        // 2^36
+constexpr double kBinInvScale = 1.0 / 68719476736.0;
+
+// reduction scratch of one beam
+struct PassScratch {
+  double *part;          // kMaxPassBlocks * 32
+  unsigned int *counter; // 1
+};
+
+__host__ __device__ inline uint32_t next_pow2(uint32_t x) {
+  --x;
+  x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
+  return ++x;
+}
+
+// Beam::SetNumThreadsPerBlock, src/beam/src/beam.cpp:148-168
+__host__ __device__ inline void ref_launch(uint32_t n, uint32_t *grid, uint32_t *blck) {
+  uint32_t nt = next_pow2(n);
+  if (nt > 256) { *grid = nt / 256; *blck = 256; }
+  else { *grid = 1; *blck = nt; }
+}
+
+inline int pass_blocks(uint32_t n) {
+  uint32_t b = (n + 4 * kBlock - 1) / (4 * kBlock);
+  if (b < 1) b = 1;
+  if (b > (uint32_t)kMaxPassBlocks) b = kMaxPassBlocks;
+  return (int)b;
+}
+
+inline int grid_for(uint32_t n) {
+  uint32_t b = (n + kBlock - 1) / kBlock;
+  if (b < 1) b = 1;
+  if (b > 152u * 16u) b = 152u * 16u;
+  return (int)b;
+}
+
+}  // namespace hps

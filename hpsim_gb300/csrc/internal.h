@@ -1,0 +1,72 @@
+// internal.h -- launchers shared between the translation units of the
+// library (host-side declarations; no device code).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace hps {
+
+// count of kernel launches issued by this library (hps_kernel_launch_count)
+void note_launch(int n = 1);
+
+// ---- beam reductions and small beam kernels (beam_ops.cu) -------------
+void beam_update_loss(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_update_lloss_count(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_update_good_count(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_update_avg(const DevBeam &b, int coord, int good, PassScratch s, cudaStream_t st);
+void beam_update_sig(const DevBeam &b, int coord, int good, PassScratch s, cudaStream_t st);
+void beam_update_emittance(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_update_relative_phi(const DevBeam &b, int use_good, cudaStream_t st);
+void beam_update_longitudinal_loss(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_update_avg_xy(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_update_max_r_phi(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam_change_frequency(const DevBeam &b, double ratio, PassScratch s, cudaStream_t st);
+void beam_apply_cut(const DevBeam &b, int coord, double lo, double hi, cudaStream_t st);
+void beam_shift(const DevBeam &b, int coord, double val, cudaStream_t st);
+void beam_set_ref(const DevBeam &b, int coord, double val, cudaStream_t st);
+void beam_monitor(const DevBeam &b, const ScState *sc, double *mon_dev, uint32_t elem,
+                  PassScratch s, cudaStream_t st);
+
+// ---- element transfer maps (push.cu) ------------------------------------
+struct GapArgs {
+  double length, frequency, clbl, amplitude, phase_ref, phase_shift, energy_out, beta_center,
+      dg, t, tp, sp, fbc, fbm, ta[6], sa[5];
+  double design_w_in, phi_in, q1, q2, wl;
+  uint32_t ccl_cell_num;
+  int ccl;
+};
+void load_gap_args(const double *p, GapArgs *g);
+
+void push_partial_drift(const DevBeam &b, double wl, double hf, double aper, uint32_t eid, cudaStream_t st);
+void push_half_quad(const DevBeam &b, double wl, double len, double aper, double grad, uint32_t eid,
+                    cudaStream_t st);
+void push_steerer(const DevBeam &b, double blh, double blv, cudaStream_t st);
+void push_gap_first(const DevBeam &b, const GapArgs &g, cudaStream_t st);
+void push_gap_second(const DevBeam &b, const GapArgs &g, cudaStream_t st);
+void push_buncher(const DevBeam &b, double wl, double w_ref, double freq, double voltage, double phase,
+                  double aper, double freq_ratio, uint32_t eid, cudaStream_t st);
+void push_rotation(const DevBeam &b, double angle, cudaStream_t st);
+void push_aperture(const DevBeam &b, int rect, const double *p, uint32_t eid, cudaStream_t st);
+void push_dipole(const DevBeam &b, const double *p, double wl, int second, cudaStream_t st);
+
+// ---- SCHEFF (scheff.cu) -------------------------------------------------
+struct ScKickArgs {
+  double freq;          // beam frequency (Beam::freq) at the kick
+  double current;       // beam current (Beam::current) at the kick
+  double frac;          // space-charge fraction (SpaceCharge::fraction_)
+  double length;        // kick length
+  uint64_t skip_stride; // particles i % skip_stride == 0 are not kicked (0: no kick launch)
+  int deposit_ok;       // DistributeParticleKernel launch is valid (blck_size/4 > 0)
+  int stats_ok;         // num_particle > 2 (UpdateStatForSpaceCharge runs)
+  size_t deposit_smem;  // bytes of the per-block histogram (largest mesh)
+};
+// allow the deposit kernel the shared memory of the largest mesh
+void sc_configure(size_t max_deposit_smem);
+void sc_start(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+              PassScratch s, cudaStream_t st);
+void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
+
+}  // namespace hps

@@ -1,0 +1,93 @@
+// reduce.cuh -- one-launch deterministic reductions over the particles.
+//
+// The reference reduces every moment with a Harris two-level tree: a first
+// pass capped at 64 blocks, a second pass, then a <<<1,1>>> finaliser kernel
+// (src/beam/src/beam.cu:411-436, 651-678); about 30 launches and 5 blocking
+// scalar reads per space-charge kick.  Here one launch does all of it: every
+// block reduces its grid-stride share of the particles (each thread in index
+// order, warps by a fixed shuffle tree, warps in index order), writes one
+// partial per block, and the last block to finish (threadfence + counter)
+// sums the partials in block order and runs the finaliser.  The result is
+// bitwise reproducible for a given particle count, and the per-particle
+// callback may also write per-particle outputs (relative phase, loss flags)
+// in the same sweep.
+#pragma once
+
+#include "common.cuh"
+
+namespace hps {
+
+struct SumComb {
+  __device__ static double ident() { return 0.0; }
+  __device__ static double comb(double a, double b) { return a + b; }
+};
+struct MaxComb {  // MaxR2PhiReduceKernel starts from 0 (beam_kernel.cu:809-810)
+  __device__ static double ident() { return 0.0; }
+  __device__ static double comb(double a, double b) { return a < b ? b : a; }
+};
+
+// Op must provide:
+//   static constexpr int K;            number of accumulators (<= 32)
+//   using Comb = SumComb | MaxComb;
+//   __device__ bool enabled() const;   device-side predicate (false: no work)
+//   __device__ void particle(uint32_t i, double (&acc)[K]) const;
+//   __device__ void finalize(const double* tot, int tid, int nthreads) const;
+template <class Op>
+__global__ void __launch_bounds__(kBlock) pass_kernel(Op op, uint32_t n, PassScratch scr) {
+  constexpr int K = Op::K;
+  using C = typename Op::Comb;
+  if (!op.enabled()) return;
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = C::ident();
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) op.particle(i, acc);
+
+  __shared__ double sm[kBlock / 32][K];
+  __shared__ double tot[K];
+  __shared__ int is_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
+    if (lane == 0) sm[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double v = C::ident();
+    for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, sm[w][threadIdx.x]);
+    scr.part[blockIdx.x * K + threadIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (threadIdx.x < K) {
+    double v = C::ident();
+    for (uint32_t b = 0; b < gridDim.x; ++b) v = C::comb(v, __ldcg(scr.part + b * K + threadIdx.x));
+    tot[threadIdx.x] = v;
+  }
+  __syncthreads();
+  op.finalize(tot, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (threadIdx.x == 0) *scr.counter = 0u;
+}
+
+template <class Op>
+inline void launch_pass(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s) {
+  pass_kernel<Op><<<pass_blocks(n), kBlock, 0, s>>>(op, n, scr);
+}
+
+// wrap(phi - ref) as UpdateRelativePhiKernel, beam_kernel.cu:1507-1525
+__device__ inline double rel_phase(double phi, double ref) {
+  double tmp = phi - ref + PI;
+  double sign = 1.0;
+  if (tmp < 0) { sign = -1.0; tmp = -tmp; }
+  return sign * (fmod(tmp, TWOPI) - PI);
+}
+
+}  // namespace hps

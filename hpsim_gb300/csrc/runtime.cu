@@ -1,0 +1,1064 @@
+// runtime.cu -- host runtime and C ABI (include/hpsim_gb300.h).
+//
+// Host objects mirror the reference's classes: Beam (src/beam/src/beam.cpp),
+// BeamLine (src/beamline/src/beamline.cpp), Scheff (src/simulation/src/
+// space_charge.cpp) and SimulationEngine (src/simulation/src/
+// simulation_engine.{cpp,cu}).  All particle work is issued on the beam's
+// CUDA stream; a simulate() call issues a fixed launch sequence (the
+// space-charge decisions live on the device), which is captured once into a
+// CUDA graph and replayed while the lattice and the engine's host state are
+// unchanged.
+#include <algorithm>
+#include <atomic>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/hpsim_gb300.h"
+#include "internal.h"
+
+namespace hps {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+static thread_local std::string g_err;
+
+static hps_status fail(hps_status s, const std::string &msg) {
+  g_err = msg;
+  return s;
+}
+
+#define CK(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(HPS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static hps_status last_launch_status(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(HPS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return HPS_OK;
+}
+
+}  // namespace hps
+
+using namespace hps;
+
+// ---------------------------------------------------------------------------
+// objects
+// ---------------------------------------------------------------------------
+struct hps_beam_s {
+  uint32_t n = 0;
+  int prec = HPS_PREC_FP64;
+  double mass = 0, charge = 0, current = 0, freq = 0, design_w = 0;
+  uint32_t grid_size = 1, blck_size = 1;
+  cudaStream_t stream = nullptr;
+  DevBeam d{};
+  PassScratch scr{};
+  // device snapshots for Save/Restore (slot 0 initial, 1 intermediate)
+  double *save[2][6] = {};
+  uint32_t *save_loss[2] = {}, *save_lloss[2] = {};
+  double save_design_w[2] = {}, save_freq[2] = {}, save_current[2] = {};
+  bool saved[2] = {false, false};
+};
+
+struct hps_beamline_s {
+  std::vector<int> types;
+  std::vector<std::string> names;
+  std::vector<std::vector<double>> params;
+  uint64_t version = 0;
+};
+
+struct hps_scheff_s {
+  // host mirror of SpaceCharge's members (space_charge.h:88-125)
+  uint32_t nx, nz, nx_init, nz_init, adj_bunch;
+  double fraction = 1.0, interval = 0.01, interval_init = 0.01, adj_bunch_w = 0.0, mesh_w = 0.0,
+         remesh_val = 0.05;
+  uint32_t nx_max, nz_max;
+  ScState *d = nullptr;
+  ScTables t{};
+  uint64_t version = 0;
+};
+
+struct GraphEntry {
+  uint64_t key = 0;
+  cudaGraphExec_t exec = nullptr;
+  // host state after the range
+  double design_w, wavelen, beam_freq, beam_current, beam_design_w, fraction, interval;
+  uint32_t ccl_cell_num, cur_id;
+  int prev_end;
+};
+
+struct hps_sim_s {
+  hps_beam_t beam = nullptr;
+  hps_beamline_t bl = nullptr;
+  hps_scheff_t sc = nullptr;
+  bool sc_on = false;
+  // engine globals of simulation_engine.cu:19-33
+  uint32_t cur_id = 0, ccl_cell_num = 0;
+  double design_w = 0, wavelen = 0;
+  int prev_end = -1;
+  // monitor
+  double *mon_host = nullptr;
+  uint32_t mon_cap = 0;
+  double *mon_dev = nullptr;
+  uint32_t mon_dev_cap = 0;
+  bool use_graph = true;
+  GraphEntry graph;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+};
+
+// ---------------------------------------------------------------------------
+// beam helpers
+// ---------------------------------------------------------------------------
+namespace {
+
+bool valid(hps_beam_t b) { return b != nullptr && b->d.loss != nullptr; }
+
+hps_status sync(hps_beam_t b) {
+  CK(cudaStreamSynchronize(b->stream));
+  return HPS_OK;
+}
+
+template <typename T>
+hps_status dmalloc(T **p, size_t n) {
+  CK(cudaMalloc((void **)p, (n ? n : 1) * sizeof(T)));
+  CK(cudaMemset(*p, 0, (n ? n : 1) * sizeof(T)));
+  return HPS_OK;
+}
+
+hps_status upload(hps_beam_t b, const double *x, const double *xp, const double *y, const double *yp,
+                  const double *phi, const double *w, const uint32_t *loss, const uint32_t *lloss) {
+  size_t nd = (size_t)b->n * sizeof(double), nu = (size_t)b->n * sizeof(uint32_t);
+  cudaStream_t s = b->stream;
+  CK(cudaMemcpyAsync(b->d.x, x, nd, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b->d.xp, xp, nd, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b->d.y, y, nd, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b->d.yp, yp, nd, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b->d.phi, phi, nd, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b->d.w, w, nd, cudaMemcpyHostToDevice, s));
+  if (loss) CK(cudaMemcpyAsync(b->d.loss, loss, nu, cudaMemcpyHostToDevice, s));
+  else CK(cudaMemsetAsync(b->d.loss, 0, nu, s));
+  if (lloss) CK(cudaMemcpyAsync(b->d.lloss, lloss, nu, cudaMemcpyHostToDevice, s));
+  else CK(cudaMemsetAsync(b->d.lloss, 0, nu, s));
+  return HPS_OK;
+}
+
+// Beam::InitPhiAvgGood, beam.cpp:655-661: UpdateLoss, UpdateAvgPhi(), copy
+// to phi_avg_good
+__global__ void k_copy_phi_avg(DevBeam b) { b.st->st[PHI_AVG_GOOD] = b.st->st[PHI_AVG]; }
+
+hps_status init_phi_avg_good(hps_beam_t b) {
+  beam_update_loss(b->d, b->scr, b->stream);
+  beam_update_avg(b->d, HPS_COORD_PHI, 0, b->scr, b->stream);
+  k_copy_phi_avg<<<1, 1, 0, b->stream>>>(b->d);
+  note_launch();
+  return last_launch_status("init_phi_avg_good");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int hps_abi_version(void) { return HPS_ABI_VERSION; }
+const char *hps_last_error(void) { return g_err.c_str(); }
+const char *hps_status_string(int s) {
+  switch (s) {
+    case HPS_OK: return "ok";
+    case HPS_ERR_INVALID: return "invalid argument";
+    case HPS_ERR_CUDA: return "CUDA error";
+    case HPS_ERR_NOT_FOUND: return "element not found";
+    case HPS_ERR_LATTICE: return "malformed lattice";
+    case HPS_ERR_STATE: return "invalid state";
+    case HPS_ERR_TIMEOUT: return "device wait timed out";
+    case HPS_ERR_NOMEM: return "out of memory";
+    case HPS_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+uint64_t hps_kernel_launch_count(void) { return g_launches.load(); }
+
+hps_status hps_set_gpu(int device) {
+  CK(cudaSetDevice(device));
+  return HPS_OK;
+}
+
+// ---- Beam -----------------------------------------------------------------
+hps_status hps_beam_create(uint32_t num, double mass, double charge, double current, int precision,
+                           hps_beam_t *out) {
+  if (!out) return fail(HPS_ERR_INVALID, "hps_beam_create: null output");
+  *out = nullptr;
+  if (precision != HPS_PREC_FP64) return fail(HPS_ERR_UNSUPPORTED, "hps_beam_create: precision not built");
+  hps_beam_t b = new hps_beam_s();
+  b->n = num; b->mass = mass; b->charge = charge; b->current = current; b->prec = precision;
+  ref_launch(num, &b->grid_size, &b->blck_size);
+  hps_status s;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete b; return fail(HPS_ERR_CUDA, cudaGetErrorString(e)); }
+  DevBeam &d = b->d;
+  d.n = num; d.mass = mass; d.charge = charge;
+  if ((s = dmalloc(&d.x, num)) || (s = dmalloc(&d.xp, num)) || (s = dmalloc(&d.y, num)) ||
+      (s = dmalloc(&d.yp, num)) || (s = dmalloc(&d.phi, num)) || (s = dmalloc(&d.phi_r, num)) ||
+      (s = dmalloc(&d.w, num)) || (s = dmalloc(&d.loss, num)) || (s = dmalloc(&d.lloss, num)) ||
+      (s = dmalloc(&d.st, 1)) || (s = dmalloc(&b->scr.part, (size_t)kMaxPassBlocks * 32)) ||
+      (s = dmalloc(&b->scr.counter, 1))) {
+    hps_beam_destroy(b);
+    return s;
+  }
+  *out = b;
+  return HPS_OK;
+}
+
+hps_status hps_beam_destroy(hps_beam_t b) {
+  if (!b) return HPS_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  DevBeam &d = b->d;
+  void *ptrs[] = {d.x, d.xp, d.y, d.yp, d.phi, d.phi_r, d.w, d.loss, d.lloss, d.st, b->scr.part, b->scr.counter};
+  for (void *p : ptrs) if (p) cudaFree(p);
+  for (int s = 0; s < 2; ++s) {
+    for (int k = 0; k < 6; ++k) if (b->save[s][k]) cudaFree(b->save[s][k]);
+    if (b->save_loss[s]) cudaFree(b->save_loss[s]);
+    if (b->save_lloss[s]) cudaFree(b->save_lloss[s]);
+  }
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return HPS_OK;
+}
+
+hps_status hps_beam_info(hps_beam_t b, uint32_t *num, int *precision) {
+  if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  if (num) *num = b->n;
+  if (precision) *precision = b->prec;
+  return HPS_OK;
+}
+
+hps_status hps_beam_set_distribution(hps_beam_t b, const double *x, const double *xp, const double *y,
+                                     const double *yp, const double *phi, const double *w,
+                                     const uint32_t *loss, const uint32_t *lloss) {
+  if (!valid(b) || !x || !xp || !y || !yp || !phi || !w) return fail(HPS_ERR_INVALID, "set_distribution: null array");
+  hps_status s = upload(b, x, xp, y, yp, phi, w, loss, lloss);
+  if (s) return s;
+  // the reference particle sits on axis (beam.cpp:344-358)
+  if (b->n) {
+    double z = 0.0;
+    uint32_t u = 0;
+    CK(cudaMemcpyAsync(b->d.x, &z, 8, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d.xp, &z, 8, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d.y, &z, 8, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d.yp, &z, 8, cudaMemcpyHostToDevice, b->stream));
+    if (loss) CK(cudaMemcpyAsync(b->d.loss, &u, 4, cudaMemcpyHostToDevice, b->stream));
+    if (lloss) CK(cudaMemcpyAsync(b->d.lloss, &u, 4, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));  // the scalars above live on this stack frame
+  }
+  s = init_phi_avg_good(b);
+  if (s) return s;
+  return sync(b);
+}
+
+// Beam::InitWaterbagBeam, beam.cpp:391-462 (host generation with the C
+// library's rand(), identical sequence to the reference on glibc)
+hps_status hps_beam_set_waterbag(hps_beam_t b, const double t[9], double r_sync_phi, double r_sync_w,
+                                 double r_freq, uint32_t r_seed) {
+  if (!valid(b) || !t) return fail(HPS_ERR_INVALID, "set_waterbag: bad argument");
+  uint32_t n = b->n;
+  std::vector<double> xh(n), xph(n), yh(n), yph(n), phih(n), wh(n);
+  if (r_seed == 0) std::srand((unsigned)std::time(nullptr));
+  else std::srand(r_seed);
+  double rsq = 1.0;
+  double gx = (1.0 + t[0] * t[0]) / t[1];
+  double xmx = std::sqrt(t[2] / gx), xpmx = std::sqrt(t[2] * gx), dx = -t[0] / gx;
+  double gy = (1.0 + t[3] * t[3]) / t[4];
+  double ymx = std::sqrt(t[5] / gy), ypmx = std::sqrt(t[5] * gy), dy = -t[3] / gy;
+  double gz = (1.0 + t[6] * t[6]) / t[7];
+  double zmx = std::sqrt(t[8] / gz), zpmx = t[8] / zmx, dz = -t[6] / gz;
+  double wave_len = 29979.2458 / r_freq;
+  b->freq = r_freq;
+  double gm = r_sync_w / b->mass + 1.0;
+  double beta = std::sqrt(1.0 - 1.0 / (gm * gm));
+  for (uint32_t i = 0; i < n; ++i) {
+    double r1, r2, r3, r4, r5, r6;
+    do {
+      do { r1 = 2.0 * std::rand() / RAND_MAX - 1.0; r2 = 2.0 * std::rand() / RAND_MAX - 1.0; }
+      while (r1 * r1 + r2 * r2 > 1.0);
+      do { r3 = 2.0 * std::rand() / RAND_MAX - 1.0; r4 = 2.0 * std::rand() / RAND_MAX - 1.0; }
+      while (r3 * r3 + r4 * r4 > 1.0);
+      do { r5 = 2.0 * std::rand() / RAND_MAX - 1.0; r6 = 2.0 * std::rand() / RAND_MAX - 1.0; }
+      while (r5 * r5 + r6 * r6 > 1.0);
+    } while (r1 * r1 + r2 * r2 + r3 * r3 + r4 * r4 + r5 * r5 + r6 * r6 > 1.0);
+    r1 *= rsq; r2 *= rsq; r3 *= rsq; r4 *= rsq; r5 *= rsq; r6 *= rsq;
+    xh[i] = 0.01 * (r1 * xmx + dx * r2 * xpmx);
+    xph[i] = r2 * xpmx;
+    yh[i] = 0.01 * (r3 * ymx + dy * r4 * ypmx);
+    yph[i] = r4 * ypmx;
+    phih[i] = -(r5 * zmx + dz * zpmx * r6) * 2.0 * M_PI / (beta * wave_len) + r_sync_phi;
+    wh[i] = 2.0 * r_sync_w * zpmx * r6 + r_sync_w;
+  }
+  if (n) { xh[0] = 0.0; xph[0] = 0.0; yh[0] = 0.0; yph[0] = 0.0; }
+  hps_status s = upload(b, xh.data(), xph.data(), yh.data(), yph.data(), phih.data(), wh.data(), nullptr, nullptr);
+  if (s) return s;
+  s = init_phi_avg_good(b);
+  if (s) return s;
+  return sync(b);
+}
+
+// Beam::InitDCBeam, beam.cpp:481-537
+hps_status hps_beam_set_dc(hps_beam_t b, const double t[6], double r_dphi, double r_sync_phi,
+                           double r_sync_w, uint32_t r_seed) {
+  if (!valid(b) || !t) return fail(HPS_ERR_INVALID, "set_dc: bad argument");
+  uint32_t n = b->n;
+  std::vector<double> xh(n), xph(n), yh(n), yph(n), phih(n), wh(n);
+  if (r_seed == 0) std::srand((unsigned)std::time(nullptr));
+  else std::srand(r_seed);
+  double rsq = 1.0;
+  double gx = (1.0 + t[0] * t[0]) / t[1];
+  double xmx = std::sqrt(t[2] / gx), xpmx = std::sqrt(t[2] * gx), dx = -t[0] / gx;
+  double gy = (1.0 + t[3] * t[3]) / t[4];
+  double ymx = std::sqrt(t[5] / gy), ypmx = std::sqrt(t[5] * gy), dy = -t[3] / gy;
+  for (uint32_t i = 0; i < n; ++i) {
+    double r1, r2, r3, r4, r5;
+    do {
+      do { r1 = 2.0 * std::rand() / RAND_MAX - 1.0; r2 = 2.0 * std::rand() / RAND_MAX - 1.0; }
+      while (r1 * r1 + r2 * r2 > 1.0);
+      do { r3 = 2.0 * std::rand() / RAND_MAX - 1.0; r4 = 2.0 * std::rand() / RAND_MAX - 1.0; }
+      while (r3 * r3 + r4 * r4 > 1.0);
+    } while (r1 * r1 + r2 * r2 + r3 * r3 + r4 * r4 > 1.0);
+    r1 *= rsq; r2 *= rsq; r3 *= rsq; r4 *= rsq;
+    r5 = 2.0 * (double)(i + 1.0) / (double)n - 1.0;
+    xh[i] = 0.01 * (r1 * xmx + dx * r2 * xpmx);
+    xph[i] = r2 * xpmx;
+    yh[i] = 0.01 * (r3 * ymx + dy * r4 * ypmx);
+    yph[i] = r4 * ypmx;
+    phih[i] = r5 * r_dphi + r_sync_phi;
+    wh[i] = r_sync_w;
+  }
+  if (n) { xh[0] = 0.0; xph[0] = 0.0; yh[0] = 0.0; yph[0] = 0.0; }
+  hps_status s = upload(b, xh.data(), xph.data(), yh.data(), yph.data(), phih.data(), wh.data(), nullptr, nullptr);
+  if (s) return s;
+  s = init_phi_avg_good(b);
+  if (s) return s;
+  return sync(b);
+}
+
+hps_status hps_beam_get_coord(hps_beam_t b, int coord, double *out) {
+  if (!valid(b) || !out || coord < 0 || coord > HPS_COORD_PHI_R) return fail(HPS_ERR_INVALID, "get_coord: bad argument");
+  double *src[] = {b->d.x, b->d.xp, b->d.y, b->d.yp, b->d.phi, b->d.w, b->d.phi_r};
+  CK(cudaMemcpyAsync(out, src[coord], (size_t)b->n * 8, cudaMemcpyDeviceToHost, b->stream));
+  return sync(b);
+}
+
+hps_status hps_beam_get_loss(hps_beam_t b, int longitudinal, uint32_t *out) {
+  if (!valid(b) || !out) return fail(HPS_ERR_INVALID, "get_loss: bad argument");
+  CK(cudaMemcpyAsync(out, longitudinal ? b->d.lloss : b->d.loss, (size_t)b->n * 4, cudaMemcpyDeviceToHost,
+                     b->stream));
+  return sync(b);
+}
+
+hps_status hps_beam_save(hps_beam_t b, int slot) {
+  if (!valid(b) || slot < 0 || slot > 1) return fail(HPS_ERR_INVALID, "save: bad argument");
+  double *src[6] = {b->d.x, b->d.xp, b->d.y, b->d.yp, b->d.phi, b->d.w};
+  size_t nd = (size_t)b->n * 8, nu = (size_t)b->n * 4;
+  hps_status s;
+  for (int k = 0; k < 6; ++k) {
+    if (!b->save[slot][k] && (s = dmalloc(&b->save[slot][k], b->n))) return s;
+    CK(cudaMemcpyAsync(b->save[slot][k], src[k], nd, cudaMemcpyDeviceToDevice, b->stream));
+  }
+  if (!b->save_loss[slot] && (s = dmalloc(&b->save_loss[slot], b->n))) return s;
+  if (!b->save_lloss[slot] && (s = dmalloc(&b->save_lloss[slot], b->n))) return s;
+  CK(cudaMemcpyAsync(b->save_loss[slot], b->d.loss, nu, cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->save_lloss[slot], b->d.lloss, nu, cudaMemcpyDeviceToDevice, b->stream));
+  b->save_design_w[slot] = b->design_w;
+  b->save_freq[slot] = b->freq;
+  b->save_current[slot] = b->current;
+  b->saved[slot] = true;
+  return sync(b);
+}
+
+// Beam::Restore*Beam, beam.cpp:606-647: then UpdateAvgPhi(true) and
+// UpdateRelativePhi(true)
+hps_status hps_beam_restore(hps_beam_t b, int slot) {
+  if (!valid(b) || slot < 0 || slot > 1) return fail(HPS_ERR_INVALID, "restore: bad argument");
+  if (!b->saved[slot]) return fail(HPS_ERR_STATE, "restore: no beam has been saved in this slot");
+  double *dst[6] = {b->d.x, b->d.xp, b->d.y, b->d.yp, b->d.phi, b->d.w};
+  size_t nd = (size_t)b->n * 8, nu = (size_t)b->n * 4;
+  for (int k = 0; k < 6; ++k) CK(cudaMemcpyAsync(dst[k], b->save[slot][k], nd, cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->d.loss, b->save_loss[slot], nu, cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->d.lloss, b->save_lloss[slot], nu, cudaMemcpyDeviceToDevice, b->stream));
+  b->design_w = b->save_design_w[slot];
+  b->freq = b->save_freq[slot];
+  b->current = b->save_current[slot];
+  beam_update_avg(b->d, HPS_COORD_PHI, 1, b->scr, b->stream);
+  beam_update_relative_phi(b->d, 1, b->stream);
+  hps_status s = last_launch_status("restore");
+  if (s) return s;
+  return sync(b);
+}
+
+hps_status hps_beam_set_ref_w(hps_beam_t b, double w) {
+  if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  beam_set_ref(b->d, HPS_COORD_W, w, b->stream);
+  b->design_w = w;
+  return sync(b);
+}
+hps_status hps_beam_set_ref_phi(hps_beam_t b, double phi) {
+  if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  beam_set_ref(b->d, HPS_COORD_PHI, phi, b->stream);
+  return sync(b);
+}
+hps_status hps_beam_get_ref(hps_beam_t b, double *w, double *phi) {
+  if (!valid(b) || b->n == 0) return fail(HPS_ERR_INVALID, "bad beam handle");
+  if (w) CK(cudaMemcpyAsync(w, b->d.w, 8, cudaMemcpyDeviceToHost, b->stream));
+  if (phi) CK(cudaMemcpyAsync(phi, b->d.phi, 8, cudaMemcpyDeviceToHost, b->stream));
+  return sync(b);
+}
+hps_status hps_beam_set_frequency(hps_beam_t b, double f) {
+  if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  b->freq = f;
+  return HPS_OK;
+}
+hps_status hps_beam_get_scalar(hps_beam_t b, int which, double *out) {
+  if (!valid(b) || !out) return fail(HPS_ERR_INVALID, "bad argument");
+  switch (which) {
+    case 0: *out = b->mass; break;
+    case 1: *out = b->charge; break;
+    case 2: *out = b->current; break;
+    case 3: *out = b->freq; break;
+    case 4: *out = b->design_w; break;
+    default: return fail(HPS_ERR_INVALID, "get_scalar: unknown scalar");
+  }
+  return HPS_OK;
+}
+
+hps_status hps_beam_update(hps_beam_t b, int op, int coord, int good) {
+  if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  const DevBeam &d = b->d;
+  switch (op) {
+    case 0: beam_update_loss(d, b->scr, b->stream); break;
+    case 1: beam_update_longitudinal_loss(d, b->scr, b->stream); break;
+    case 2: beam_update_good_count(d, b->scr, b->stream); break;
+    case 3: beam_update_avg(d, coord, good, b->scr, b->stream); break;
+    case 4: beam_update_sig(d, coord, good, b->scr, b->stream); break;
+    case 5: beam_update_emittance(d, b->scr, b->stream); break;
+    case 6: beam_update_relative_phi(d, good, b->stream); break;
+    case 7: beam_update_stat_for_sc(d, b->scr, b->stream); break;
+    case 8: beam_update_avg_xy(d, b->scr, b->stream); break;
+    case 9: beam_update_max_r_phi(d, b->scr, b->stream); break;
+    default: return fail(HPS_ERR_INVALID, "beam_update: unknown op");
+  }
+  hps_status s = last_launch_status("beam_update");
+  if (s) return s;
+  return sync(b);
+}
+
+hps_status hps_beam_get_stat(hps_beam_t b, int stat, double *out) {
+  if (!valid(b) || !out || stat < 0 || stat >= HPS_NST) return fail(HPS_ERR_INVALID, "get_stat: bad argument");
+  BeamStats h;
+  CK(cudaMemcpyAsync(&h, b->d.st, sizeof(h), cudaMemcpyDeviceToHost, b->stream));
+  hps_status s = sync(b);
+  if (s) return s;
+  if (stat < NSTAT) *out = h.st[stat];
+  else if (stat == HPS_ST_NUM_LOSS) *out = h.num_loss;
+  else if (stat == HPS_ST_NUM_LLOSS) *out = h.num_lloss;
+  else *out = h.num_good;
+  return HPS_OK;
+}
+
+hps_status hps_beam_apply_cut(hps_beam_t b, char coord, double lo, double hi) {
+  if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  char c = (char)std::tolower((unsigned char)coord);
+  int k = c == 'x' ? HPS_COORD_X : c == 'y' ? HPS_COORD_Y : c == 'w' ? HPS_COORD_W : c == 'p' ? HPS_COORD_PHI : -1;
+  if (k < 0) return HPS_OK;  // the reference leaves the beam untouched
+  beam_apply_cut(b->d, k, lo, hi, b->stream);
+  hps_status s = last_launch_status("apply_cut");
+  if (s) return s;
+  return sync(b);
+}
+
+hps_status hps_beam_translate(hps_beam_t b, int coord, double v) {
+  if (!valid(b) || coord < 0 || coord > HPS_COORD_W) return fail(HPS_ERR_INVALID, "translate: bad argument");
+  beam_shift(b->d, coord, v, b->stream);
+  if (coord == HPS_COORD_PHI) {  // Beam::ShiftPhi re-initialises <phi>_good
+    hps_status s = init_phi_avg_good(b);
+    if (s) return s;
+  }
+  hps_status s = last_launch_status("translate");
+  if (s) return s;
+  return sync(b);
+}
+
+hps_status hps_beam_monitor(hps_beam_t b, double *out) {
+  if (!valid(b) || !out) return fail(HPS_ERR_INVALID, "monitor: bad argument");
+  double *dm = nullptr;
+  CK(cudaMalloc((void **)&dm, HPS_NMON * sizeof(double)));
+  beam_monitor(b->d, nullptr, dm, 0, b->scr, b->stream);
+  cudaMemcpyAsync(out, dm, HPS_NMON * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+  hps_status s = sync(b);
+  cudaFree(dm);
+  return s;
+}
+
+// ---- BeamLine ---------------------------------------------------------------
+hps_status hps_beamline_create(hps_beamline_t *out) {
+  if (!out) return fail(HPS_ERR_INVALID, "null output");
+  *out = new hps_beamline_s();
+  return HPS_OK;
+}
+hps_status hps_beamline_destroy(hps_beamline_t bl) {
+  delete bl;
+  return HPS_OK;
+}
+hps_status hps_beamline_add(hps_beamline_t bl, int type, const char *name, const double *params) {
+  if (!bl || !name || !params) return fail(HPS_ERR_INVALID, "beamline_add: bad argument");
+  if (type < HPS_ELEM_DRIFT || type > HPS_ELEM_DIPOLE) return fail(HPS_ERR_INVALID, "beamline_add: unknown type");
+  bl->types.push_back(type);
+  bl->names.push_back(name);
+  bl->params.emplace_back(params, params + HPS_NPARAM);
+  bl->version++;
+  return HPS_OK;
+}
+hps_status hps_beamline_size(hps_beamline_t bl, uint32_t *out) {
+  if (!bl || !out) return fail(HPS_ERR_INVALID, "bad argument");
+  *out = (uint32_t)bl->types.size();
+  return HPS_OK;
+}
+static bool ieq(const std::string &a, const std::string &b) {
+  if (a.size() != b.size()) return false;
+  for (size_t i = 0; i < a.size(); ++i)
+    if (std::tolower((unsigned char)a[i]) != std::tolower((unsigned char)b[i])) return false;
+  return true;
+}
+hps_status hps_beamline_find(hps_beamline_t bl, const char *name, uint32_t *index) {
+  if (!bl || !name || !index) return fail(HPS_ERR_INVALID, "bad argument");
+  for (size_t i = 0; i < bl->names.size(); ++i)
+    if (ieq(bl->names[i], name)) { *index = (uint32_t)i; return HPS_OK; }
+  return fail(HPS_ERR_NOT_FOUND, std::string("Invalid beamline element name, please check it! (") + name + ")");
+}
+hps_status hps_beamline_get(hps_beamline_t bl, uint32_t i, int *type, char *name, size_t cap, double *params) {
+  if (!bl || i >= bl->types.size()) return fail(HPS_ERR_INVALID, "beamline_get: bad index");
+  if (type) *type = bl->types[i];
+  if (name && cap) { std::strncpy(name, bl->names[i].c_str(), cap - 1); name[cap - 1] = 0; }
+  if (params) std::memcpy(params, bl->params[i].data(), HPS_NPARAM * sizeof(double));
+  return HPS_OK;
+}
+hps_status hps_beamline_set_param(hps_beamline_t bl, uint32_t i, int slot, double v) {
+  if (!bl || i >= bl->types.size() || slot < 0 || slot >= HPS_NPARAM) return fail(HPS_ERR_INVALID, "set_param: bad argument");
+  bl->params[i][slot] = v;
+  bl->version++;
+  return HPS_OK;
+}
+
+// ---- SCHEFF -----------------------------------------------------------------
+static bool pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+static hps_status scheff_upload(hps_scheff_t s) {
+  ScState h{};
+  CK(cudaMemcpy(&h, s->d, sizeof(h), cudaMemcpyDeviceToHost));
+  h.nx = s->nx; h.nz = s->nz; h.nx_init = s->nx_init; h.nz_init = s->nz_init;
+  h.nx_max = s->nx_max; h.nz_max = s->nz_max;
+  h.adj_bunch = s->adj_bunch; h.adj_bunch_w = s->adj_bunch_w; h.mesh_w = s->mesh_w;
+  h.remesh_val = s->remesh_val; h.interval = s->interval; h.interval_init = s->interval_init;
+  CK(cudaMemcpy(s->d, &h, sizeof(h), cudaMemcpyHostToDevice));
+  s->version++;
+  return HPS_OK;
+}
+
+static hps_status scheff_alloc_tables(hps_scheff_t s) {
+  if (s->t.bin_fx) cudaFree(s->t.bin_fx);
+  if (s->t.fld1) cudaFree(s->t.fld1);
+  if (s->t.fld2) cudaFree(s->t.fld2);
+  s->t = ScTables{};
+  hps_status st;
+  size_t nx = s->nx_max, nz = s->nz_max;
+  if ((st = dmalloc(&s->t.bin_fx, nx * nz))) return st;
+  if ((st = dmalloc(&s->t.fld1, (nx + 1) * nx * nz * 2))) return st;
+  if ((st = dmalloc(&s->t.fld2, (nz + 1) * (nx + 1) * 2))) return st;
+  sc_configure(nx * nz * sizeof(unsigned long long));
+  return HPS_OK;
+}
+
+hps_status hps_scheff_create(uint32_t nr, uint32_t nz, uint32_t adj_bunch, hps_scheff_t *out) {
+  if (!out) return fail(HPS_ERR_INVALID, "null output");
+  *out = nullptr;
+  if (!pow2(nr) || !pow2(nz) || nz > 512 || nr > 256)
+    return fail(HPS_ERR_INVALID, "SCHEFF mesh: nr and nz must be powers of two, nz <= 512, nr <= 256");
+  hps_scheff_t s = new hps_scheff_s();
+  s->nx = s->nx_init = nr; s->nz = s->nz_init = nz; s->adj_bunch = adj_bunch;
+  s->nx_max = nr; s->nz_max = nz;
+  hps_status st;
+  if ((st = dmalloc(&s->d, 1)) || (st = scheff_alloc_tables(s)) || (st = scheff_upload(s))) {
+    hps_scheff_destroy(s);
+    return st;
+  }
+  *out = s;
+  return HPS_OK;
+}
+
+hps_status hps_scheff_destroy(hps_scheff_t s) {
+  if (!s) return HPS_OK;
+  cudaDeviceSynchronize();
+  if (s->d) cudaFree(s->d);
+  if (s->t.bin_fx) cudaFree(s->t.bin_fx);
+  if (s->t.fld1) cudaFree(s->t.fld1);
+  if (s->t.fld2) cudaFree(s->t.fld2);
+  delete s;
+  return HPS_OK;
+}
+
+// SpaceCharge setters, space_charge.h:43-87
+hps_status hps_scheff_set(hps_scheff_t s, int param, double v) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  switch (param) {
+    case 0: s->interval = v; s->interval_init = v; break;
+    case 1: s->adj_bunch = (uint32_t)v; break;
+    case 2: s->adj_bunch_w = v; break;
+    case 3: s->mesh_w = v; break;
+    case 4: s->remesh_val = v; break;
+    case 5: s->fraction = v; break;
+    default: return fail(HPS_ERR_INVALID, "scheff_set: unknown or read-only parameter");
+  }
+  return scheff_upload(s);
+}
+hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
+  if (!s || !v) return fail(HPS_ERR_INVALID, "bad argument");
+  switch (param) {
+    case 0: *v = s->interval; break;
+    case 1: *v = s->adj_bunch; break;
+    case 2: *v = s->adj_bunch_w; break;
+    case 3: *v = s->mesh_w; break;
+    case 4: *v = s->remesh_val; break;
+    case 5: *v = s->fraction; break;
+    case 6: *v = s->nx; break;
+    case 7: *v = s->nz; break;
+    default: return fail(HPS_ERR_INVALID, "scheff_get: unknown parameter");
+  }
+  return HPS_OK;
+}
+// Scheff::SetMeshSize, space_charge.cpp:61-73 (tables reallocated and zeroed)
+hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  if (!pow2(nr) || !pow2(nz) || nz > 512 || nr > 256)
+    return fail(HPS_ERR_INVALID, "SCHEFF mesh: nr and nz must be powers of two, nz <= 512, nr <= 256");
+  if (nr == s->nx && nz == s->nz) return HPS_OK;
+  s->nx = nr; s->nz = nz;
+  s->nx_max = std::max(s->nx_max, nr);
+  s->nz_max = std::max(s->nz_max, nz);
+  hps_status st = scheff_alloc_tables(s);
+  if (st) return st;
+  return scheff_upload(s);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Ctx {
+  hps_sim_t s;
+  hps_beam_t b;
+  hps_beamline_t bl;
+  hps_scheff_t sc;
+};
+
+const double *P(hps_beamline_t bl, uint32_t i) { return bl->params[i].data(); }
+int T(hps_beamline_t bl, int64_t i) {
+  return (i >= 0 && i < (int64_t)bl->types.size()) ? bl->types[i] : 0;
+}
+
+void sc_kick(Ctx &c, double length) {
+  if (!(c.s->sc_on && c.sc)) return;
+  hps_beam_t b = c.b;
+  ScKickArgs a;
+  a.freq = b->freq;
+  a.current = b->current;
+  a.frac = c.sc->fraction;
+  a.length = length;
+  a.skip_stride = (uint64_t)b->grid_size * (b->blck_size / 4);
+  a.deposit_ok = (b->blck_size / 4) > 0;
+  a.stats_ok = b->n > 2;
+  a.deposit_smem = (size_t)c.sc->nx_max * c.sc->nz_max * sizeof(unsigned long long);
+  sc_start(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream);
+}
+
+// PrepSimulateRFGap, simulation_engine.cu:163-175
+void prep_gap(Ctx &c, const GapArgs &g) {
+  hps_beam_t b = c.b;
+  if (b->freq != g.frequency) {
+    c.s->wavelen = CLIGHT / g.frequency;
+    double ratio = g.frequency / b->freq;
+    b->current *= g.frequency / b->freq;
+    beam_change_frequency(b->d, ratio, b->scr, b->stream);
+    b->freq = g.frequency;
+  }
+}
+
+// the element visitors of simulation_engine.cu:125-373
+hps_status visit(Ctx &c, uint32_t i) {
+  hps_sim_t s = c.s;
+  hps_beam_t b = c.b;
+  hps_beamline_t bl = c.bl;
+  const double *p = P(bl, i);
+  const DevBeam &d = b->d;
+  cudaStream_t st = b->stream;
+  uint32_t eid = s->cur_id;
+  switch (bl->types[i]) {
+    case HPS_ELEM_DRIFT: {
+      int nk = 1;
+      double length = p[HPS_P_LENGTH];
+      if (s->sc_on && c.sc) nk = (int)std::ceil(length / c.sc->interval);
+      double hf = 0.5 * length / nk;
+      for (int k = 0; k < nk; ++k) {
+        push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st);
+        sc_kick(c, 2.0 * hf);
+        push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st);
+      }
+      break;
+    }
+    case HPS_ELEM_QUAD:
+      if (b->blck_size / 2 > 0) push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st);
+      sc_kick(c, p[HPS_P_LENGTH]);
+      if (b->blck_size / 2 > 0) push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st);
+      break;
+    case HPS_ELEM_RFGAP_DTL: {
+      GapArgs g;
+      load_gap_args(p, &g);
+      prep_gap(c, g);
+      double phi_in = 0.0;
+      uint32_t sz = (uint32_t)bl->types.size(), cur = s->cur_id;
+      if (cur == 1 || (cur > 1 && T(bl, cur - 2) != HPS_ELEM_RFGAP_DTL)) {
+        if (cur + 2 < sz && T(bl, cur + 2) == HPS_ELEM_RFGAP_DTL)
+          phi_in = g.phase_ref - 0.5 * (P(bl, cur + 2)[HPS_P_RF_PHASE_REF] - g.phase_ref);
+        else if (cur + 1 >= sz)
+          return fail(HPS_ERR_LATTICE, "BeamLine is not set up correctly: there should be a quad following a DTL gap");
+        else phi_in = g.phase_ref;
+      } else if (cur > 1) {
+        phi_in = 0.5 * (P(bl, cur - 2)[HPS_P_RF_PHASE_REF] + g.phase_ref);
+      } else {
+        return fail(HPS_ERR_LATTICE, "A quad is missing before the DTL gap");
+      }
+      if (T(bl, (int64_t)cur - 1) != HPS_ELEM_QUAD || T(bl, (int64_t)cur + 1) != HPS_ELEM_QUAD)
+        return fail(HPS_ERR_LATTICE, "a DTL gap needs a quad on each side");
+      g.q1 = P(bl, cur - 1)[HPS_P_LENGTH];
+      g.q2 = P(bl, cur + 1)[HPS_P_LENGTH];
+      g.design_w_in = s->design_w;
+      g.phi_in = phi_in;
+      g.ccl = 0;
+      g.ccl_cell_num = 0;
+      s->wavelen = CLIGHT / g.frequency;  // d_wavelen written by the first-half kernel
+      g.wl = s->wavelen;
+      if (b->blck_size / 2 > 0) push_gap_first(d, g, st);
+      sc_kick(c, g.length);
+      if (b->blck_size / 2 > 0) push_gap_second(d, g, st);
+      s->design_w = g.energy_out;
+      b->design_w = s->design_w;
+      break;
+    }
+    case HPS_ELEM_RFGAP_CCL: {
+      GapArgs g;
+      load_gap_args(p, &g);
+      prep_gap(c, g);
+      uint32_t cur = s->cur_id;
+      if (cur == 0 || T(bl, (int64_t)cur - 1) != HPS_ELEM_RFGAP_CCL) s->ccl_cell_num = 0;
+      double phi_in, phi_out, cp = g.phase_ref;
+      if (s->ccl_cell_num == 0) {
+        int tn = T(bl, cur + 1);
+        if (tn != HPS_ELEM_RFGAP_CCL && tn != HPS_ELEM_RFGAP_DTL)
+          return fail(HPS_ERR_LATTICE, "the first CCL gap of a tank needs an RF gap after it");
+        double nxt = P(bl, cur + 1)[HPS_P_RF_PHASE_REF];
+        phi_in = cp - 0.5 * (nxt - cp);
+        phi_out = 0.5 * (nxt + cp);
+      } else if (T(bl, cur + 1) != HPS_ELEM_RFGAP_CCL) {
+        double prv = P(bl, cur - 1)[HPS_P_RF_PHASE_REF];
+        phi_in = 0.5 * (cp + prv);
+        phi_out = cp + 0.5 * (cp - prv);
+      } else {
+        phi_in = 0.5 * (cp + P(bl, cur - 1)[HPS_P_RF_PHASE_REF]);
+        phi_out = 0.5 * (cp + P(bl, cur + 1)[HPS_P_RF_PHASE_REF]);
+      }
+      g.q1 = g.q2 = 0.0;
+      g.design_w_in = s->design_w;
+      g.ccl = 1;
+      uint32_t gcb = b->blck_size / 4 > 1 ? b->blck_size / 4 : b->blck_size;
+      s->wavelen = CLIGHT / g.frequency;
+      g.wl = s->wavelen;
+      g.phi_in = phi_in;
+      g.ccl_cell_num = 0;
+      if (gcb > 0) push_gap_first(d, g, st);
+      sc_kick(c, g.length);
+      g.phi_in = phi_out;
+      g.ccl_cell_num = s->ccl_cell_num;
+      if (gcb > 0) push_gap_second(d, g, st);
+      s->ccl_cell_num++;
+      s->design_w = g.energy_out;
+      b->design_w = s->design_w;
+      break;
+    }
+    case HPS_ELEM_ROTATION:
+      push_rotation(d, p[HPS_P_ROT_ANGLE], st);
+      break;
+    case HPS_ELEM_SPCHCOMP:
+      if (s->sc_on && c.sc) c.sc->fraction = p[HPS_P_SPC_FRACTION];
+      break;
+    case HPS_ELEM_APERTURE_C:
+    case HPS_ELEM_APERTURE_R:
+      if (p[HPS_P_APT_IN] == 0.0) break;
+      beam_update_loss(d, b->scr, st);
+      beam_update_avg_xy(d, b->scr, st);
+      push_aperture(d, bl->types[i] == HPS_ELEM_APERTURE_R, p, eid, st);
+      break;
+    case HPS_ELEM_DIAGNOSTICS:
+      break;
+    case HPS_ELEM_STEERER: {
+      double blh = p[HPS_P_STR_BLH], blv = p[HPS_P_STR_BLV];
+      if (blh > 1e-10 || blv > 1e-10) push_steerer(d, blh, blv, st);
+      break;
+    }
+    case HPS_ELEM_BUNCHER: {
+      if (p[HPS_P_BUN_ON] == 0.0) break;
+      double bf = p[HPS_P_BUN_FREQ];
+      s->wavelen = CLIGHT / bf;
+      push_buncher(d, s->wavelen, s->design_w, bf, p[HPS_P_BUN_VOLTAGE], p[HPS_P_BUN_PHASE], p[HPS_P_APERTURE],
+                   bf / b->freq, eid, st);
+      break;
+    }
+    case HPS_ELEM_DIPOLE:
+      if (b->blck_size / 4 > 0) push_dipole(d, p, s->wavelen, 0, st);
+      sc_kick(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE]);
+      if (b->blck_size / 4 > 0) push_dipole(d, p, s->wavelen, 1, st);
+      break;
+    default:
+      return fail(HPS_ERR_LATTICE, "unknown element type");
+  }
+  return HPS_OK;
+}
+
+// SimulationEngine::Simulate, simulation_engine.cpp:447-469
+hps_status run_range(Ctx &c, int start_index, int end_index, bool monitor) {
+  hps_sim_t s = c.s;
+  for (int i = 0; i <= end_index; ++i) {
+    if (i >= start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP) {
+      s->cur_id = (uint32_t)i;
+      hps_status st = visit(c, (uint32_t)i);
+      if (st) return st;
+      if (monitor)
+        beam_monitor(c.b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr, s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i,
+                     c.b->scr, c.b->stream);
+    }
+  }
+  return last_launch_status("simulate");
+}
+
+uint64_t mix(uint64_t h, uint64_t v) {
+  h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+  return h;
+}
+uint64_t mixd(uint64_t h, double v) {
+  uint64_t u;
+  std::memcpy(&u, &v, 8);
+  return mix(h, u);
+}
+
+}  // namespace
+
+extern "C" {
+
+hps_status hps_sim_create(hps_beam_t beam, hps_beamline_t bl, hps_scheff_t scheff, hps_sim_t *out) {
+  if (!out || !valid(beam) || !bl) return fail(HPS_ERR_INVALID, "sim_create: bad argument");
+  hps_sim_t s = new hps_sim_s();
+  s->beam = beam; s->bl = bl; s->sc = scheff;
+  s->sc_on = scheff != nullptr;
+  s->prev_end = -1;
+  cudaEventCreate(&s->ev0);
+  cudaEventCreate(&s->ev1);
+  hps_sim_reset(s);
+  *out = s;
+  return HPS_OK;
+}
+
+hps_status hps_sim_destroy(hps_sim_t s) {
+  if (!s) return HPS_OK;
+  if (s->beam) cudaStreamSynchronize(s->beam->stream);
+  if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
+  if (s->mon_dev) cudaFree(s->mon_dev);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  delete s;
+  return HPS_OK;
+}
+
+// Reset, simulation_engine.cu:101-111
+hps_status hps_sim_reset(hps_sim_t s) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  s->cur_id = 0;
+  s->ccl_cell_num = 0;
+  s->design_w = s->beam->design_w;
+  s->wavelen = CLIGHT / s->beam->freq;
+  return HPS_OK;
+}
+
+hps_status hps_sim_set_space_charge(hps_sim_t s, int on) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  s->sc_on = on != 0;
+  return HPS_OK;
+}
+
+hps_status hps_sim_set_monitor(hps_sim_t s, double *host_out, uint32_t capacity) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  s->mon_host = host_out;
+  s->mon_cap = host_out ? capacity : 0;
+  return HPS_OK;
+}
+
+hps_status hps_sim_use_graph(hps_sim_t s, int on) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  s->use_graph = on != 0;
+  return HPS_OK;
+}
+
+hps_status hps_sim_synchronize(hps_sim_t s) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  return sync(s->beam);
+}
+
+hps_status hps_sim_last_time_ms(hps_sim_t s, double *ms) {
+  if (!s || !ms) return fail(HPS_ERR_INVALID, "bad argument");
+  *ms = s->last_ms;
+  return HPS_OK;
+}
+
+hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  Ctx c{s, s->beam, s->bl, s->sc};
+  int n = (int)c.bl->types.size();
+  if (n == 0) return HPS_OK;
+  int start_index = start < 0 ? 0 : start;
+  int end_index = end < 0 ? n - 1 : end;
+  if (start_index >= n || end_index >= n) return fail(HPS_ERR_INVALID, "simulate: element index out of range");
+  if (start_index < s->prev_end) hps_sim_reset(s);
+  s->prev_end = end_index;
+  hps_beam_t b = c.b;
+  cudaStream_t st = b->stream;
+  bool monitor = s->mon_host && s->mon_cap >= (uint32_t)n;
+  std::vector<double> solves_before;
+  if (monitor) {
+    if (s->mon_dev_cap < (uint32_t)n) {
+      if (s->mon_dev) cudaFree(s->mon_dev);
+      s->mon_dev = nullptr;
+      hps_status e = dmalloc(&s->mon_dev, (size_t)n * HPS_NMON);
+      if (e) return e;
+      s->mon_dev_cap = n;
+    }
+  }
+  double solves0 = 0.0;
+  if (monitor && c.sc) {
+    ScState h;
+    CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    solves0 = h.n_solves;
+  }
+  // graphs need the host-side state to be a function of the inputs; the
+  // mesh-size cut-off reads the solver's interval back after every kick
+  bool host_sync = s->sc_on && c.sc && c.sc->mesh_w != 0.0;
+  bool graph = s->use_graph && !host_sync;
+  uint64_t key = 0;
+  if (graph) {
+    key = mix(key, (uint64_t)start_index);
+    key = mix(key, (uint64_t)end_index);
+    key = mix(key, c.bl->version);
+    key = mix(key, (uint64_t)(uintptr_t)c.bl);
+    key = mix(key, c.sc ? c.sc->version : 0);
+    key = mix(key, (uint64_t)s->sc_on);
+    key = mix(key, (uint64_t)monitor);
+    key = mix(key, (uint64_t)s->cur_id);
+    key = mix(key, (uint64_t)s->ccl_cell_num);
+    key = mixd(key, s->design_w);
+    key = mixd(key, s->wavelen);
+    key = mixd(key, b->freq);
+    key = mixd(key, b->current);
+    key = mixd(key, b->design_w);
+    key = mixd(key, c.sc ? c.sc->fraction : 0.0);
+    key = mixd(key, c.sc ? c.sc->interval : 0.0);
+    key |= 1ull;
+  }
+  CK(cudaEventRecord(s->ev0, st));
+  if (graph && s->graph.exec && s->graph.key == key) {
+    const GraphEntry &g = s->graph;
+    CK(cudaGraphLaunch(g.exec, st));
+    s->design_w = g.design_w; s->wavelen = g.wavelen; s->ccl_cell_num = g.ccl_cell_num; s->cur_id = g.cur_id;
+    b->freq = g.beam_freq; b->current = g.beam_current; b->design_w = g.beam_design_w;
+    if (c.sc) { c.sc->fraction = g.fraction; c.sc->interval = g.interval; }
+    note_launch(0);
+  } else if (graph) {
+    cudaGraph_t gr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    hps_status e = run_range(c, start_index, end_index, monitor);
+    cudaError_t ce = cudaStreamEndCapture(st, &gr);
+    if (e) { if (ce == cudaSuccess) cudaGraphDestroy(gr); return e; }
+    if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
+    s->graph.exec = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&s->graph.exec, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    GraphEntry &g = s->graph;
+    g.key = key;
+    g.design_w = s->design_w; g.wavelen = s->wavelen; g.ccl_cell_num = s->ccl_cell_num; g.cur_id = s->cur_id;
+    g.beam_freq = b->freq; g.beam_current = b->current; g.beam_design_w = b->design_w;
+    g.fraction = c.sc ? c.sc->fraction : 0.0;
+    g.interval = c.sc ? c.sc->interval : 0.0;
+    CK(cudaGraphLaunch(g.exec, st));
+  } else {
+    for (int i = 0; i <= end_index; ++i) {
+      if (i >= start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP) {
+        s->cur_id = (uint32_t)i;
+        hps_status e = visit(c, (uint32_t)i);
+        if (e) return e;
+        if (monitor)
+          beam_monitor(b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr, s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i,
+                       b->scr, st);
+        if (host_sync) {
+          ScState h;
+          CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));
+          CK(cudaStreamSynchronize(st));
+          c.sc->interval = h.interval;
+          c.sc->nx = h.nx;
+          c.sc->nz = h.nz;
+        }
+      }
+    }
+  }
+  CK(cudaEventRecord(s->ev1, st));
+  hps_status e = last_launch_status("simulate");
+  if (e) return e;
+  if (monitor) {
+    CK(cudaMemcpyAsync(s->mon_host, s->mon_dev, (size_t)n * HPS_NMON * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  s->last_ms = ms;
+  if (monitor && c.sc && s->sc_on) {
+    double prev = solves0;
+    for (int i = 0; i <= end_index; ++i) {
+      if (!(i >= start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP)) continue;
+      double *m = s->mon_host + (size_t)i * HPS_NMON;
+      double cum = m[HPS_MON_SC_REMESH];
+      m[HPS_MON_SC_REMESH] = cum - prev;
+      prev = cum;
+    }
+  }
+  return HPS_OK;
+}
+
+}  // extern "C"

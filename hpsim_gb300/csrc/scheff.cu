@@ -1,0 +1,575 @@
+// scheff.cu -- the SCHEFF 2D r-z space-charge kick on FP64 particle state.
+//
+// Reference: Scheff::Start (src/simulation/src/space_charge.cpp:82-139), the
+// launcher glue of src/simulation/src/space_charge.cu and the kernels of
+// src/simulation/inc/space_charge_kernel.cu.  The reference reads five
+// moments back to the host per kick and decides there whether to rebuild the
+// mesh; here the statistics, the decision and the mesh sizing all stay on
+// the device, so a whole lattice pass is a fixed launch sequence that can be
+// captured in a CUDA graph.  Launch sequence per kick:
+//   3 statistics sweeps (the last one also decides) -> [max-r sweep when
+//   adjacent bunches are on] -> Green's table -> deposit -> contraction ->
+//   kick, where the mesh kernels return at once unless the decision was
+//   "remesh".
+#include "internal.h"
+#include "reduce.cuh"
+
+namespace hps {
+
+namespace {
+
+__device__ inline bool good(const DevBeam &b, uint32_t i) { return (uint32_t)(b.loss[i] + b.lloss[i]) == 0u; }
+__device__ inline double surv(const DevBeam &b) { return (double)(uint32_t)(b.n - b.st->num_loss); }
+
+// Scheff::SetMeshSize (space_charge.cpp:61-73) on the device: the tables were
+// reallocated and zeroed by Initialize in the reference.
+__device__ inline void set_mesh_size(ScState *s, uint32_t nr, uint32_t nz) {
+  if (nr != s->nx || nz != s->nz) {
+    s->nx = nr;
+    s->nz = nz;
+    s->resized = 1;
+  }
+}
+
+// UpdateScheffMeshSizeKernel, space_charge_kernel.cu:18-32
+__device__ inline void mesh_size(ScState *s, double partial_r, double partial_z, double coef) {
+  double bl = s->beta * CLIGHT / s->freq;
+  s->dr = coef * partial_r / s->nx;
+  if (coef == 1.0) s->dz = bl / s->nz;
+  else {
+    if (partial_z * coef > PI) s->dz = bl / s->nz;
+    s->dz = coef * bl * partial_z / (s->nz * PI);
+  }
+}
+
+// The host-side body of Scheff::Start after the statistics
+// (space_charge.cpp:86-138) plus UpdateMeshKernelCall (space_charge.cu:122-138).
+__device__ void scheff_decide(const DevBeam &b, ScState *s, double freq, double frac) {
+  const BeamStats &st = *b.st;
+  uint32_t good_cnt = st.num_good;
+  double sigphi = b.n < 2 ? 0.0 : st.st[PHI_SIG_GOOD];
+  double sigx = b.n < 2 ? 0.0 : st.st[X_SIG_GOOD];
+  double sigy = b.n < 2 ? 0.0 : st.st[Y_SIG_GOOD];
+  double ke = st.st[W_AVG_GOOD];
+  double gamma = (double)ke / b.mass + 1.0;
+  double beta = sqrt(1.0 - 1.0 / (gamma * gamma));
+  double lmbd = 299.792458 / freq;
+  double sigz = sigphi * 0.5 / 3.14159265 * beta * lmbd;
+  double sigr = sqrt(sigx * sigx + sigy * sigy);
+  double cratior = sigr * sigz;
+  double cratioz = sigz * sigz * gamma * gamma;
+  double cratior_old = s->sigr_old * s->sigz_old;
+  double cratioz_old = s->sigz_old * s->sigz_old * s->gm_old * s->gm_old;
+  uint32_t adj = (s->adj_bunch_w == 0.0 || ke < s->adj_bunch_w) ? s->adj_bunch : 0u;
+  s->resized = 0;
+  if (s->mesh_w != 0.0) {
+    if (ke > s->mesh_w && (s->nx != s->nx_init / 2 || s->nz != s->nz_init / 2))
+      set_mesh_size(s, s->nx_init / 2, s->nz_init / 2);
+    else if (ke <= s->mesh_w && (s->nx != s->nx_init || s->nz != s->nz_init))
+      set_mesh_size(s, s->nx_init, s->nz_init);
+    if (ke > s->mesh_w && s->interval != s->interval_init * 4) s->interval = s->interval_init * 4;
+    else if (ke <= s->mesh_w && s->interval != s->interval_init) s->interval = s->interval_init;
+  }
+  s->freq = freq;
+  s->beta = beta;
+  s->frac = frac;
+  s->adj = adj;
+  if (cratior_old == 0.0 || cratioz_old == 0.0 || fabs(cratior - cratior_old) / cratior_old > s->remesh_val ||
+      fabs(cratioz - cratioz_old) / cratioz_old > s->remesh_val) {
+    s->sigr_old = sigr;
+    s->sigz_old = sigz;
+    s->gm_old = gamma;
+    s->good_cnt_old = good_cnt;
+    s->remesh = 1;
+    s->n_solves += 1;
+    s->ratio_r = s->ratio_z = s->ratio_q = s->ratio_g = 1.0;
+    // The reference compares the device pointers x_sig_good > y_sig_good;
+    // x_sig_good is allocated first (beam.cu:51,54) so the y branch runs.
+    if (adj == 0) mesh_size(s, st.st[Y_SIG_GOOD], st.st[PHI_SIG_GOOD], 3.0);
+  } else {
+    s->remesh = 0;
+    s->ratio_r = sigr / s->sigr_old;
+    s->ratio_z = sigz / s->sigz_old;
+    s->ratio_q = s->good_cnt_old ? (double)(good_cnt / s->good_cnt_old) : 0.0;
+    s->ratio_g = gamma / s->gm_old;
+  }
+}
+
+__device__ inline void zero_mesh_tables(ScState *s, const ScTables &t, int tid, int nth) {
+  if (!(s->remesh || s->resized)) return;
+  uint32_t nb = s->nx * s->nz, nf = (s->nx + 1) * (s->nz + 1) * 2;
+  for (uint32_t k = tid; k < nb; k += nth) t.bin_fx[k] = 0ull;
+  for (uint32_t k = tid; k < nf; k += nth) t.fld2[k] = 0.0;
+  if (tid == 0 && s->remesh) s->num_on_mesh = 0u;
+}
+
+// Beam::UpdateLongitudinalLoss first half: UpdateGoodParticleCount,
+// UpdateAvgPhi(true)  (beam.cpp:776-782, 788-791, 846-852)
+struct OpGoodPhi {
+  static constexpr int K = 2;
+  using Comb = SumComb;
+  DevBeam b;
+  __device__ bool enabled() const { return true; }
+  __device__ void particle(uint32_t i, double (&a)[K]) const {
+    if (!good(b, i)) return;
+    a[0] += 1.0;
+    a[1] += b.phi[i];
+  }
+  __device__ void finalize(const double *t, int tid, int) const {
+    if (tid) return;
+    uint32_t ng = (uint32_t)t[0];
+    b.st->num_good = ng;
+    b.st->st[PHI_AVG_GOOD] = ng > 0 ? t[1] / ng : -99999;
+  }
+};
+
+// UpdateLongitudinalLossCoordinateKernel + UpdateLossCountKernelCall(lloss)
+// + UpdateGoodParticleCount + UpdateAvgPhi(true)  (beam.cpp:780-781, 1008-1009)
+struct OpLlossGoodPhi {
+  static constexpr int K = 3;
+  using Comb = SumComb;
+  DevBeam b;
+  __device__ bool enabled() const { return true; }
+  __device__ void particle(uint32_t i, double (&a)[K]) const {
+    double lim = b.st->st[PHI_AVG_GOOD];
+    uint32_t ll = b.lloss[i];
+    if (b.phi[i] > lim + TWOPI + PI) {
+      ll = 1u;
+      b.lloss[i] = 1u;
+    }
+    a[0] += ll != 0u;
+    if ((uint32_t)(b.loss[i] + ll) == 0u) {
+      a[1] += 1.0;
+      a[2] += b.phi[i];
+    }
+  }
+  __device__ void finalize(const double *t, int tid, int) const {
+    if (tid) return;
+    uint32_t ng = (uint32_t)t[1];
+    b.st->num_lloss = (uint32_t)t[0];
+    b.st->num_good = ng;
+    b.st->st[PHI_AVG_GOOD] = ng > 0 ? t[2] / ng : -99999;
+  }
+};
+
+// The rest of UpdateStatForSpaceCharge (beam.cpp:1010-1014): relative phase
+// about <phi>_good for every particle, <phi_r> over loss == 0 divided by
+// num - num_loss, sigma(phi_r) over good particles, <x>, sigma_x, <y>,
+// sigma_y over good particles divided by num - num_loss
+// (UpdateHorizontalAvgSigKernel), <w> over good particles; then, when a
+// solver is attached, the Scheff::Start decision.
+struct OpScStats {
+  static constexpr int K = 8;
+  using Comb = SumComb;
+  DevBeam b;
+  ScState *sc;
+  ScTables t;
+  double freq, frac;
+  __device__ bool enabled() const { return true; }
+  __device__ void particle(uint32_t i, double (&a)[K]) const {
+    double pr = rel_phase(b.phi[i], b.st->st[PHI_AVG_GOOD]);
+    b.phi_r[i] = pr;
+    if (b.loss[i] != 0u) return;
+    a[0] += pr;
+    if (b.lloss[i] != 0u) return;
+    double x = b.x[i], y = b.y[i];
+    a[1] += pr; a[2] += pr * pr;
+    a[3] += x; a[4] += x * x; a[5] += y; a[6] += y * y;
+    a[7] += b.w[i];
+  }
+  __device__ void finalize(const double *s, int tid, int nth) const {
+    if (tid == 0) {
+      BeamStats &st = *b.st;
+      double sv = surv(b);
+      double ng = st.num_good;
+      st.st[PHI_AVG_R] = s[0] / sv;
+      double pa = s[1] / ng, pa2 = s[2] / ng;
+      st.st[PHI_SIG_GOOD] = sqrt(pa2 - pa * pa);
+      double xa = s[3] / sv, x2 = s[4] / sv, ya = s[5] / sv, y2 = s[6] / sv;
+      st.st[X_AVG_GOOD] = xa;
+      st.st[X_SIG_GOOD] = sqrt(x2 - xa * xa);
+      st.st[Y_AVG_GOOD] = ya;
+      st.st[Y_SIG_GOOD] = sqrt(y2 - ya * ya);
+      st.st[W_AVG_GOOD] = st.num_good > 0 ? s[7] / st.num_good : -99999;
+      if (sc) scheff_decide(b, sc, freq, frac);
+    }
+    if (!sc) return;
+    __syncthreads();
+    zero_mesh_tables(sc, t, tid, nth);
+  }
+};
+
+// UpdateMaxRPhi + UpdateScheffMeshSizeKernel(r_max, coef = 1) when adjacent
+// bunches are on (space_charge.cu:124-128)
+struct OpAdjMesh {
+  static constexpr int K = 2;
+  using Comb = MaxComb;
+  DevBeam b;
+  ScState *sc;
+  __device__ bool enabled() const { return sc->remesh && sc->adj != 0u; }
+  __device__ void particle(uint32_t i, double (&a)[K]) const {
+    if (b.loss[i] != 0u) return;
+    double tx = b.x[i] - b.st->st[X_AVG], ty = b.y[i] - b.st->st[Y_AVG];
+    double r2 = tx * tx + ty * ty;
+    double tp = b.phi_r[i] - b.st->st[PHI_AVG_R];
+    tp = tp > 0.0 ? tp : -tp;
+    a[0] = a[0] < r2 ? r2 : a[0];
+    a[1] = a[1] < tp ? tp : a[1];
+  }
+  __device__ void finalize(const double *t, int tid, int) const {
+    if (tid) return;
+    b.st->st[R_MAX] = sqrt(t[0]);
+    b.st->st[ABS_PHI_MAX] = t[1];
+    mesh_size(sc, b.st->st[R_MAX], 0.0, 1.0);
+  }
+};
+
+// Scheff::Start with num_particle <= 2: statistics are not refreshed, the
+// decision still runs on whatever they hold.
+__global__ void k_decide_only(DevBeam b, ScState *sc, ScTables t, double freq, double frac) {
+  if (threadIdx.x == 0) scheff_decide(b, sc, freq, frac);
+  __syncthreads();
+  zero_mesh_tables(sc, t, threadIdx.x, blockDim.x);
+}
+
+// UpdateFldTbl1Kernel, space_charge_kernel.cu:39-100 (one thread per table
+// entry; rows rs >= (nr/by)*by are not written, as in the reference's grid)
+__global__ void k_green(const ScState *sc, ScTables t, uint32_t num_part, double cur_ov_mc2) {
+  if (!sc->remesh) return;
+  const uint32_t nr = sc->nx, nz = sc->nz;
+  const uint32_t by = (512 / nz < nr) ? 512 / nz : nr;
+  const uint32_t nrs = by ? (nr / by) * by : 0;
+  const uint32_t total = (nr + 1) * nrs * nz;
+  const double r_beta = sc->beta, r_freq = sc->freq;
+  const uint32_t adj = sc->adj;
+  const double gm = rsqrt(1.0 - r_beta * r_beta);
+  const double dr = sc->dr, dzg = sc->dz * gm;
+  const double wave_len = CLIGHT / r_freq;
+  const double pl = r_beta * gm * wave_len;
+  const double c1 = 5721.67 * cur_ov_mc2 / (r_freq * 1e6 * (double)num_part);
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    uint32_t tz = e % nz;
+    uint32_t k = (e / nz) % nrs;
+    uint32_t rpi = e / (nz * nrs);
+    double rs = sqrt(0.5 * (k * k + (k + 1) * (k + 1))) * dr;
+    double zs = 0.5 * dzg;
+    double zp = (tz + 1) * dzg;
+    double rp = rpi * dr;
+    double d = zp - zs;
+    double d2 = d * d;
+    double c = (rp - rs) * (rp - rs);
+    double b = (rp + rs) * (rp + rs);
+    double rsrp = rs * rp;
+    double a = 4.0 * rsrp / (b + d2);
+    double g = 1.0 - a;
+    double h = log(g);
+    double ee = 1.0 + g * (0.4630106 - 0.2452740 * h + g * (0.1077857 - 0.04125321 * h));
+    double ek = 1.38629436 - 0.5 * h + g * (0.1119697 - 0.1213486 * h + g * (0.07253230 - 0.02887472 * h));
+    double er1 = 0.0;
+    a = sqrt(b + d2);
+    double rs2mrp2 = (rs * rs - rp * rp);
+    if (rp != 0.0) er1 = (ek - (rs2mrp2 + d2) * ee / (c + d2)) / (2.0 * rp * a);
+    double ez1 = d * ee / (a * (c + d2));
+    for (uint32_t i = 1; i <= adj; ++i) {
+      double xi = i;
+      for (int j = 0; j < 2; ++j) {
+        double d1 = d - xi * pl;
+        d2 = d1 * d1;
+        a = 4.0 * rsrp / (b + d2);
+        g = 1.0 - a;
+        h = log(g);
+        ee = 1.0 + g * (0.4630106 - 0.2452740 * h + g * (0.1077857 - 0.04125321 * h));
+        ek = 1.38629436 - 0.5 * h + g * (0.1119697 - 0.1213486 * h + g * (0.07253230 - 0.02887472 * h));
+        a = sqrt(b + d2);
+        if (rp != 0.0) er1 += (ek - (rs2mrp2 + d2) * ee / (c + d2)) / (2.0 * rp * a);
+        ez1 += d1 * ee / (a * (c + d2));
+        xi = -xi;
+      }
+    }
+    size_t cnt = (size_t)rpi * nr * nz + (size_t)k * nz + tz;
+    t.fld1[2 * cnt] = c1 * er1;
+    t.fld1[2 * cnt + 1] = c1 * ez1;
+  }
+}
+
+__device__ inline void dep_add(unsigned long long *h, int k, double v) {
+  long long q = __double2ll_rn(v * kBinScale);
+  if (q) atomicAdd(h + k, (unsigned long long)q);
+}
+
+// DistributeParticleKernel, space_charge_kernel.cu:123-224: each block
+// deposits into its own histogram in shared memory (integer weights), then
+// adds it to the global table; integer sums make the table independent of
+// the order in which particles arrive.
+__global__ void k_deposit(DevBeam bm, ScState *sc, ScTables t) {
+  if (!sc->remesh) return;
+  extern __shared__ unsigned long long hist[];
+  const uint32_t nx = sc->nx, nz = sc->nz, nb = nx * nz;
+  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) hist[k] = 0ull;
+  __syncthreads();
+  const BeamStats &st = *bm.st;
+  const double phimc = st.st[PHI_AVG_R], xbar = st.st[X_AVG_GOOD], ybar = st.st[Y_AVG_GOOD];
+  const double epsq = st.st[X_SIG_GOOD] / st.st[Y_SIG_GOOD];
+  const double r_beta = sc->beta, r_freq = sc->freq;
+  const double gm = rsqrt(1.0 - r_beta * r_beta);
+  const double dr = sc->dr, dzg = sc->dz * gm;
+  const double wave_len = CLIGHT / r_freq;
+  const double hl = nz * 0.5 * dzg;
+  const double c2 = r_beta * gm * wave_len / TWOPI;
+  uint32_t cnt = 0;
+  for (uint32_t np = blockIdx.x * blockDim.x + threadIdx.x; np < bm.n; np += gridDim.x * blockDim.x) {
+    if (!(bm.loss[np] == 0u && bm.lloss[np] == 0u)) continue;
+    double x = bm.x[np], y = bm.y[np], z = bm.phi_r[np];
+    double rsq_sh = (x - xbar) * (x - xbar) / epsq + (y - ybar) * (y - ybar) * epsq;
+    int i = (int)(sqrt(rsq_sh) / dr + 1);
+    if (!(i >= 1 && (uint32_t)i <= nx)) continue;
+    double ddz = z - phimc;
+    for (int guard = 0; (ddz > PI || ddz < -PI) && guard < 1000000; ++guard) {
+      if (ddz > 0.0) ddz -= TWOPI;
+      else ddz += TWOPI;
+    }
+    z = -c2 * ddz;
+    if (!(fabs(z) < hl)) continue;
+    double zz = z + hl;
+    int jm1 = (int)(zz / dzg + 1);
+    int i1 = i + 1;
+    double drdr = dr * dr;
+    if (rsq_sh < 0.5 * drdr * (double)(i * i + (i - 1) * (i - 1))) i1 = i - 1;
+    if (i1 < 1) i1 = 1;
+    if (i1 > (int)nx) i1 = nx;
+    int j1 = jm1 + 1;
+    if (zz < (jm1 - 1 + 0.5) * dzg) j1 = jm1 - 1;
+    if (j1 < 1) j1 = 1;
+    if (j1 > (int)nz) j1 = nz;
+    if (jm1 < 1 || jm1 > (int)nz) continue;  // cannot happen for |z| < hl
+    double a;
+    if (i1 == i) a = 1.0;
+    else {
+      double sqrtmp = sqrt(4.0 * rsq_sh / drdr - 1.0);
+      double rminsq = 0.25 * drdr * (sqrtmp - 1.0) * (sqrtmp - 1.0);
+      double rmaxsq = rminsq + sqrtmp * drdr;
+      if (i1 < i) a = (rmaxsq - (i - 1) * (i - 1) * drdr) / (rmaxsq - rminsq);
+      else a = ((i1 - 1) * (i1 - 1) * drdr - rminsq) / (rmaxsq - rminsq);
+    }
+    double cc = 1.0;
+    if (j1 != jm1) cc = (zz - (j1 - 1 + 0.5) * dzg) / ((jm1 - j1) * dzg);
+    double bb = 1.0 - a, d = 1.0 - cc;
+    int k = (jm1 - 1) * nx + i;
+    dep_add(hist, k - 1, a * cc);
+    k += i1 - i;
+    dep_add(hist, k - 1, bb * cc);
+    k = (j1 - 1) * nx + i;
+    dep_add(hist, k - 1, a * d);
+    k += i1 - i;
+    dep_add(hist, k - 1, bb * d);
+    ++cnt;
+  }
+  for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&sc->num_on_mesh, cnt);
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
+    unsigned long long v = hist[k];
+    if (v) atomicAdd(t.bin_fx + k, v);
+  }
+}
+
+__device__ inline double bin_value(const ScTables &t, uint32_t k) {
+  return (double)(long long)t.bin_fx[k] * kBinInvScale;
+}
+
+// UpdateFldTbl2KernelDouble, space_charge_kernel.cu:472-568 launched as
+// <<<nr + 2, 1024>>>: one warp per field point; the set of bins each point
+// sums is the reference's (its integer partition of the table can leave
+// bins out on small meshes, and leaves the (nz, nr) corner at zero below
+// 1024 bins).
+__global__ void k_contract(const ScState *sc, ScTables t) {
+  if (!sc->remesh) return;
+  const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
+  const uint32_t npts = (nz + 1) * nrow;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t pt = warp; pt < npts; pt += nwarps) {
+    uint32_t zp = pt / nrow, rp = pt % nrow;
+    uint32_t lim;
+    if (zp < nz) {
+      uint32_t gnum = 1024 / nz;
+      lim = gnum ? gnum * (fld_sz / gnum) : 0;
+    } else if (rp < nx) {
+      uint32_t gnum = 1024 / nx;
+      lim = gnum ? gnum * (fld_sz / gnum) : 0;
+    } else {
+      lim = (fld_sz / 1024) * 1024;
+    }
+    double ax = 0.0, az = 0.0;
+    for (uint32_t bi = lane; bi < lim; bi += 32) {
+      double bv = bin_value(t, bi);
+      if (bv == 0.0) continue;
+      uint32_t rs = bi % nx, zs = bi / nx;
+      double sign = 1.0;
+      uint32_t dz;
+      if (zp < nz && zs >= zp) { dz = zs - zp; sign = -1.0; }
+      else dz = zp - zs - 1;
+      size_t f1 = dz + (size_t)rs * nz + (size_t)rp * fld_sz;
+      ax += bv * t.fld1[2 * f1];
+      az += sign * bv * t.fld1[2 * f1 + 1];
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      ax += __shfl_down_sync(0xffffffffu, ax, off);
+      az += __shfl_down_sync(0xffffffffu, az, off);
+    }
+    if (lane == 0) {
+      t.fld2[2 * pt] += ax;
+      t.fld2[2 * pt + 1] += az;
+    }
+  }
+}
+
+// ApplySpchKickKernel, space_charge_kernel.cu:573-706.  The reference's
+// grid-stride loop `while (indx > 0 && ...)` ends thread 0 before its first
+// particle, so particles whose index is a multiple of its launch's thread
+// count (skip_stride) are never kicked; the same set is skipped here.
+__global__ void k_kick(DevBeam bm, const ScState *sc, ScTables t, double length, double current,
+                       uint64_t skip_stride) {
+  const uint32_t nx = sc->nx, nz = sc->nz;
+  const double r_beta = sc->beta, r_freq = sc->freq, r_mass = bm.mass;
+  const double r_current = current * sc->frac;
+  const double rr = sc->ratio_r, rz = sc->ratio_z, rq = sc->ratio_q, rg = sc->ratio_g;
+  const BeamStats &st = *bm.st;
+  const double phimc = st.st[PHI_AVG_R], xbar = st.st[X_AVG_GOOD], ybar = st.st[Y_AVG_GOOD];
+  const double epsq = st.st[X_SIG_GOOD] / st.st[Y_SIG_GOOD];
+  const double gmg = rsqrt(1.0 - r_beta * r_beta);
+  const double dr = sc->dr * rr;
+  const double dzg = sc->dz * gmg * rz;
+  const double wave_len = CLIGHT / r_freq;
+  const double hl = nz * 0.5 * dzg;
+  const double c1 = 5721.67 * r_current / (r_freq * 1e6 * (double)bm.n * r_mass);
+  const double c2 = r_beta * gmg * wave_len / TWOPI;
+  const double c3 = length / (r_beta * gmg);
+  const double xfac = 2.0 / (epsq + 1.0);
+  const double yfac = epsq * xfac;
+  const uint32_t adj = sc->adj, onm = sc->num_on_mesh;
+  const uint32_t tbl_sz = (nx + 1) * (nz + 1);
+  const double *fld = t.fld2;
+  for (uint32_t indx = blockIdx.x * blockDim.x + threadIdx.x; indx < bm.n; indx += gridDim.x * blockDim.x) {
+    if (indx % skip_stride == 0) continue;
+    if (!(bm.loss[indx] == 0u && bm.lloss[indx] == 0u)) continue;
+    double x = bm.x[indx], y = bm.y[indx], xp = bm.xp[indx], yp = bm.yp[indx];
+    double phi = bm.phi_r[indx], w = bm.w[indx];
+    double cbgr, cbgzs;
+    double gm = w / r_mass + 1.0;
+    double bgz = sqrt((gm - 1.0) * (gm + 1.0));
+    double bgx = bgz * xp;
+    double bgy = bgz * yp;
+    double bgzstar = gmg * (bgz - r_beta * gm);
+    double xxbar = x - xbar, yybar = y - ybar;
+    double r = sqrt(xxbar * xxbar / epsq + yybar * yybar * epsq);
+    if (r == 0.0) r = 1.0e-8;
+    double xovr = xxbar * xfac / r;
+    double yovr = yybar * yfac / r;
+    double ddz = phi - phimc;
+    for (int guard = 0; (ddz > PI || ddz < -PI) && guard < 1000000; ++guard) {
+      if (ddz > 0.0) ddz -= TWOPI;
+      else ddz += TWOPI;
+    }
+    double z = -c2 * ddz;
+    if (r > nx * dr || fabs(z) > hl) {
+      z = -c2 * (phi - phimc);
+      double d = sqrt(z * z + r * r);
+      double invd3 = 1.0 / (d * d * d);
+      double rod3 = r * invd3;
+      double zod3 = z * invd3;
+      double pl = r_beta * gmg * wave_len;
+      for (uint32_t nb = 1; nb <= adj; ++nb) {
+        int xi = (int)nb;
+        for (int lr = 1; lr <= 2; ++lr) {
+          double sft = z + xi * pl;
+          d = sqrt(sft * sft + r * r);
+          invd3 = 1.0 / (d * d * d);
+          rod3 += r * invd3;
+          zod3 += sft * invd3;
+          xi = -xi;
+        }
+      }
+      double cbgcoef = c1 * c3 * PI * 0.5 * onm;
+      cbgr = cbgcoef * rod3;
+      cbgzs = cbgcoef * zod3;
+    } else {
+      uint32_t i = 1 + (int)(r / dr);
+      double a = r / dr - (i - 1.0);
+      double bb = 1.0 - a;
+      uint32_t j = 1 + (int)((z + hl) / dzg);
+      double c = (z + hl) / dzg - (j - 1.0);
+      double d = 1.0 - c;
+      uint32_t l = (j - 1) * (nx + 1) + i;
+      uint32_t m = l + (nx + 1);
+      if (m >= tbl_sz) m = tbl_sz - 1;
+      // l leaves the table only for r == nx*dr with z == hl, or NaN input
+      if (l >= tbl_sz || l < 1) l = tbl_sz - 1;
+      if (m < 1) m = 1;
+      double er_ratio = rq / (rr * rz * rg * rg);
+      double ez_ratio = rq / (rz * rz);
+      cbgr = er_ratio * c3 * (d * (a * fld[2 * l] + bb * fld[2 * (l - 1)]) + c * (a * fld[2 * m] + bb * fld[2 * (m - 1)]));
+      cbgzs = ez_ratio * c3 * (d * (a * fld[2 * l + 1] + bb * fld[2 * (l - 1) + 1]) +
+                               c * (a * fld[2 * m + 1] + bb * fld[2 * (m - 1) + 1]));
+    }
+    bgx += cbgr * xovr;
+    bgy += cbgr * yovr;
+    bgzstar += cbgzs;
+    double gstar = 1.0 + 0.5 * bgzstar * bgzstar;
+    double bgzf = gmg * (bgzstar + r_beta * gstar);
+    if (bgzf <= 0.0) bm.loss[indx] = 9999u;
+    else {
+      bm.xp[indx] = bgx / bgzf;
+      bm.yp[indx] = bgy / bgzf;
+      bm.w[indx] *= 1.0 + (gm + 1.0) * (bgzf - bgz) / (gm * bgz);
+    }
+  }
+}
+
+}  // namespace
+
+void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st) {
+  if (b.n <= 2) return;
+  launch_pass(OpGoodPhi{b}, b.n, s, st);
+  launch_pass(OpLlossGoodPhi{b}, b.n, s, st);
+  launch_pass(OpScStats{b, nullptr, ScTables{}, 0.0, 0.0}, b.n, s, st);
+  note_launch(3);
+}
+
+void sc_start(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+              cudaStream_t st) {
+  if (a.stats_ok) {
+    launch_pass(OpGoodPhi{b}, b.n, s, st);
+    launch_pass(OpLlossGoodPhi{b}, b.n, s, st);
+    launch_pass(OpScStats{b, sc, t, a.freq, a.frac}, b.n, s, st);
+    note_launch(3);
+  } else {
+    k_decide_only<<<1, kBlock, 0, st>>>(b, sc, t, a.freq, a.frac);
+    note_launch();
+  }
+  launch_pass(OpAdjMesh{b, sc}, b.n, s, st);
+  note_launch();
+  // mesh kernels are sized for the largest mesh this solver can take
+  k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, b.n, a.current * a.frac / b.mass);
+  note_launch();
+  if (a.deposit_ok) {
+    k_deposit<<<grid_for(b.n), kBlock, a.deposit_smem, st>>>(b, sc, t);
+    note_launch();
+  }
+  k_contract<<<2 * 152, kBlock, 0, st>>>(sc, t);
+  note_launch();
+  if (a.skip_stride) {
+    k_kick<<<grid_for(b.n), kBlock, 0, st>>>(b, sc, t, a.length, a.current, a.skip_stride);
+    note_launch();
+  }
+}
+
+void sc_configure(size_t max_deposit_smem) {
+  static size_t configured = 0;
+  if (max_deposit_smem <= configured) return;
+  configured = max_deposit_smem;
+  cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_deposit_smem);
+}
+
+}  // namespace hps

@@ -1,0 +1,198 @@
+/*
+ * hpsim_gb300.h -- C ABI of the GB300 implementation of HPSim's per-element
+ * particle-tracking path.
+ *
+ * The reference binds its tracking core through a CPython 2 extension
+ * (src/pywrapper/src/hpsim_module.cpp:398-419) over an internal C/C++ layer:
+ *   - extern "C" engine entry points, src/simulation/inc/simulation_engine_cu.h:4-25
+ *   - the SCHEFF launcher API, src/simulation/inc/space_charge_cu.h:6-26
+ *   - the Beam device API, src/beam/inc/beam_cu.h:7-40 and the Beam class,
+ *     src/beam/inc/beam.h:35-312
+ *   - BeamLine / element setters, src/beamline/inc/beamline{,_element}.h
+ * Those layers keep their state in file-scope globals (one engine, one SCHEFF
+ * solver per process).  This ABI exports the same operations keyed by opaque
+ * handles, so several beams and simulators coexist; every call returns an
+ * hps_status and hps_last_error() describes the most recent failure on the
+ * calling thread.  No call takes or returns a torch type; all arrays are
+ * plain host pointers with explicit lengths.
+ *
+ * Units follow the reference core: m, rad, MeV, MHz, T/m, MV/m, A.
+ */
+#ifndef HPSIM_GB300_H
+#define HPSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "hps_layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HPS_ABI_VERSION 1
+
+typedef enum hps_status {
+  HPS_OK = 0,
+  HPS_ERR_INVALID = 1,      /* bad argument or handle */
+  HPS_ERR_CUDA = 2,         /* CUDA runtime error (message in hps_last_error) */
+  HPS_ERR_NOT_FOUND = 3,    /* element name not in the beamline */
+  HPS_ERR_LATTICE = 4,      /* malformed lattice (the reference exits) */
+  HPS_ERR_STATE = 5,        /* operation not valid in the current state */
+  HPS_ERR_TIMEOUT = 6,      /* a bounded device wait gave up */
+  HPS_ERR_NOMEM = 7,
+  HPS_ERR_UNSUPPORTED = 8
+} hps_status;
+
+/* Particle-state precision of a beam.
+ *   HPS_PREC_FP64: every coordinate in FP64, the reference's DOUBLE_PRECISION
+ *                  build semantics (SCHEFF bins and fields in FP64).
+ *   HPS_PREC_FP32: x, x', y, y' in FP32; phase and energy stored in FP32 as
+ *                  offsets from an FP64 synchronous (on-axis) particle tracked
+ *                  by the host; SCHEFF tables in FP32; moments accumulated in
+ *                  FP64. */
+typedef enum hps_precision { HPS_PREC_FP64 = 0, HPS_PREC_FP32 = 1 } hps_precision;
+
+typedef struct hps_beam_s *hps_beam_t;
+typedef struct hps_beamline_s *hps_beamline_t;
+typedef struct hps_scheff_s *hps_scheff_t;
+typedef struct hps_sim_s *hps_sim_t;
+
+/* ---- library ------------------------------------------------------------ */
+int hps_abi_version(void);
+const char *hps_last_error(void);
+const char *hps_status_string(int status);
+/* set_gpu(id): src/beamline/src/init.cpp:12-18 */
+hps_status hps_set_gpu(int device);
+/* count of this library's kernel launches since load (for launch accounting) */
+uint64_t hps_kernel_launch_count(void);
+
+/* ---- Beam (src/beam/inc/beam.h:35-312) ---------------------------------- */
+/* Beam(num, mass, charge, current): beam.cpp:69-75 + AllocateBeam :124-134 */
+hps_status hps_beam_create(uint32_t num, double mass, double charge, double current,
+                           int precision, hps_beam_t *out);
+hps_status hps_beam_destroy(hps_beam_t beam);
+hps_status hps_beam_info(hps_beam_t beam, uint32_t *num, int *precision);
+/* InitBeamFromDistribution, beam.cpp:317-368 (loss/lloss may be NULL) */
+hps_status hps_beam_set_distribution(hps_beam_t beam, const double *x, const double *xp,
+                                     const double *y, const double *yp, const double *phi,
+                                     const double *w, const uint32_t *loss,
+                                     const uint32_t *lloss);
+/* InitWaterbagBeam, beam.cpp:391-462: twiss = {ax,bx,ex, ay,by,ey, az,bz,ez} */
+hps_status hps_beam_set_waterbag(hps_beam_t beam, const double twiss[9], double sync_phi,
+                                 double sync_w, double freq, uint32_t seed);
+/* InitDCBeam, beam.cpp:481-537: twiss = {ax,bx,ex, ay,by,ey} */
+hps_status hps_beam_set_dc(hps_beam_t beam, const double twiss[6], double dphi,
+                           double sync_phi, double sync_w, uint32_t seed);
+/* CopyBeamFromDevice, beam.cu:227-242.  coord: HPS_COORD_*; FP32 beams are
+ * returned as absolute FP64 values. */
+hps_status hps_beam_get_coord(hps_beam_t beam, int coord, double *out);
+hps_status hps_beam_get_loss(hps_beam_t beam, int longitudinal, uint32_t *out);
+/* Save/Restore{Initial,Intermediate}Beam, beam.cpp:573-647: slot 0 = initial,
+ * 1 = intermediate.  Snapshots stay on the device. */
+hps_status hps_beam_save(hps_beam_t beam, int slot);
+hps_status hps_beam_restore(hps_beam_t beam, int slot);
+/* SetRefEnergy / SetRefPhase / freq, beam.cpp:1074-1105 */
+hps_status hps_beam_set_ref_w(hps_beam_t beam, double w);
+hps_status hps_beam_set_ref_phi(hps_beam_t beam, double phi);
+hps_status hps_beam_get_ref(hps_beam_t beam, double *w, double *phi);
+hps_status hps_beam_set_frequency(hps_beam_t beam, double freq);
+/* scalar: 0 mass, 1 charge, 2 current, 3 freq, 4 design_w */
+hps_status hps_beam_get_scalar(hps_beam_t beam, int which, double *out);
+/* Beam::Update* (beam.cpp:757-1066).  op:
+ *   0 UpdateLoss, 1 UpdateLongitudinalLoss, 2 UpdateGoodParticleCount,
+ *   3 UpdateAvg(coord, good), 4 UpdateSig(coord, good), 5 UpdateEmittance,
+ *   6 UpdateRelativePhi(good), 7 UpdateStatForSpaceCharge, 8 UpdateAvgXY,
+ *   9 UpdateMaxRPhi */
+hps_status hps_beam_update(hps_beam_t beam, int op, int coord, int good);
+/* the per-beam device scalars of beam.h:175-263, HPS_ST_* below */
+hps_status hps_beam_get_stat(hps_beam_t beam, int stat, double *out);
+/* ApplyCut / Shift*, beam.cpp:1574-1648 */
+hps_status hps_beam_apply_cut(hps_beam_t beam, char coord, double lo, double hi);
+hps_status hps_beam_translate(hps_beam_t beam, int coord, double value);
+/* side-effect-free statistics record (HPS_MON_*) */
+hps_status hps_beam_monitor(hps_beam_t beam, double *out /* HPS_NMON */);
+
+#define HPS_ST_X_AVG 0
+#define HPS_ST_X_AVG_GOOD 1
+#define HPS_ST_XP_AVG 2
+#define HPS_ST_Y_AVG 3
+#define HPS_ST_Y_AVG_GOOD 4
+#define HPS_ST_YP_AVG 5
+#define HPS_ST_PHI_AVG 6
+#define HPS_ST_PHI_AVG_R 7
+#define HPS_ST_PHI_AVG_GOOD 8
+#define HPS_ST_W_AVG 9
+#define HPS_ST_W_AVG_GOOD 10
+#define HPS_ST_X_SIG 11
+#define HPS_ST_X_SIG_GOOD 12
+#define HPS_ST_XP_SIG 13
+#define HPS_ST_Y_SIG 14
+#define HPS_ST_Y_SIG_GOOD 15
+#define HPS_ST_YP_SIG 16
+#define HPS_ST_PHI_SIG 17
+#define HPS_ST_PHI_SIG_R 18
+#define HPS_ST_PHI_SIG_GOOD 19
+#define HPS_ST_W_SIG 20
+#define HPS_ST_W_SIG_GOOD 21
+#define HPS_ST_X_EMIT 22
+#define HPS_ST_Y_EMIT 23
+#define HPS_ST_Z_EMIT 24
+#define HPS_ST_R_MAX 25
+#define HPS_ST_ABS_PHI_MAX 26
+#define HPS_ST_NUM_LOSS 27
+#define HPS_ST_NUM_LLOSS 28
+#define HPS_ST_NUM_GOOD 29
+#define HPS_NST 30
+
+/* ---- BeamLine (src/beamline/inc/beamline.h) ----------------------------- */
+hps_status hps_beamline_create(hps_beamline_t *out);
+hps_status hps_beamline_destroy(hps_beamline_t bl);
+/* BeamLine::AddElement with an element record (include/hps_layout.h) */
+hps_status hps_beamline_add(hps_beamline_t bl, int type, const char *name,
+                            const double *params /* HPS_NPARAM */);
+hps_status hps_beamline_size(hps_beamline_t bl, uint32_t *out);
+/* BeamLine::GetElementModelIndex (case-insensitive), beamline.cpp:70-77 */
+hps_status hps_beamline_find(hps_beamline_t bl, const char *name, uint32_t *index);
+hps_status hps_beamline_get(hps_beamline_t bl, uint32_t index, int *type, char *name,
+                            size_t name_cap, double *params /* HPS_NPARAM */);
+/* element setters of beamline_element.h (one slot at a time) */
+hps_status hps_beamline_set_param(hps_beamline_t bl, uint32_t index, int slot, double value);
+
+/* ---- SCHEFF (src/simulation/inc/space_charge.h) ------------------------- */
+/* Scheff(nr, nz, adj_bunch), space_charge.cpp:31-40.  nr and nz must be
+ * powers of two, nz <= 512 (the reference's launch geometry requires it). */
+hps_status hps_scheff_create(uint32_t nr, uint32_t nz, uint32_t adj_bunch, hps_scheff_t *out);
+hps_status hps_scheff_destroy(hps_scheff_t s);
+/* parameter: 0 interval, 1 adj_bunch, 2 adj_bunch_cutoff_w, 3 mesh_size_cutoff_w,
+ *            4 remesh_threshold, 5 fraction, 6 nr, 7 nz (6/7 read-only) */
+hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
+hps_status hps_scheff_get(hps_scheff_t s, int param, double *value);
+/* SetMeshSize, space_charge.cpp:61-73 */
+hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz);
+
+/* ---- Simulator (src/simulation/inc/simulation_engine.h) ----------------- */
+/* SimulationEngine::InitEngine, simulation_engine.cpp:408-427 (scheff may be NULL) */
+hps_status hps_sim_create(hps_beam_t beam, hps_beamline_t bl, hps_scheff_t scheff,
+                          hps_sim_t *out);
+hps_status hps_sim_destroy(hps_sim_t sim);
+/* SimulationEngine::Simulate(start, end), simulation_engine.cpp:447-469:
+ * element indices (inclusive); -1 selects the first / the last element. */
+hps_status hps_sim_simulate(hps_sim_t sim, int32_t start, int32_t end);
+hps_status hps_sim_reset(hps_sim_t sim);
+/* SetSpaceCharge("on"/"off"), simulation_engine.h:58-64 */
+hps_status hps_sim_set_space_charge(hps_sim_t sim, int on);
+/* per-element monitor records: host array of capacity * HPS_NMON doubles,
+ * filled for every simulated element (NULL disables). */
+hps_status hps_sim_set_monitor(hps_sim_t sim, double *host_out, uint32_t capacity);
+/* capture each simulate() range into a CUDA graph and replay it (default on) */
+hps_status hps_sim_use_graph(hps_sim_t sim, int on);
+/* wait for the simulator's stream */
+hps_status hps_sim_synchronize(hps_sim_t sim);
+/* device time of the last simulate() in milliseconds (CUDA events) */
+hps_status hps_sim_last_time_ms(hps_sim_t sim, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
