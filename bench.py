@@ -1,0 +1,353 @@
+"""Particle-element steps/s of HPSim's tracking path on one GB300.
+
+Workload (one "step"): one pass of the DTL-like lattice -- 165 DTL RF gaps
+(E0 = 2.5 MV/m, phi_s = -26 deg, cubic T(beta), S(beta)) between 166 quads
+(0.04 m), a full SCHEFF 32x128 space-charge solve at every gap and quad --
+over 1,048,576 H- macro-particles from a 6D waterbag at 0.75 MeV.  The beam
+state is restored on the device before every step; the metric is
+N x elements / step time.  Synthetic seeded inputs stand in for a lattice
+database and a measured input beam.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--precision fp32|fp64]
+
+Multi-GPU: every rank runs an independent replica beam (the single-beam path
+has no data-parallel exchange); value = all ranks' particle-element steps /
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-element steps/s"
+N_PART = 1 << 20
+GAPS = 165
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--particles", type=int, default=N_PART)
+    p.add_argument("--gaps", type=int, default=GAPS)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def workload(args):
+    from hpsim_gb300 import lattices as L
+    elems = L.dtl_like(n_gaps=args.gaps)
+    return elems
+
+
+def make_sim(args, elems, seed):
+    from hpsim_gb300 import HPSim, lattices as L
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=args.particles, precision=args.precision)
+    beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, seed)
+    beam.set_ref_w(0.75)
+    beam.set_ref_phi(0.0)
+    beam.save_initial_beam()
+    bl = HPSim.BeamLine(elements=elems)
+    sc = HPSim.SpaceCharge(32, 128, 0.01, 0)
+    sc.set_remesh_threshold(0.0)
+    sim = HPSim.Simulator(beam, bl, sc)
+    return beam, bl, sc, sim
+
+
+def algorithmic_bytes(phase, n, prec):
+    """Compulsory bytes per launch of a phase (reads + writes of the
+    particle arrays it must touch)."""
+    f = 8 if prec == "fp64" else 4
+    per = {
+        "gap2": 2 * 6 * f + 4,            # 6 coordinates in and out, loss flag in
+        "gap1": 6 * f + 4 + 3 * f,        # 6 in, x/y/phi out
+        "quad": 6 * f + 4 + 5 * f,        # 6 in, x/xp/y/yp/phi out
+        "drift": 5 * f + 4 + 3 * f,       # x/xp/y/yp/w in, x/y/phi out
+        "sc_kick": 6 * f + 8 + 3 * f,     # x/y/xp/yp/phase/w + 2 flags in, xp/yp/w out
+        "sc_stats": 3 * 8 + 4 * f + 8 * 2,
+        "sc_mesh": 3 * f + 8,
+    }
+    return per.get(phase, 2 * 6 * f + 8) * n
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic(phase, prec):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            t = json.load(fh)
+        return t.get(f"{prec}:{phase}")
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(args, elems, budget_s=12.0, impl_kind="port"):
+    """The FP64 oracle (oracle/, OpenMP over all host cores) on a bounded
+    prefix of the same lattice at the same particle count."""
+    import numpy as np  # noqa: F401
+    from hpsim_gb300 import lattices as L
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.lib().orc_set_threads(threads)
+    types, params, _ = L.lattice_arrays(elems)
+    b = O.Beam(args.particles)
+    b.set_waterbag(L.waterbag_twiss(), 0.0, 0.75, 201.25, 12345)
+    b.set_ref_w(0.75)
+    b.set_ref_phi(0.0)
+    sp = O.Scheff(32, 128, 0.01, 0)
+    sp.set(remesh_threshold=0.0)
+    sim = O.Sim(b, types, params, sp)
+    done = 0
+    t0 = time.perf_counter()
+    for i in range(len(elems)):
+        sim.simulate(i, i)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": args.particles * done / dt, "unit": METRIC, "cores": threads, "kind": impl_kind,
+            "sample": f"{args.particles} particles x first {done} of {len(elems)} elements, FP64 oracle, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    elems = workload(args)
+    per_step = 4.0
+    for _ in range(args.warmup):
+        cpu_baseline(args, elems, budget_s=per_step / 4)
+    vals, times = [], []
+    for _ in range(args.steps):
+        r = cpu_baseline(args, elems, budget_s=per_step)
+        vals.append(r["value"])
+        times.append(args.particles * len(elems) / r["value"])
+    v = args.steps / sum(1.0 / x for x in vals)
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"dtl_like {args.gaps} gaps, {args.particles} particles, SCHEFF 32x128 every "
+                                   f"element (time extrapolated from bounded prefixes)",
+                       "particles": args.particles, "elements": len(elems)},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_env()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from hpsim_gb300 import HPSim, build
+    build.build()
+    HPSim.set_gpu(local)
+    elems = workload(args)
+    n_elem = len(elems)
+    beam, bl, sc, sim = make_sim(args, elems, seed=12345 + rank)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def step():
+        beam.restore_initial_beam()
+        sim.simulate()
+        return sim.last_time_ms()
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    launches0 = HPSim.kernel_launch_count()
+    barrier()
+    dev_ms = []
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()          # L2 flush between steps (256 MB > 129 MB L2)
+            torch.cuda.synchronize()
+            dev_ms.append(step())
+    barrier()
+    wall = time.perf_counter() - wall0
+    launches = HPSim.kernel_launch_count() - launches0
+    t_step = sum(dev_ms) / len(dev_ms) / 1000.0
+    if ws > 1:
+        t = torch.tensor([t_step], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = ws * args.particles * n_elem / t_step
+
+    # per-phase breakdown of one more (untimed) step: dominant kernel + roofline
+    sim.profile(True)
+    sim.profile_read(reset=True)
+    step()
+    prof = sim.profile_read(reset=True)
+    sim.profile(False)
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    per_launch_s = dom_ms / 1000.0 / max(dom_n, 1)
+    peak, peak_kind = load_peaks()
+    achieved = algorithmic_bytes(dom, args.particles, args.precision) / per_launch_s / 1e9
+    traffic = load_traffic(dom, args.precision)
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        n = args.particles
+        pin = lambda dt: torch.empty(n, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+        beam.restore_initial_beam()
+        host_in = {k: pin(torch.float64) for k in ("x", "xp", "y", "yp", "phi", "w")}
+        for k in host_in:
+            host_in[k][:] = beam._coord(k)
+        loss_in, lloss_in = pin(torch.int32).view(np.uint32), pin(torch.int32).view(np.uint32)
+        loss_in[:] = 0
+        lloss_in[:] = 0
+        host_out = {k: pin(torch.float64) for k in ("x", "xp", "y", "yp", "phi", "w")}
+        loss_out = pin(torch.int32).view(np.uint32)
+        from hpsim_gb300._capi import call, dptr, uptr
+        ref_w, ref_phi = beam.get_ref_w(), beam.get_ref_phi()
+
+        def e2e_step():
+            call("hps_beam_set_distribution", beam.handle, *[dptr(host_in[k]) for k in host_in],
+                 uptr(loss_in), uptr(lloss_in))
+            beam.set_ref_w(ref_w)
+            beam.set_ref_phi(ref_phi)
+            sim.simulate()
+            for k, c in zip(host_out, range(6)):
+                call("hps_beam_get_coord", beam.handle, c, dptr(host_out[k]))
+            call("hps_beam_get_loss", beam.handle, 0, uptr(loss_out))
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        ek = max(1, min(args.steps, 3))
+        for _ in range(ek):
+            e2e_step()
+        barrier()
+        te = (time.perf_counter() - t0) / ek
+        e2e = {"value": ws * n * n_elem / te, "unit": METRIC, "h2d_bytes_per_step": n * (6 * 8 + 4 + 4),
+               "d2h_bytes_per_step": n * (6 * 8 + 4)}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, elems)
+    ck = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * t_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+        "config": {"workload": f"dtl_like: {args.gaps} DTL gaps + {args.gaps + 1} quads, {args.particles} H- "
+                               f"particles, waterbag 0.75 MeV, SCHEFF 32x128 full solve at every element",
+                   "particles": args.particles, "elements": n_elem, "precision": args.precision,
+                   "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write)",
+                   "wall_s": wall},
+        "roofline": {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "launch_ms": per_launch_s * 1000.0,
+                     "phases_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()}},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": ck,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

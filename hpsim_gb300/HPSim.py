@@ -567,6 +567,19 @@ class Simulator:
     def use_graph(self, on=True):
         call("hps_sim_use_graph", self._h, 1 if on else 0)
 
+    PHASES = ("drift", "quad", "gap1", "gap2", "other", "sc_stats", "sc_mesh", "sc_kick", "monitor")
+
+    def profile(self, on=True):
+        """Per-phase CUDA-event timers (launches go direct, not through a graph)."""
+        call("hps_sim_profile", self._h, 1 if on else 0)
+
+    def profile_read(self, reset=True):
+        """{phase: (milliseconds, phase count)} accumulated since the last reset."""
+        ms = np.zeros(len(self.PHASES))
+        cnt = np.zeros(len(self.PHASES), dtype=np.uint64)
+        call("hps_sim_profile_read", self._h, dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_uint64)), int(reset))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.PHASES)}
+
     def last_time_ms(self):
         v = C.c_double()
         call("hps_sim_last_time_ms", self._h, C.byref(v))

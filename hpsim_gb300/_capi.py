@@ -88,6 +88,8 @@ def lib():
         "hps_sim_use_graph": (st, [vp, i32]),
         "hps_sim_synchronize": (st, [vp]),
         "hps_sim_last_time_ms": (st, [vp, dp]),
+        "hps_sim_profile": (st, [vp, i32]),
+        "hps_sim_profile_read": (st, [vp, dp, C.POINTER(C.c_uint64), i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

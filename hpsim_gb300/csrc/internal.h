@@ -65,8 +65,13 @@ struct ScKickArgs {
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);
-void sc_start(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
-              PassScratch s, cudaStream_t st);
+// Scheff::Start split in three phases: statistics + decision, mesh (Green's
+// table, deposit, contraction; no-ops unless remeshing), kick
+void sc_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+              cudaStream_t st);
+void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+             cudaStream_t st);
+void sc_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
 void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
 
 }  // namespace hps

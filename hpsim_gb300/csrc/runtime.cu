@@ -94,6 +94,7 @@ struct GraphEntry {
   double design_w, wavelen, beam_freq, beam_current, beam_design_w, fraction, interval;
   uint32_t ccl_cell_num, cur_id;
   int prev_end;
+  uint64_t nkernels = 0;  // kernels in the captured graph
 };
 
 struct hps_sim_s {
@@ -112,6 +113,13 @@ struct hps_sim_s {
   uint32_t mon_dev_cap = 0;
   bool use_graph = true;
   GraphEntry graph;
+  // per-phase timers
+  bool prof_on = false;
+  std::vector<cudaEvent_t> prof_pool;
+  std::vector<int> prof_cls;  // class of event pair k (events 2k, 2k+1)
+  size_t prof_used = 0;
+  double prof_ms[HPS_NPROF] = {};
+  uint64_t prof_cnt[HPS_NPROF] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
 };
@@ -672,11 +680,34 @@ struct Ctx {
 };
 
 const double *P(hps_beamline_t bl, uint32_t i) { return bl->params[i].data(); }
+
+void prof_mark(Ctx &c, int cls, bool begin) {
+  hps_sim_t s = c.s;
+  if (!s->prof_on) return;
+  size_t k = begin ? 2 * s->prof_used : 2 * s->prof_used + 1;
+  while (s->prof_pool.size() <= k) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    s->prof_pool.push_back(e);
+  }
+  cudaEventRecord(s->prof_pool[k], c.b->stream);
+  if (!begin) {
+    if (s->prof_cls.size() <= s->prof_used) s->prof_cls.resize(s->prof_used + 1);
+    s->prof_cls[s->prof_used] = cls;
+    s->prof_used++;
+  }
+}
+#define PHASE(cls, ...)            \
+  do {                              \
+    prof_mark(c, cls, true);        \
+    __VA_ARGS__;                    \
+    prof_mark(c, cls, false);       \
+  } while (0)
 int T(hps_beamline_t bl, int64_t i) {
   return (i >= 0 && i < (int64_t)bl->types.size()) ? bl->types[i] : 0;
 }
 
-void sc_kick(Ctx &c, double length) {
+void sc_apply(Ctx &c, double length) {
   if (!(c.s->sc_on && c.sc)) return;
   hps_beam_t b = c.b;
   ScKickArgs a;
@@ -688,7 +719,9 @@ void sc_kick(Ctx &c, double length) {
   a.deposit_ok = (b->blck_size / 4) > 0;
   a.stats_ok = b->n > 2;
   a.deposit_smem = (size_t)c.sc->nx_max * c.sc->nz_max * sizeof(unsigned long long);
-  sc_start(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream);
+  PHASE(HPS_PROF_SC_STATS, sc_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+  PHASE(HPS_PROF_SC_MESH, sc_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+  PHASE(HPS_PROF_SC_KICK, sc_kick(b->d, c.sc->d, c.sc->t, a, b->stream));
 }
 
 // PrepSimulateRFGap, simulation_engine.cu:163-175
@@ -698,7 +731,7 @@ void prep_gap(Ctx &c, const GapArgs &g) {
     c.s->wavelen = CLIGHT / g.frequency;
     double ratio = g.frequency / b->freq;
     b->current *= g.frequency / b->freq;
-    beam_change_frequency(b->d, ratio, b->scr, b->stream);
+    PHASE(HPS_PROF_OTHER, beam_change_frequency(b->d, ratio, b->scr, b->stream));
     b->freq = g.frequency;
   }
 }
@@ -719,16 +752,18 @@ hps_status visit(Ctx &c, uint32_t i) {
       if (s->sc_on && c.sc) nk = (int)std::ceil(length / c.sc->interval);
       double hf = 0.5 * length / nk;
       for (int k = 0; k < nk; ++k) {
-        push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st);
-        sc_kick(c, 2.0 * hf);
-        push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st);
+        PHASE(HPS_PROF_DRIFT, push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
+        sc_apply(c, 2.0 * hf);
+        PHASE(HPS_PROF_DRIFT, push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
       }
       break;
     }
     case HPS_ELEM_QUAD:
-      if (b->blck_size / 2 > 0) push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st);
-      sc_kick(c, p[HPS_P_LENGTH]);
-      if (b->blck_size / 2 > 0) push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st);
+      if (b->blck_size / 2 > 0)
+        PHASE(HPS_PROF_QUAD, push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
+      sc_apply(c, p[HPS_P_LENGTH]);
+      if (b->blck_size / 2 > 0)
+        PHASE(HPS_PROF_QUAD, push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       break;
     case HPS_ELEM_RFGAP_DTL: {
       GapArgs g;
@@ -757,9 +792,9 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.ccl_cell_num = 0;
       s->wavelen = CLIGHT / g.frequency;  // d_wavelen written by the first-half kernel
       g.wl = s->wavelen;
-      if (b->blck_size / 2 > 0) push_gap_first(d, g, st);
-      sc_kick(c, g.length);
-      if (b->blck_size / 2 > 0) push_gap_second(d, g, st);
+      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, push_gap_first(d, g, st));
+      sc_apply(c, g.length);
+      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP2, push_gap_second(d, g, st));
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
       break;
@@ -794,18 +829,18 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.wl = s->wavelen;
       g.phi_in = phi_in;
       g.ccl_cell_num = 0;
-      if (gcb > 0) push_gap_first(d, g, st);
-      sc_kick(c, g.length);
+      if (gcb > 0) PHASE(HPS_PROF_GAP1, push_gap_first(d, g, st));
+      sc_apply(c, g.length);
       g.phi_in = phi_out;
       g.ccl_cell_num = s->ccl_cell_num;
-      if (gcb > 0) push_gap_second(d, g, st);
+      if (gcb > 0) PHASE(HPS_PROF_GAP2, push_gap_second(d, g, st));
       s->ccl_cell_num++;
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
       break;
     }
     case HPS_ELEM_ROTATION:
-      push_rotation(d, p[HPS_P_ROT_ANGLE], st);
+      PHASE(HPS_PROF_OTHER, push_rotation(d, p[HPS_P_ROT_ANGLE], st));
       break;
     case HPS_ELEM_SPCHCOMP:
       if (s->sc_on && c.sc) c.sc->fraction = p[HPS_P_SPC_FRACTION];
@@ -813,29 +848,28 @@ hps_status visit(Ctx &c, uint32_t i) {
     case HPS_ELEM_APERTURE_C:
     case HPS_ELEM_APERTURE_R:
       if (p[HPS_P_APT_IN] == 0.0) break;
-      beam_update_loss(d, b->scr, st);
-      beam_update_avg_xy(d, b->scr, st);
-      push_aperture(d, bl->types[i] == HPS_ELEM_APERTURE_R, p, eid, st);
+      PHASE(HPS_PROF_OTHER, beam_update_loss(d, b->scr, st); beam_update_avg_xy(d, b->scr, st);
+                            push_aperture(d, bl->types[i] == HPS_ELEM_APERTURE_R, p, eid, st));
       break;
     case HPS_ELEM_DIAGNOSTICS:
       break;
     case HPS_ELEM_STEERER: {
       double blh = p[HPS_P_STR_BLH], blv = p[HPS_P_STR_BLV];
-      if (blh > 1e-10 || blv > 1e-10) push_steerer(d, blh, blv, st);
+      if (blh > 1e-10 || blv > 1e-10) PHASE(HPS_PROF_OTHER, push_steerer(d, blh, blv, st));
       break;
     }
     case HPS_ELEM_BUNCHER: {
       if (p[HPS_P_BUN_ON] == 0.0) break;
       double bf = p[HPS_P_BUN_FREQ];
       s->wavelen = CLIGHT / bf;
-      push_buncher(d, s->wavelen, s->design_w, bf, p[HPS_P_BUN_VOLTAGE], p[HPS_P_BUN_PHASE], p[HPS_P_APERTURE],
-                   bf / b->freq, eid, st);
+      PHASE(HPS_PROF_OTHER, push_buncher(d, s->wavelen, s->design_w, bf, p[HPS_P_BUN_VOLTAGE], p[HPS_P_BUN_PHASE],
+                                         p[HPS_P_APERTURE], bf / b->freq, eid, st));
       break;
     }
     case HPS_ELEM_DIPOLE:
-      if (b->blck_size / 4 > 0) push_dipole(d, p, s->wavelen, 0, st);
-      sc_kick(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE]);
-      if (b->blck_size / 4 > 0) push_dipole(d, p, s->wavelen, 1, st);
+      if (b->blck_size / 4 > 0) PHASE(HPS_PROF_OTHER, push_dipole(d, p, s->wavelen, 0, st));
+      sc_apply(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE]);
+      if (b->blck_size / 4 > 0) PHASE(HPS_PROF_OTHER, push_dipole(d, p, s->wavelen, 1, st));
       break;
     default:
       return fail(HPS_ERR_LATTICE, "unknown element type");
@@ -852,8 +886,8 @@ hps_status run_range(Ctx &c, int start_index, int end_index, bool monitor) {
       hps_status st = visit(c, (uint32_t)i);
       if (st) return st;
       if (monitor)
-        beam_monitor(c.b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr, s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i,
-                     c.b->scr, c.b->stream);
+        PHASE(HPS_PROF_MONITOR, beam_monitor(c.b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr,
+                                             s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i, c.b->scr, c.b->stream));
     }
   }
   return last_launch_status("simulate");
@@ -893,6 +927,7 @@ hps_status hps_sim_destroy(hps_sim_t s) {
   if (s->mon_dev) cudaFree(s->mon_dev);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
+  for (cudaEvent_t e : s->prof_pool) cudaEventDestroy(e);
   delete s;
   return HPS_OK;
 }
@@ -929,6 +964,22 @@ hps_status hps_sim_use_graph(hps_sim_t s, int on) {
 hps_status hps_sim_synchronize(hps_sim_t s) {
   if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
   return sync(s->beam);
+}
+
+hps_status hps_sim_profile(hps_sim_t s, int on) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  s->prof_on = on != 0;
+  return HPS_OK;
+}
+
+hps_status hps_sim_profile_read(hps_sim_t s, double *ms, uint64_t *count, int reset) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  for (int k = 0; k < HPS_NPROF; ++k) {
+    if (ms) ms[k] = s->prof_ms[k];
+    if (count) count[k] = s->prof_cnt[k];
+    if (reset) { s->prof_ms[k] = 0.0; s->prof_cnt[k] = 0; }
+  }
+  return HPS_OK;
 }
 
 hps_status hps_sim_last_time_ms(hps_sim_t s, double *ms) {
@@ -970,7 +1021,8 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
   // graphs need the host-side state to be a function of the inputs; the
   // mesh-size cut-off reads the solver's interval back after every kick
   bool host_sync = s->sc_on && c.sc && c.sc->mesh_w != 0.0;
-  bool graph = s->use_graph && !host_sync;
+  bool graph = s->use_graph && !host_sync && !s->prof_on;
+  s->prof_used = 0;
   uint64_t key = 0;
   if (graph) {
     key = mix(key, (uint64_t)start_index);
@@ -998,11 +1050,13 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
     s->design_w = g.design_w; s->wavelen = g.wavelen; s->ccl_cell_num = g.ccl_cell_num; s->cur_id = g.cur_id;
     b->freq = g.beam_freq; b->current = g.beam_current; b->design_w = g.beam_design_w;
     if (c.sc) { c.sc->fraction = g.fraction; c.sc->interval = g.interval; }
-    note_launch(0);
+    note_launch((int)g.nkernels);  // a replay launches the captured kernels again
   } else if (graph) {
     cudaGraph_t gr;
+    uint64_t launches0 = g_launches.load();
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     hps_status e = run_range(c, start_index, end_index, monitor);
+    s->graph.nkernels = g_launches.load() - launches0;
     cudaError_t ce = cudaStreamEndCapture(st, &gr);
     if (e) { if (ce == cudaSuccess) cudaGraphDestroy(gr); return e; }
     if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
@@ -1025,8 +1079,8 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
         hps_status e = visit(c, (uint32_t)i);
         if (e) return e;
         if (monitor)
-          beam_monitor(b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr, s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i,
-                       b->scr, st);
+          PHASE(HPS_PROF_MONITOR, beam_monitor(b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr,
+                                               s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i, b->scr, st));
         if (host_sync) {
           ScState h;
           CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -1048,6 +1102,13 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, s->ev0, s->ev1);
   s->last_ms = ms;
+  for (size_t k = 0; k < s->prof_used; ++k) {
+    float pm = 0.f;
+    cudaEventElapsedTime(&pm, s->prof_pool[2 * k], s->prof_pool[2 * k + 1]);
+    s->prof_ms[s->prof_cls[k]] += pm;
+    s->prof_cnt[s->prof_cls[k]] += 1;
+  }
+  s->prof_used = 0;
   if (monitor && c.sc && s->sc_on) {
     double prev = solves0;
     for (int i = 0; i <= end_index; ++i) {

@@ -537,7 +537,7 @@ void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st) {
   note_launch(3);
 }
 
-void sc_start(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+void sc_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
               cudaStream_t st) {
   if (a.stats_ok) {
     launch_pass(OpGoodPhi{b}, b.n, s, st);
@@ -548,6 +548,10 @@ void sc_start(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs
     k_decide_only<<<1, kBlock, 0, st>>>(b, sc, t, a.freq, a.frac);
     note_launch();
   }
+}
+
+void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+             cudaStream_t st) {
   launch_pass(OpAdjMesh{b, sc}, b.n, s, st);
   note_launch();
   // mesh kernels are sized for the largest mesh this solver can take
@@ -559,6 +563,9 @@ void sc_start(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs
   }
   k_contract<<<2 * 152, kBlock, 0, st>>>(sc, t);
   note_launch();
+}
+
+void sc_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st) {
   if (a.skip_stride) {
     k_kick<<<grid_for(b.n), kBlock, 0, st>>>(b, sc, t, a.length, a.current, a.skip_stride);
     note_launch();

@@ -191,6 +191,24 @@ hps_status hps_sim_use_graph(hps_sim_t sim, int on);
 hps_status hps_sim_synchronize(hps_sim_t sim);
 /* device time of the last simulate() in milliseconds (CUDA events) */
 hps_status hps_sim_last_time_ms(hps_sim_t sim, double *ms);
+/* Per-phase CUDA-event timers (the reference's StartTimer/StopTimer around
+ * Simulate, src/util/src/timer.cpp:4-18, broken down by phase).  While on,
+ * simulate() issues launches directly (no graph) with an event pair around
+ * every phase; hps_sim_profile_read returns the accumulated milliseconds and
+ * phase counts per HPS_PROF_* class. */
+#define HPS_PROF_DRIFT 0     /* partial drifts */
+#define HPS_PROF_QUAD 1      /* half quads */
+#define HPS_PROF_GAP1 2      /* RF gap first halves */
+#define HPS_PROF_GAP2 3      /* RF gap second halves */
+#define HPS_PROF_OTHER 4     /* buncher, steerer, rotation, apertures, dipoles, frequency changes */
+#define HPS_PROF_SC_STATS 5  /* SCHEFF statistics sweeps + remesh decision */
+#define HPS_PROF_SC_MESH 6   /* Green's table, deposit, contraction */
+#define HPS_PROF_SC_KICK 7   /* SCHEFF kick */
+#define HPS_PROF_MONITOR 8   /* per-element monitor records */
+#define HPS_NPROF 9
+hps_status hps_sim_profile(hps_sim_t sim, int on);
+hps_status hps_sim_profile_read(hps_sim_t sim, double *ms /* HPS_NPROF */, uint64_t *count /* HPS_NPROF */,
+                                int reset);
 
 #ifdef __cplusplus
 }
