@@ -11,6 +11,8 @@ namespace hps {
 
 // count of kernel launches issued by this library (hps_kernel_launch_count)
 void note_launch(int n = 1);
+// record the message returned by hps_last_error() and pass the status through
+int set_error(int status, const char *msg);
 
 // ---- beam reductions and small beam kernels (beam_ops.cu) -------------
 void beam_update_loss(const DevBeam &b, PassScratch s, cudaStream_t st);

@@ -33,6 +33,7 @@ static hps_status fail(hps_status s, const std::string &msg) {
   g_err = msg;
   return s;
 }
+int set_error(int status, const char *msg) { return (int)fail((hps_status)status, msg); }
 
 #define CK(call)                                                                    \
   do {                                                                              \

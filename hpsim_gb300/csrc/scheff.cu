@@ -11,6 +11,7 @@
 //   adjacent bunches are on] -> Green's table -> deposit -> contraction ->
 //   kick, where the mesh kernels return at once unless the decision was
 //   "remesh".
+#include "../../include/hpsim_gb300.h"
 #include "internal.h"
 #include "reduce.cuh"
 
@@ -579,4 +580,78 @@ void sc_configure(size_t max_deposit_smem) {
   cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_deposit_smem);
 }
 
+// ---- standalone field solve: charge table -> field table ------------------
+
+namespace {
+
+// Mesh description of a standalone solve (what Scheff::Start would have
+// settled on before UpdateTblsKernelCall / UpdateFinalFldTblKernelCall).
+__global__ void k_field_setup(ScState *sc, uint32_t nr, uint32_t nz, double dr, double dz, double beta,
+                              double freq, uint32_t adj) {
+  sc->nx = nr; sc->nz = nz; sc->nx_init = nr; sc->nz_init = nz; sc->nx_max = nr; sc->nz_max = nz;
+  sc->dr = dr; sc->dz = dz; sc->beta = beta; sc->freq = freq; sc->adj = adj;
+  sc->remesh = 1;
+}
+
+// charge table in FP64 -> the deposit's fixed-point table
+__global__ void k_bins_to_fixed(const double *bins, unsigned long long *fx, uint32_t nb) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += gridDim.x * blockDim.x)
+    fx[k] = (unsigned long long)__double2ll_rn(bins[k] * kBinScale);
+}
+
+bool mesh_ok(uint32_t nr, uint32_t nz) {
+  return nr && nz && !(nr & (nr - 1)) && !(nz & (nz - 1)) && nz <= 512 && nr <= 256;
+}
+
+}  // namespace
+
+// Green's table + contraction for a given charge table (UpdateFldTbl1Kernel
+// and UpdateFldTbl2KernelDouble).  sc, fx, fld1 and fld2 are device buffers
+// sized for (nr, nz); fld2 is overwritten.
+void sc_field_solve(ScState *sc, unsigned long long *fx, double *fld1, double *fld2, uint32_t nr, uint32_t nz,
+                    const double *bins_dev, const double *mesh, cudaStream_t st) {
+  k_field_setup<<<1, 1, 0, st>>>(sc, nr, nz, mesh[0], mesh[1], mesh[2], mesh[3], (uint32_t)mesh[6]);
+  k_bins_to_fixed<<<64, kBlock, 0, st>>>(bins_dev, fx, nr * nz);
+  cudaMemsetAsync(fld2, 0, (size_t)(nz + 1) * (nr + 1) * 2 * sizeof(double), st);
+  ScTables t{};
+  t.bin_fx = fx;
+  t.fld1 = fld1;
+  t.fld2 = fld2;
+  k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, (uint32_t)mesh[4], mesh[5]);
+  k_contract<<<2 * 152, kBlock, 0, st>>>(sc, t);
+  note_launch(4);
+}
+
 }  // namespace hps
+
+extern "C" {
+
+// UpdateTblsKernelCall (Green's table part) + UpdateFinalFldTblKernelCall,
+// src/simulation/src/space_charge.cu:148-218, on a caller-given charge table.
+hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field) {
+  using namespace hps;
+  if (!bins || !mesh || !field) return (hps_status)set_error(HPS_ERR_INVALID, "scheff_field: null pointer");
+  if (!mesh_ok(nr, nz))
+    return (hps_status)set_error(HPS_ERR_INVALID, "scheff_field: nr and nz must be powers of two, nz <= 512, nr <= 256");
+  size_t nb = (size_t)nr * nz, n1 = (size_t)(nr + 1) * nr * nz * 2, n2 = (size_t)(nz + 1) * (nr + 1) * 2;
+  ScState *sc = nullptr;
+  unsigned long long *fx = nullptr;
+  double *b = nullptr, *f1 = nullptr, *f2 = nullptr;
+  cudaError_t e = cudaMalloc((void **)&sc, sizeof(ScState));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&fx, nb * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b, nb * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&f1, n1 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&f2, n2 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(sc, 0, sizeof(ScState));
+  if (e == cudaSuccess) e = cudaMemcpy(b, bins, nb * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    sc_field_solve(sc, fx, f1, f2, nr, nz, b, mesh, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(field, f2, n2 * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(sc); cudaFree(fx); cudaFree(b); cudaFree(f1); cudaFree(f2);
+  if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
+  return HPS_OK;
+}
+
+}  // extern "C"

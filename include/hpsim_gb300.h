@@ -170,6 +170,14 @@ hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
 hps_status hps_scheff_get(hps_scheff_t s, int param, double *value);
 /* SetMeshSize, space_charge.cpp:61-73 */
 hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz);
+/* The SCHEFF table stage on its own: Green's table (UpdateFldTbl1Kernel via
+ * UpdateTblsKernelCall, space_charge.cu:148-187) and its contraction with a
+ * charge table (UpdateFinalFldTblKernelCall, space_charge.cu:189-218).
+ *   bins:  host, nr*nz charges, bin (zs, rs) at zs*nr + rs
+ *   mesh:  host, {dr, dz, beta, freq, num_particle, current*fraction/mass, adj_bunch}
+ *   field: host, (nz+1)*(nr+1) pairs (E_r, E_z) at zp*(nr+1) + rp
+ * Allocates and frees its device buffers on every call. */
+hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field);
 
 /* ---- Simulator (src/simulation/inc/simulation_engine.h) ----------------- */
 /* SimulationEngine::InitEngine, simulation_engine.cpp:408-427 (scheff may be NULL) */

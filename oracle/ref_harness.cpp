@@ -689,6 +689,11 @@ void *ref_scheff_create(uint nr, uint nz, int adj, double interval, double remes
 }
 void ref_scheff_free(void *s) { delete (Scheff *)s; }
 void ref_scheff_mesh(double *dr, double *dz, uint *onm) { *dr = scheff_sz.dr; *dz = scheff_sz.dz; *onm = num_on_mesh; }
+// mesh description of the last solve: {dr, dz, beta, freq, num_particle, current*frac/mass, adj}
+void ref_scheff_mesh_params(double *m) {
+  m[0] = scheff_sz.dr; m[1] = scheff_sz.dz; m[2] = sc_beta; m[3] = sc_freq;
+  m[4] = sc_beam->num_particle; m[5] = sc_beam->current * sc_frac / sc_beam->mass; m[6] = sc_adj;
+}
 
 void ref_scheff_tables(double *bin, double *fld1, double *fld2) {
   std::memcpy(bin, g_bin, (size_t)sc_nr * sc_nz * sizeof(double));

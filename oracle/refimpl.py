@@ -35,6 +35,7 @@ def lib():
             "ref_beam_set_distribution": (None, [vp, dp, dp, dp, dp, dp, dp, up, up]),
             "ref_beam_set_dc": (None, [vp] + [d] * 9 + [u32]),
             "ref_scheff_tables": (None, [dp, dp, dp]),
+            "ref_scheff_mesh_params": (None, [dp]),
             "ref_beam_set_ref_w": (None, [vp, d]),
             "ref_beam_set_ref_phi": (None, [vp, d]),
             "ref_beam_set_frequency": (None, [vp, d]),

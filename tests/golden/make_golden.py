@@ -142,7 +142,9 @@ def make_tables():
     m = np.zeros((1, 24))
     lb.ref_sim_simulate(sim, b, -1, -1, R._dp(m))
     lb.ref_scheff_tables(R._dp(bin_), R._dp(fld1), R._dp(fld2))
-    np.savez_compressed(os.path.join(HERE, "scheff_tables_8x64.npz"), bin=bin_, fld1=fld1, fld2=fld2,
+    mesh = np.zeros(7)
+    lb.ref_scheff_mesh_params(R._dp(mesh))
+    np.savez_compressed(os.path.join(HERE, "scheff_tables_8x64.npz"), bin=bin_, fld1=fld1, fld2=fld2, mesh=mesh,
                         mon=m, spch=json.dumps(spch))
     lb.ref_sim_free(sim)
     lb.ref_scheff_free(sp)

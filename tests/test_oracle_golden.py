@@ -93,3 +93,21 @@ def test_oracle_against_reference_build(oracle):
     assert np.array_equal(cr["loss"], co["loss"])
     for k in G.COORDS:
         assert np.allclose(cr[k], co[k], rtol=1e-10, atol=1e-12), k
+
+
+def test_field_from_charge_table(oracle):
+    """The table stage alone: the reference's charge table and mesh
+    parameters through the oracle's Green's table and contraction give the
+    reference's field table."""
+    import ctypes as C
+    z = np.load(f"{G.GOLDEN}/scheff_tables_8x64.npz")
+    m = z["mesh"]
+    s = oracle.Scheff(8, 64, 0.02, 0)
+    s.s.dr, s.s.dz = m[0], m[1]
+    oracle.lib().orc_scheff_green_table(s.h, m[2], m[3], int(m[4]), m[5], int(m[6]))
+    C.memmove(s.s.bin, z["bin"].ctypes.data, z["bin"].nbytes)
+    C.memset(s.s.fld2, 0, z["fld2"].nbytes)
+    oracle.lib().orc_scheff_contract(s.h)
+    _, fld1, fld2 = s.tables()
+    assert np.allclose(fld1, z["fld1"], rtol=1e-12, atol=1e-13 * np.abs(z["fld1"]).max())
+    assert np.allclose(fld2, z["fld2"], rtol=1e-11, atol=1e-13 * np.abs(z["fld2"]).max())
