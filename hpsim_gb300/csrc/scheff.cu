@@ -11,6 +11,8 @@
 //   adjacent bunches are on] -> Green's table -> deposit -> contraction ->
 //   kick, where the mesh kernels return at once unless the decision was
 //   "remesh".
+#include <mutex>
+
 #include "../../include/hpsim_gb300.h"
 #include "internal.h"
 #include "reduce.cuh"
@@ -650,6 +652,90 @@ hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const 
   }
   if (e == cudaSuccess) e = cudaMemcpy(field, f2, n2 * sizeof(double), cudaMemcpyDeviceToHost);
   cudaFree(sc); cudaFree(fx); cudaFree(b); cudaFree(f1); cudaFree(f2);
+  if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
+  return HPS_OK;
+}
+
+}  // extern "C"
+
+// ---- field solve without allocation --------------------------------------
+//
+// Some callers cannot allocate device memory while they run: an online model
+// that re-solves the space-charge field inside a control-system cycle and
+// must not wait on the CUDA allocator, or a host application that owns the
+// whole device through its own memory pool and hands its plugins finished
+// buffers.  hps_scheff_field_noalloc serves them: the caller supplies the
+// charge table and the field table in device memory, and the intermediate
+// tables live in one statically sized device array of this library (held
+// by every GPU that loads the library until the process exits).
+namespace hps {
+namespace {
+
+constexpr uint32_t kNoAllocMaxBins = 4096;                // nr * nz
+constexpr uint32_t kNoAllocMaxGreen = 33u * 32u * 128u;   // (nr + 1) * nr * nz
+constexpr size_t kNoAllocStateBytes = 256;
+constexpr size_t kNoAllocBytes =
+    kNoAllocStateBytes + kNoAllocMaxBins * sizeof(unsigned long long) + (size_t)kNoAllocMaxGreen * 2 * sizeof(double);
+static_assert(sizeof(ScState) <= kNoAllocStateBytes, "ScState outgrew its slot in the static scratch");
+
+// state block | fixed-point charge table | Green's table
+static __device__ __align__(256) unsigned char g_field_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void *g_scratch_addr[kMaxDevices];  // device address of g_field_scratch, per device
+
+// Device address of the scratch array on the current device.  The symbol's
+// name is only a host-side handle: the address has to be asked for once per
+// device, with that device current.
+int scratch_address(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(HPS_ERR_UNSUPPORTED, "scheff_field_noalloc: device index too large");
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_field_scratch);
+    if (e != cudaSuccess) return set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return HPS_OK;
+}
+
+}  // namespace
+}  // namespace hps
+
+extern "C" {
+
+// Same computation as hps_scheff_field on device buffers, allocating nothing.
+// The first call on a device looks up the scratch array's device address;
+// make that first call before any stream capture.  Meshes are limited to
+// nr*nz <= 4096 and (nr+1)*nr*nz <= 135168 (32 x 128 at most for nr = 32);
+// larger ones are rejected.  All calls share the scratch, so calls whose
+// work overlaps on the GPU (different streams, or other threads) race; the
+// scratch keeps the previous call's tables, and every entry this call reads
+// is rewritten first.  The field table is cleared before it is summed into.
+hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins_dev, const double *mesh,
+                                    double *field_dev, void *stream) {
+  using namespace hps;
+  if (!bins_dev || !mesh || !field_dev) return (hps_status)set_error(HPS_ERR_INVALID, "scheff_field_noalloc: null pointer");
+  if (!mesh_ok(nr, nz))
+    return (hps_status)set_error(HPS_ERR_INVALID, "scheff_field_noalloc: nr and nz must be powers of two");
+  if ((size_t)nr * nz > kNoAllocMaxBins || (size_t)(nr + 1) * nr * nz > kNoAllocMaxGreen)
+    return (hps_status)set_error(HPS_ERR_INVALID,
+                                 "scheff_field_noalloc: mesh too large for the static scratch "
+                                 "(limit nr*nz <= 4096 and (nr+1)*nr*nz <= 135168, e.g. 32 x 128)");
+  void *base = nullptr;
+  int st = scratch_address(&base);
+  if (st != HPS_OK) return (hps_status)st;
+  unsigned char *p = (unsigned char *)base;
+  ScState *sc = (ScState *)p;
+  unsigned long long *fx = (unsigned long long *)(p + kNoAllocStateBytes);
+  double *fld1 = (double *)(p + kNoAllocStateBytes + kNoAllocMaxBins * sizeof(unsigned long long));
+  sc_field_solve(sc, fx, fld1, field_dev, nr, nz, bins_dev, mesh, (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
   return HPS_OK;
 }

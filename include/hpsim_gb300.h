@@ -178,6 +178,21 @@ hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz);
  *   field: host, (nz+1)*(nr+1) pairs (E_r, E_z) at zp*(nr+1) + rp
  * Allocates and frees its device buffers on every call. */
 hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field);
+/* hps_scheff_field for callers that must not allocate device memory while
+ * they run (an online model re-solving the field inside a control cycle, a
+ * host application whose own memory pool owns the device).  No counterpart
+ * in the reference.  bins_dev and field_dev are device pointers supplied by
+ * the caller, mesh is the same 7-double host array as above, stream a
+ * cudaStream_t (NULL: default stream).  Nothing is allocated: the
+ * intermediate tables live in one static device array of the library,
+ * about 2.2 MB, kept on every GPU that loads the library until exit.  The
+ * first call on a device looks that array's address up, so make the first
+ * call before any stream capture.  Limit: nr*nz <= 4096 and
+ * (nr+1)*nr*nz <= 135168 (e.g. 32 x 128); larger meshes return
+ * HPS_ERR_INVALID.  Calls share the array: calls that overlap on the GPU
+ * race. */
+hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins_dev, const double *mesh,
+                                    double *field_dev, void *stream);
 
 /* ---- Simulator (src/simulation/inc/simulation_engine.h) ----------------- */
 /* SimulationEngine::InitEngine, simulation_engine.cpp:408-427 (scheff may be NULL) */
