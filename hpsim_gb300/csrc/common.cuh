@@ -40,6 +40,10 @@ struct DevBeam {
   float *fx, *fxp, *fy, *fyp, *fphi, *fw, *fphi_r;
   uint32_t *loss, *lloss;
   BeamStats *st;
+  // FP32 beams: absolute phase and energy of the synchronous (reference)
+  // particle the offsets fphi, fw are taken from.  Tracked on the host in
+  // FP64 through the same element formulas (on axis) and passed by value.
+  double phi_ref, w_ref;
 };
 
 // SCHEFF solver state in device memory (configuration, the adaptive-remesh
@@ -60,12 +64,56 @@ struct ScState {
   int resized;
 };
 
+// Constants of one FP32 SCHEFF kick, formed once per kick in FP64 by the
+// thread that takes the space-charge decision, read by every FP32 kernel of
+// the kick (FP64 arithmetic per thread or per block would cost more than the
+// particle sweeps themselves on GB300).
+struct Sc32Consts {
+  float phimc, xbar, ybar, epsq, inv_epsq, xfac, yfac;  // bunch centre and aspect
+  float beta, gmg, c2, pl;                              // bunch-frame kinematics
+  float dr, dzg, inv_dr, inv_dzg, hl, rmesh;            // mesh as seen by the kick (ratio-scaled)
+  float dr0, dzg0, inv_dr0, inv_dzg0, hl0;              // mesh of the last solve (deposit, Green's table)
+  float cbg_per_onm;                                    // c1 c3 pi/2 (times num_on_mesh)
+  float er_c3, ez_c3;                                   // interpolated-field scale
+  float dwc;                                            // synchronous particle - bunch-frame energy
+  float green_c1;                                       // Green's table scale
+};
+
 struct ScTables {
   unsigned long long *bin_fx;  // fixed-point deposit, nz_max*nx_max
   double *fld1;                // (nx+1)*nx*nz (x,y interleaved)
   double *fld2;                // (nz+1)*(nx+1) (x,y interleaved)
-  float *ffld1, *ffld2;        // FP32 variants
+  float *ffld1, *ffld2;        // FP32 variants (FP32 beams)
+  Sc32Consts *c32;             // FP32 beams: constants of the current kick
 };
+
+// Kinematics of the reference particle in FP32, for offset arithmetic.
+struct RefK {
+  float w, g, gam, beta, minv;
+};
+__host__ __device__ inline RefK make_refk(double w, double mass) {
+  double g = w / mass;
+  RefK r;
+  r.w = (float)w;
+  r.g = (float)g;
+  r.gam = (float)(g + 1.0);
+  r.beta = (float)(sqrt(g * (g + 2.0)) / (g + 1.0));
+  r.minv = (float)(1.0 / mass);
+  return r;
+}
+
+// 1/beta_i - 1/beta_ref for a particle dw above the reference, computed from
+// beta_i^2 - beta_r^2 = (gamma_i^2 - gamma_r^2)/(gamma_i^2 gamma_r^2) so the
+// difference keeps FP32 relative precision; also returns g_i = W_i/m and beta_i.
+__device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta) {
+  g = fmaf(dw, r.minv, r.g);
+  float gam = g + 1.0f;
+  float bg = sqrtf(g * (g + 2.0f));
+  beta = bg / gam;
+  float dg = dw * r.minv;
+  float db = dg * (gam + r.gam) / (gam * gam * r.gam * r.gam * (beta + r.beta));
+  return -db / (beta * r.beta);
+}
 
 // deposit weights are accumulated as integers: deterministic in any order
 constexpr double kBinScale = 68719476736.0;        // 2^36

@@ -64,6 +64,7 @@ struct ScKickArgs {
   int deposit_ok;       // DistributeParticleKernel launch is valid (blck_size/4 > 0)
   int stats_ok;         // num_particle > 2 (UpdateStatForSpaceCharge runs)
   size_t deposit_smem;  // bytes of the per-block histogram (largest mesh)
+  uint32_t nx_max, nz_max;  // largest mesh the solver's tables hold
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);
@@ -75,5 +76,44 @@ void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs 
              cudaStream_t st);
 void sc_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
 void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
+// Green's table (k_green) for a solver whose state says "remesh"
+void sc_green(const ScState *sc, const ScTables &t, uint32_t num_part, double cur_ov_mc2, cudaStream_t st);
+
+// ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
+// Launchers that move the synchronous particle update b.phi_ref / b.w_ref.
+void push32_partial_drift(DevBeam &b, double wl, double hf, double aper, uint32_t eid, cudaStream_t st);
+void push32_half_quad(DevBeam &b, double wl, double len, double aper, double grad, uint32_t eid, cudaStream_t st);
+void push32_steerer(DevBeam &b, double blh, double blv, cudaStream_t st);
+void push32_gap_first(DevBeam &b, const GapArgs &g, cudaStream_t st);
+void push32_gap_second(DevBeam &b, const GapArgs &g, cudaStream_t st);
+void push32_buncher(DevBeam &b, double wl, double w_ref_design, double freq, double voltage, double phase,
+                    double aper, double freq_ratio, uint32_t eid, cudaStream_t st);
+void push32_rotation(DevBeam &b, double angle, cudaStream_t st);
+void push32_aperture(DevBeam &b, int rect, const double *p, uint32_t eid, cudaStream_t st);
+void push32_dipole(DevBeam &b, const double *p, double wl, int second, cudaStream_t st);
+
+void beam32_update_avg(const DevBeam &b, int coord, int good, PassScratch s, cudaStream_t st);
+void beam32_update_sig(const DevBeam &b, int coord, int good, PassScratch s, cudaStream_t st);
+void beam32_update_emittance(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam32_update_relative_phi(const DevBeam &b, int use_good, cudaStream_t st);
+void beam32_update_longitudinal_loss(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam32_update_avg_xy(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam32_update_max_r_phi(const DevBeam &b, PassScratch s, cudaStream_t st);
+void beam32_change_frequency(DevBeam &b, double ratio, PassScratch s, cudaStream_t st);
+void beam32_apply_cut(const DevBeam &b, int coord, double lo, double hi, cudaStream_t st);
+void beam32_shift(const DevBeam &b, int coord, double val, cudaStream_t st);
+void beam32_set_ref(DevBeam &b, int coord, double val, cudaStream_t st);
+void beam32_monitor(const DevBeam &b, const ScState *sc, double *mon_dev, uint32_t elem, PassScratch s,
+                    cudaStream_t st);
+void beam32_from_double(const DevBeam &b, const double *const *src, cudaStream_t st);
+void beam32_to_double(const DevBeam &b, int coord, double *out, cudaStream_t st);
+void beam32_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
+
+void sc32_configure();
+void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+                cudaStream_t st);
+void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
+               cudaStream_t st);
+void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
 
 }  // namespace hps

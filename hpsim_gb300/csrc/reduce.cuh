@@ -26,6 +26,37 @@ struct MaxComb {  // MaxR2PhiReduceKernel starts from 0 (beam_kernel.cu:809-810)
   __device__ static double comb(double a, double b) { return a < b ? b : a; }
 };
 
+// Total of the per-block partials, taken by the last block: thread t combines
+// blocks t, t + blockDim, ... in order (independent loads, so the sweep runs
+// at memory parallelism rather than one L2 round trip per block), then the
+// lanes by a fixed shuffle tree and the warps in order.
+template <class C, int K>
+__device__ inline void combine_partials(const double *part, uint32_t nb, double (*sm)[K], double *tot) {
+  double v[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = C::ident();
+  for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = C::comb(v[k], __ldcg(part + (size_t)b * K + k));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x = C::comb(x, __shfl_down_sync(0xffffffffu, x, off));
+    if (lane == 0) sm[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double x = C::ident();
+    for (int w = 0; w < kBlock / 32; ++w) x = C::comb(x, sm[w][threadIdx.x]);
+    tot[threadIdx.x] = x;
+  }
+  __syncthreads();
+}
+
 // Op must provide:
 //   static constexpr int K;            number of accumulators (<= 32)
 //   using Comb = SumComb | MaxComb;
@@ -66,12 +97,7 @@ __global__ void __launch_bounds__(kBlock) pass_kernel(Op op, uint32_t n, PassScr
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  if (threadIdx.x < K) {
-    double v = C::ident();
-    for (uint32_t b = 0; b < gridDim.x; ++b) v = C::comb(v, __ldcg(scr.part + b * K + threadIdx.x));
-    tot[threadIdx.x] = v;
-  }
-  __syncthreads();
+  combine_partials<C, K>(scr.part, gridDim.x, sm, tot);
   op.finalize(tot, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) *scr.counter = 0u;
@@ -80,6 +106,75 @@ __global__ void __launch_bounds__(kBlock) pass_kernel(Op op, uint32_t n, PassScr
 template <class Op>
 inline void launch_pass(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s) {
   pass_kernel<Op><<<pass_blocks(n), kBlock, 0, s>>>(op, n, scr);
+}
+
+// Same scheme for FP32 particle state: each thread accumulates its particles
+// in FP32 and the warp tree runs in FP32 (FP64 arithmetic on GB300 runs at
+// 1/64 of the FP32 rate, so per-particle FP64 sums would dominate); warps,
+// blocks and the finaliser combine in FP64.  Op::particle takes float
+// accumulators and the constants Op::setup() returns (offsets of device-side
+// averages from the synchronous particle), computed once per block: FP64
+// arithmetic per thread would cost more than the sweep itself.
+template <class Op>
+__global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
+  constexpr int K = Op::K;
+  using C = typename Op::Comb;
+  if (!op.enabled()) return;
+  __shared__ double sm[kBlock / 32][K];
+  __shared__ double tot[K];
+  __shared__ int is_last;
+  __shared__ typename Op::Ctx sctx;
+  if (threadIdx.x == 0) sctx = op.setup();
+  __syncthreads();
+  const typename Op::Ctx ctx = sctx;
+  float acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) op.particle(i, acc, ctx);
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float v = acc[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      float o = __shfl_down_sync(0xffffffffu, v, off);
+      v = (float)C::comb(v, o);
+    }
+    if (lane == 0) sm[warp][k] = (double)v;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double v = C::ident();
+    for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, sm[w][threadIdx.x]);
+    scr.part[blockIdx.x * K + threadIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  combine_partials<C, K>(scr.part, gridDim.x, sm, tot);
+  op.finalize(tot, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (threadIdx.x == 0) *scr.counter = 0u;
+}
+
+template <class Op>
+inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s) {
+  pass_kernel_f<Op><<<pass_blocks(n), kBlock, 0, s>>>(op, n, scr);
+}
+
+// FP32 version of rel_phase for offsets that are already small
+__device__ inline float rel_phase_f(float d) {
+  const float pi = 3.14159265358979323846f, twopi = 6.28318530717958647692f;
+  float tmp = d + pi;
+  float sign = 1.0f;
+  if (tmp < 0.0f) { sign = -1.0f; tmp = -tmp; }
+  if (tmp < twopi) return sign * (tmp - pi);
+  return sign * (fmodf(tmp, twopi) - pi);
 }
 
 // wrap(phi - ref) as UpdateRelativePhiKernel, beam_kernel.cu:1507-1525

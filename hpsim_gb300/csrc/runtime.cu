@@ -64,10 +64,13 @@ struct hps_beam_s {
   DevBeam d{};
   PassScratch scr{};
   // device snapshots for Save/Restore (slot 0 initial, 1 intermediate)
-  double *save[2][6] = {};
+  void *save[2][6] = {};
   uint32_t *save_loss[2] = {}, *save_lloss[2] = {};
   double save_design_w[2] = {}, save_freq[2] = {}, save_current[2] = {};
+  double save_phi_ref[2] = {}, save_w_ref[2] = {};
   bool saved[2] = {false, false};
+  // FP32 beams: 6 x n doubles on the device for host <-> device conversion
+  double *stage = nullptr;
 };
 
 struct hps_beamline_s {
@@ -93,6 +96,7 @@ struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
   // host state after the range
   double design_w, wavelen, beam_freq, beam_current, beam_design_w, fraction, interval;
+  double phi_ref, w_ref;  // synchronous particle of an FP32 beam
   uint32_t ccl_cell_num, cur_id;
   int prev_end;
   uint64_t nkernels = 0;  // kernels in the captured graph
@@ -131,6 +135,18 @@ struct hps_sim_s {
 namespace {
 
 bool valid(hps_beam_t b) { return b != nullptr && b->d.loss != nullptr; }
+bool f32(hps_beam_t b) { return b->prec == HPS_PREC_FP32; }
+size_t esize(hps_beam_t b) { return f32(b) ? sizeof(float) : sizeof(double); }
+// the six coordinate arrays of the beam's own precision
+void *coord_ptr(hps_beam_t b, int k) {
+  const DevBeam &d = b->d;
+  if (f32(b)) {
+    float *p[] = {d.fx, d.fxp, d.fy, d.fyp, d.fphi, d.fw, d.fphi_r};
+    return p[k];
+  }
+  double *p[] = {d.x, d.xp, d.y, d.yp, d.phi, d.w, d.phi_r};
+  return p[k];
+}
 
 hps_status sync(hps_beam_t b) {
   CK(cudaStreamSynchronize(b->stream));
@@ -144,16 +160,32 @@ hps_status dmalloc(T **p, size_t n) {
   return HPS_OK;
 }
 
+hps_status stage_alloc(hps_beam_t b) {
+  if (b->stage) return HPS_OK;
+  return dmalloc(&b->stage, (size_t)b->n * 6);
+}
+
 hps_status upload(hps_beam_t b, const double *x, const double *xp, const double *y, const double *yp,
                   const double *phi, const double *w, const uint32_t *loss, const uint32_t *lloss) {
   size_t nd = (size_t)b->n * sizeof(double), nu = (size_t)b->n * sizeof(uint32_t);
   cudaStream_t s = b->stream;
-  CK(cudaMemcpyAsync(b->d.x, x, nd, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(b->d.xp, xp, nd, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(b->d.y, y, nd, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(b->d.yp, yp, nd, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(b->d.phi, phi, nd, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(b->d.w, w, nd, cudaMemcpyHostToDevice, s));
+  const double *src[6] = {x, xp, y, yp, phi, w};
+  if (f32(b)) {
+    // FP64 host arrays -> staging -> FP32 offsets from particle 0's phase
+    // and energy (the reference particle)
+    hps_status e = stage_alloc(b);
+    if (e) return e;
+    const double *dst[6];
+    for (int k = 0; k < 6; ++k) {
+      dst[k] = b->stage + (size_t)k * b->n;
+      CK(cudaMemcpyAsync((void *)dst[k], src[k], nd, cudaMemcpyHostToDevice, s));
+    }
+    b->d.phi_ref = b->n ? phi[0] : 0.0;
+    b->d.w_ref = b->n ? w[0] : 0.0;
+    beam32_from_double(b->d, dst, s);
+  } else {
+    for (int k = 0; k < 6; ++k) CK(cudaMemcpyAsync(coord_ptr(b, k), src[k], nd, cudaMemcpyHostToDevice, s));
+  }
   if (loss) CK(cudaMemcpyAsync(b->d.loss, loss, nu, cudaMemcpyHostToDevice, s));
   else CK(cudaMemsetAsync(b->d.loss, 0, nu, s));
   if (lloss) CK(cudaMemcpyAsync(b->d.lloss, lloss, nu, cudaMemcpyHostToDevice, s));
@@ -167,7 +199,8 @@ __global__ void k_copy_phi_avg(DevBeam b) { b.st->st[PHI_AVG_GOOD] = b.st->st[PH
 
 hps_status init_phi_avg_good(hps_beam_t b) {
   beam_update_loss(b->d, b->scr, b->stream);
-  beam_update_avg(b->d, HPS_COORD_PHI, 0, b->scr, b->stream);
+  if (f32(b)) beam32_update_avg(b->d, HPS_COORD_PHI, 0, b->scr, b->stream);
+  else beam_update_avg(b->d, HPS_COORD_PHI, 0, b->scr, b->stream);
   k_copy_phi_avg<<<1, 1, 0, b->stream>>>(b->d);
   note_launch();
   return last_launch_status("init_phi_avg_good");
@@ -208,20 +241,27 @@ hps_status hps_beam_create(uint32_t num, double mass, double charge, double curr
                            hps_beam_t *out) {
   if (!out) return fail(HPS_ERR_INVALID, "hps_beam_create: null output");
   *out = nullptr;
-  if (precision != HPS_PREC_FP64) return fail(HPS_ERR_UNSUPPORTED, "hps_beam_create: precision not built");
+  if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32)
+    return fail(HPS_ERR_UNSUPPORTED, "hps_beam_create: unknown precision");
   hps_beam_t b = new hps_beam_s();
   b->n = num; b->mass = mass; b->charge = charge; b->current = current; b->prec = precision;
   ref_launch(num, &b->grid_size, &b->blck_size);
-  hps_status s;
+  hps_status s = HPS_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete b; return fail(HPS_ERR_CUDA, cudaGetErrorString(e)); }
   DevBeam &d = b->d;
   d.n = num; d.mass = mass; d.charge = charge;
-  if ((s = dmalloc(&d.x, num)) || (s = dmalloc(&d.xp, num)) || (s = dmalloc(&d.y, num)) ||
-      (s = dmalloc(&d.yp, num)) || (s = dmalloc(&d.phi, num)) || (s = dmalloc(&d.phi_r, num)) ||
-      (s = dmalloc(&d.w, num)) || (s = dmalloc(&d.loss, num)) || (s = dmalloc(&d.lloss, num)) ||
-      (s = dmalloc(&d.st, 1)) || (s = dmalloc(&b->scr.part, (size_t)kMaxPassBlocks * 32)) ||
-      (s = dmalloc(&b->scr.counter, 1))) {
+  if (precision == HPS_PREC_FP64) {
+    if ((s = dmalloc(&d.x, num)) || (s = dmalloc(&d.xp, num)) || (s = dmalloc(&d.y, num)) ||
+        (s = dmalloc(&d.yp, num)) || (s = dmalloc(&d.phi, num)) || (s = dmalloc(&d.phi_r, num)) ||
+        (s = dmalloc(&d.w, num))) {}
+  } else {
+    if ((s = dmalloc(&d.fx, num)) || (s = dmalloc(&d.fxp, num)) || (s = dmalloc(&d.fy, num)) ||
+        (s = dmalloc(&d.fyp, num)) || (s = dmalloc(&d.fphi, num)) || (s = dmalloc(&d.fphi_r, num)) ||
+        (s = dmalloc(&d.fw, num))) {}
+  }
+  if (s || (s = dmalloc(&d.loss, num)) || (s = dmalloc(&d.lloss, num)) || (s = dmalloc(&d.st, 1)) ||
+      (s = dmalloc(&b->scr.part, (size_t)kMaxPassBlocks * 32)) || (s = dmalloc(&b->scr.counter, 1))) {
     hps_beam_destroy(b);
     return s;
   }
@@ -233,7 +273,9 @@ hps_status hps_beam_destroy(hps_beam_t b) {
   if (!b) return HPS_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   DevBeam &d = b->d;
-  void *ptrs[] = {d.x, d.xp, d.y, d.yp, d.phi, d.phi_r, d.w, d.loss, d.lloss, d.st, b->scr.part, b->scr.counter};
+  void *ptrs[] = {d.x,   d.xp,  d.y,   d.yp,     d.phi,  d.phi_r, d.w,    d.fx,          d.fxp,
+                  d.fy,  d.fyp, d.fphi, d.fphi_r, d.fw,   d.loss,  d.lloss, d.st, b->scr.part,
+                  b->scr.counter, b->stage};
   for (void *p : ptrs) if (p) cudaFree(p);
   for (int s = 0; s < 2; ++s) {
     for (int k = 0; k < 6; ++k) if (b->save[s][k]) cudaFree(b->save[s][k]);
@@ -260,12 +302,8 @@ hps_status hps_beam_set_distribution(hps_beam_t b, const double *x, const double
   if (s) return s;
   // the reference particle sits on axis (beam.cpp:344-358)
   if (b->n) {
-    double z = 0.0;
     uint32_t u = 0;
-    CK(cudaMemcpyAsync(b->d.x, &z, 8, cudaMemcpyHostToDevice, b->stream));
-    CK(cudaMemcpyAsync(b->d.xp, &z, 8, cudaMemcpyHostToDevice, b->stream));
-    CK(cudaMemcpyAsync(b->d.y, &z, 8, cudaMemcpyHostToDevice, b->stream));
-    CK(cudaMemcpyAsync(b->d.yp, &z, 8, cudaMemcpyHostToDevice, b->stream));
+    for (int k = 0; k < 4; ++k) CK(cudaMemsetAsync(coord_ptr(b, k), 0, esize(b), b->stream));
     if (loss) CK(cudaMemcpyAsync(b->d.loss, &u, 4, cudaMemcpyHostToDevice, b->stream));
     if (lloss) CK(cudaMemcpyAsync(b->d.lloss, &u, 4, cudaMemcpyHostToDevice, b->stream));
     CK(cudaStreamSynchronize(b->stream));  // the scalars above live on this stack frame
@@ -361,8 +399,14 @@ hps_status hps_beam_set_dc(hps_beam_t b, const double t[6], double r_dphi, doubl
 
 hps_status hps_beam_get_coord(hps_beam_t b, int coord, double *out) {
   if (!valid(b) || !out || coord < 0 || coord > HPS_COORD_PHI_R) return fail(HPS_ERR_INVALID, "get_coord: bad argument");
-  double *src[] = {b->d.x, b->d.xp, b->d.y, b->d.yp, b->d.phi, b->d.w, b->d.phi_r};
-  CK(cudaMemcpyAsync(out, src[coord], (size_t)b->n * 8, cudaMemcpyDeviceToHost, b->stream));
+  if (f32(b)) {
+    hps_status e = stage_alloc(b);
+    if (e) return e;
+    beam32_to_double(b->d, coord, b->stage, b->stream);
+    CK(cudaMemcpyAsync(out, b->stage, (size_t)b->n * 8, cudaMemcpyDeviceToHost, b->stream));
+  } else {
+    CK(cudaMemcpyAsync(out, coord_ptr(b, coord), (size_t)b->n * 8, cudaMemcpyDeviceToHost, b->stream));
+  }
   return sync(b);
 }
 
@@ -375,13 +419,18 @@ hps_status hps_beam_get_loss(hps_beam_t b, int longitudinal, uint32_t *out) {
 
 hps_status hps_beam_save(hps_beam_t b, int slot) {
   if (!valid(b) || slot < 0 || slot > 1) return fail(HPS_ERR_INVALID, "save: bad argument");
-  double *src[6] = {b->d.x, b->d.xp, b->d.y, b->d.yp, b->d.phi, b->d.w};
-  size_t nd = (size_t)b->n * 8, nu = (size_t)b->n * 4;
+  size_t nd = (size_t)b->n * esize(b), nu = (size_t)b->n * 4;
   hps_status s;
   for (int k = 0; k < 6; ++k) {
-    if (!b->save[slot][k] && (s = dmalloc(&b->save[slot][k], b->n))) return s;
-    CK(cudaMemcpyAsync(b->save[slot][k], src[k], nd, cudaMemcpyDeviceToDevice, b->stream));
+    if (!b->save[slot][k]) {
+      unsigned char *p = nullptr;
+      if ((s = dmalloc(&p, nd))) return s;
+      b->save[slot][k] = p;
+    }
+    CK(cudaMemcpyAsync(b->save[slot][k], coord_ptr(b, k), nd, cudaMemcpyDeviceToDevice, b->stream));
   }
+  b->save_phi_ref[slot] = b->d.phi_ref;
+  b->save_w_ref[slot] = b->d.w_ref;
   if (!b->save_loss[slot] && (s = dmalloc(&b->save_loss[slot], b->n))) return s;
   if (!b->save_lloss[slot] && (s = dmalloc(&b->save_lloss[slot], b->n))) return s;
   CK(cudaMemcpyAsync(b->save_loss[slot], b->d.loss, nu, cudaMemcpyDeviceToDevice, b->stream));
@@ -398,16 +447,23 @@ hps_status hps_beam_save(hps_beam_t b, int slot) {
 hps_status hps_beam_restore(hps_beam_t b, int slot) {
   if (!valid(b) || slot < 0 || slot > 1) return fail(HPS_ERR_INVALID, "restore: bad argument");
   if (!b->saved[slot]) return fail(HPS_ERR_STATE, "restore: no beam has been saved in this slot");
-  double *dst[6] = {b->d.x, b->d.xp, b->d.y, b->d.yp, b->d.phi, b->d.w};
-  size_t nd = (size_t)b->n * 8, nu = (size_t)b->n * 4;
-  for (int k = 0; k < 6; ++k) CK(cudaMemcpyAsync(dst[k], b->save[slot][k], nd, cudaMemcpyDeviceToDevice, b->stream));
+  size_t nd = (size_t)b->n * esize(b), nu = (size_t)b->n * 4;
+  for (int k = 0; k < 6; ++k)
+    CK(cudaMemcpyAsync(coord_ptr(b, k), b->save[slot][k], nd, cudaMemcpyDeviceToDevice, b->stream));
   CK(cudaMemcpyAsync(b->d.loss, b->save_loss[slot], nu, cudaMemcpyDeviceToDevice, b->stream));
   CK(cudaMemcpyAsync(b->d.lloss, b->save_lloss[slot], nu, cudaMemcpyDeviceToDevice, b->stream));
   b->design_w = b->save_design_w[slot];
   b->freq = b->save_freq[slot];
   b->current = b->save_current[slot];
-  beam_update_avg(b->d, HPS_COORD_PHI, 1, b->scr, b->stream);
-  beam_update_relative_phi(b->d, 1, b->stream);
+  b->d.phi_ref = b->save_phi_ref[slot];
+  b->d.w_ref = b->save_w_ref[slot];
+  if (f32(b)) {
+    beam32_update_avg(b->d, HPS_COORD_PHI, 1, b->scr, b->stream);
+    beam32_update_relative_phi(b->d, 1, b->stream);
+  } else {
+    beam_update_avg(b->d, HPS_COORD_PHI, 1, b->scr, b->stream);
+    beam_update_relative_phi(b->d, 1, b->stream);
+  }
   hps_status s = last_launch_status("restore");
   if (s) return s;
   return sync(b);
@@ -415,17 +471,29 @@ hps_status hps_beam_restore(hps_beam_t b, int slot) {
 
 hps_status hps_beam_set_ref_w(hps_beam_t b, double w) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
-  beam_set_ref(b->d, HPS_COORD_W, w, b->stream);
+  if (f32(b)) beam32_set_ref(b->d, HPS_COORD_W, w, b->stream);
+  else beam_set_ref(b->d, HPS_COORD_W, w, b->stream);
   b->design_w = w;
   return sync(b);
 }
 hps_status hps_beam_set_ref_phi(hps_beam_t b, double phi) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
-  beam_set_ref(b->d, HPS_COORD_PHI, phi, b->stream);
+  if (f32(b)) beam32_set_ref(b->d, HPS_COORD_PHI, phi, b->stream);
+  else beam_set_ref(b->d, HPS_COORD_PHI, phi, b->stream);
   return sync(b);
 }
 hps_status hps_beam_get_ref(hps_beam_t b, double *w, double *phi) {
   if (!valid(b) || b->n == 0) return fail(HPS_ERR_INVALID, "bad beam handle");
+  if (f32(b)) {
+    float fw = 0.f, fp = 0.f;
+    CK(cudaMemcpyAsync(&fw, b->d.fw, 4, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaMemcpyAsync(&fp, b->d.fphi, 4, cudaMemcpyDeviceToHost, b->stream));
+    hps_status s = sync(b);
+    if (s) return s;
+    if (w) *w = b->d.w_ref + (double)fw;
+    if (phi) *phi = b->d.phi_ref + (double)fp;
+    return HPS_OK;
+  }
   if (w) CK(cudaMemcpyAsync(w, b->d.w, 8, cudaMemcpyDeviceToHost, b->stream));
   if (phi) CK(cudaMemcpyAsync(phi, b->d.phi, 8, cudaMemcpyDeviceToHost, b->stream));
   return sync(b);
@@ -451,17 +519,23 @@ hps_status hps_beam_get_scalar(hps_beam_t b, int which, double *out) {
 hps_status hps_beam_update(hps_beam_t b, int op, int coord, int good) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
   const DevBeam &d = b->d;
+  if ((op == 3 || op == 4) && (coord < 0 || coord > HPS_COORD_PHI_R))
+    return fail(HPS_ERR_INVALID, "beam_update: bad coordinate");
+  const bool f = f32(b);
   switch (op) {
     case 0: beam_update_loss(d, b->scr, b->stream); break;
-    case 1: beam_update_longitudinal_loss(d, b->scr, b->stream); break;
+    case 1: f ? beam32_update_longitudinal_loss(d, b->scr, b->stream)
+              : beam_update_longitudinal_loss(d, b->scr, b->stream); break;
     case 2: beam_update_good_count(d, b->scr, b->stream); break;
-    case 3: beam_update_avg(d, coord, good, b->scr, b->stream); break;
-    case 4: beam_update_sig(d, coord, good, b->scr, b->stream); break;
-    case 5: beam_update_emittance(d, b->scr, b->stream); break;
-    case 6: beam_update_relative_phi(d, good, b->stream); break;
-    case 7: beam_update_stat_for_sc(d, b->scr, b->stream); break;
-    case 8: beam_update_avg_xy(d, b->scr, b->stream); break;
-    case 9: beam_update_max_r_phi(d, b->scr, b->stream); break;
+    case 3: f ? beam32_update_avg(d, coord, good, b->scr, b->stream)
+              : beam_update_avg(d, coord, good, b->scr, b->stream); break;
+    case 4: f ? beam32_update_sig(d, coord, good, b->scr, b->stream)
+              : beam_update_sig(d, coord, good, b->scr, b->stream); break;
+    case 5: f ? beam32_update_emittance(d, b->scr, b->stream) : beam_update_emittance(d, b->scr, b->stream); break;
+    case 6: f ? beam32_update_relative_phi(d, good, b->stream) : beam_update_relative_phi(d, good, b->stream); break;
+    case 7: f ? beam32_update_stat_for_sc(d, b->scr, b->stream) : beam_update_stat_for_sc(d, b->scr, b->stream); break;
+    case 8: f ? beam32_update_avg_xy(d, b->scr, b->stream) : beam_update_avg_xy(d, b->scr, b->stream); break;
+    case 9: f ? beam32_update_max_r_phi(d, b->scr, b->stream) : beam_update_max_r_phi(d, b->scr, b->stream); break;
     default: return fail(HPS_ERR_INVALID, "beam_update: unknown op");
   }
   hps_status s = last_launch_status("beam_update");
@@ -487,7 +561,8 @@ hps_status hps_beam_apply_cut(hps_beam_t b, char coord, double lo, double hi) {
   char c = (char)std::tolower((unsigned char)coord);
   int k = c == 'x' ? HPS_COORD_X : c == 'y' ? HPS_COORD_Y : c == 'w' ? HPS_COORD_W : c == 'p' ? HPS_COORD_PHI : -1;
   if (k < 0) return HPS_OK;  // the reference leaves the beam untouched
-  beam_apply_cut(b->d, k, lo, hi, b->stream);
+  if (f32(b)) beam32_apply_cut(b->d, k, lo, hi, b->stream);
+  else beam_apply_cut(b->d, k, lo, hi, b->stream);
   hps_status s = last_launch_status("apply_cut");
   if (s) return s;
   return sync(b);
@@ -495,7 +570,8 @@ hps_status hps_beam_apply_cut(hps_beam_t b, char coord, double lo, double hi) {
 
 hps_status hps_beam_translate(hps_beam_t b, int coord, double v) {
   if (!valid(b) || coord < 0 || coord > HPS_COORD_W) return fail(HPS_ERR_INVALID, "translate: bad argument");
-  beam_shift(b->d, coord, v, b->stream);
+  if (f32(b)) beam32_shift(b->d, coord, v, b->stream);
+  else beam_shift(b->d, coord, v, b->stream);
   if (coord == HPS_COORD_PHI) {  // Beam::ShiftPhi re-initialises <phi>_good
     hps_status s = init_phi_avg_good(b);
     if (s) return s;
@@ -509,7 +585,8 @@ hps_status hps_beam_monitor(hps_beam_t b, double *out) {
   if (!valid(b) || !out) return fail(HPS_ERR_INVALID, "monitor: bad argument");
   double *dm = nullptr;
   CK(cudaMalloc((void **)&dm, HPS_NMON * sizeof(double)));
-  beam_monitor(b->d, nullptr, dm, 0, b->scr, b->stream);
+  if (f32(b)) beam32_monitor(b->d, nullptr, dm, 0, b->scr, b->stream);
+  else beam_monitor(b->d, nullptr, dm, 0, b->scr, b->stream);
   cudaMemcpyAsync(out, dm, HPS_NMON * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
   hps_status s = sync(b);
   cudaFree(dm);
@@ -585,12 +662,18 @@ static hps_status scheff_alloc_tables(hps_scheff_t s) {
   if (s->t.bin_fx) cudaFree(s->t.bin_fx);
   if (s->t.fld1) cudaFree(s->t.fld1);
   if (s->t.fld2) cudaFree(s->t.fld2);
+  if (s->t.ffld1) cudaFree(s->t.ffld1);
+  if (s->t.ffld2) cudaFree(s->t.ffld2);
+  if (s->t.c32) cudaFree(s->t.c32);
   s->t = ScTables{};
   hps_status st;
   size_t nx = s->nx_max, nz = s->nz_max;
   if ((st = dmalloc(&s->t.bin_fx, nx * nz))) return st;
   if ((st = dmalloc(&s->t.fld1, (nx + 1) * nx * nz * 2))) return st;
   if ((st = dmalloc(&s->t.fld2, (nz + 1) * (nx + 1) * 2))) return st;
+  if ((st = dmalloc(&s->t.ffld1, (nx + 1) * nx * nz * 2))) return st;
+  if ((st = dmalloc(&s->t.ffld2, (nz + 1) * (nx + 1) * 2))) return st;
+  if ((st = dmalloc(&s->t.c32, 1))) return st;
   sc_configure(nx * nz * sizeof(unsigned long long));
   return HPS_OK;
 }
@@ -619,6 +702,9 @@ hps_status hps_scheff_destroy(hps_scheff_t s) {
   if (s->t.bin_fx) cudaFree(s->t.bin_fx);
   if (s->t.fld1) cudaFree(s->t.fld1);
   if (s->t.fld2) cudaFree(s->t.fld2);
+  if (s->t.ffld1) cudaFree(s->t.ffld1);
+  if (s->t.ffld2) cudaFree(s->t.ffld2);
+  if (s->t.c32) cudaFree(s->t.c32);
   delete s;
   return HPS_OK;
 }
@@ -720,9 +806,20 @@ void sc_apply(Ctx &c, double length) {
   a.deposit_ok = (b->blck_size / 4) > 0;
   a.stats_ok = b->n > 2;
   a.deposit_smem = (size_t)c.sc->nx_max * c.sc->nz_max * sizeof(unsigned long long);
-  PHASE(HPS_PROF_SC_STATS, sc_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
-  PHASE(HPS_PROF_SC_MESH, sc_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
-  PHASE(HPS_PROF_SC_KICK, sc_kick(b->d, c.sc->d, c.sc->t, a, b->stream));
+  a.nx_max = c.sc->nx_max;
+  a.nz_max = c.sc->nz_max;
+  if (f32(b)) {
+    sc32_configure();
+    PHASE(HPS_PROF_SC_STATS, sc32_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+    PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+    PHASE(HPS_PROF_SC_KICK, sc32_kick(b->d, c.sc->d, c.sc->t, a, b->stream));
+    return;
+  }
+  ScTables t = c.sc->t;
+  t.ffld2 = nullptr;  // FP64 beams use fld2
+  PHASE(HPS_PROF_SC_STATS, sc_stats(b->d, c.sc->d, t, a, b->scr, b->stream));
+  PHASE(HPS_PROF_SC_MESH, sc_mesh(b->d, c.sc->d, t, a, b->scr, b->stream));
+  PHASE(HPS_PROF_SC_KICK, sc_kick(b->d, c.sc->d, t, a, b->stream));
 }
 
 // PrepSimulateRFGap, simulation_engine.cu:163-175
@@ -732,9 +829,18 @@ void prep_gap(Ctx &c, const GapArgs &g) {
     c.s->wavelen = CLIGHT / g.frequency;
     double ratio = g.frequency / b->freq;
     b->current *= g.frequency / b->freq;
-    PHASE(HPS_PROF_OTHER, beam_change_frequency(b->d, ratio, b->scr, b->stream));
+    if (f32(b)) PHASE(HPS_PROF_OTHER, beam32_change_frequency(b->d, ratio, b->scr, b->stream));
+    else PHASE(HPS_PROF_OTHER, beam_change_frequency(b->d, ratio, b->scr, b->stream));
     b->freq = g.frequency;
   }
+}
+
+void monitor_at(Ctx &c, uint32_t i) {
+  hps_beam_t b = c.b;
+  const ScState *sc = (c.s->sc_on && c.sc) ? c.sc->d : nullptr;
+  double *dst = c.s->mon_dev + (size_t)i * HPS_NMON;
+  if (f32(b)) PHASE(HPS_PROF_MONITOR, beam32_monitor(b->d, sc, dst, i, b->scr, b->stream));
+  else PHASE(HPS_PROF_MONITOR, beam_monitor(b->d, sc, dst, i, b->scr, b->stream));
 }
 
 // the element visitors of simulation_engine.cu:125-373
@@ -743,7 +849,8 @@ hps_status visit(Ctx &c, uint32_t i) {
   hps_beam_t b = c.b;
   hps_beamline_t bl = c.bl;
   const double *p = P(bl, i);
-  const DevBeam &d = b->d;
+  DevBeam &d = b->d;
+  const bool f = f32(b);
   cudaStream_t st = b->stream;
   uint32_t eid = s->cur_id;
   switch (bl->types[i]) {
@@ -753,18 +860,24 @@ hps_status visit(Ctx &c, uint32_t i) {
       if (s->sc_on && c.sc) nk = (int)std::ceil(length / c.sc->interval);
       double hf = 0.5 * length / nk;
       for (int k = 0; k < nk; ++k) {
-        PHASE(HPS_PROF_DRIFT, push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
+        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st)
+                                : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
         sc_apply(c, 2.0 * hf);
-        PHASE(HPS_PROF_DRIFT, push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
+        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st)
+                                : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
       }
       break;
     }
     case HPS_ELEM_QUAD:
       if (b->blck_size / 2 > 0)
-        PHASE(HPS_PROF_QUAD, push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
+        PHASE(HPS_PROF_QUAD,
+              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st)
+                : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       sc_apply(c, p[HPS_P_LENGTH]);
       if (b->blck_size / 2 > 0)
-        PHASE(HPS_PROF_QUAD, push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
+        PHASE(HPS_PROF_QUAD,
+              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st)
+                : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       break;
     case HPS_ELEM_RFGAP_DTL: {
       GapArgs g;
@@ -793,9 +906,9 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.ccl_cell_num = 0;
       s->wavelen = CLIGHT / g.frequency;  // d_wavelen written by the first-half kernel
       g.wl = s->wavelen;
-      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, push_gap_first(d, g, st));
+      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st) : push_gap_first(d, g, st));
       sc_apply(c, g.length);
-      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP2, push_gap_second(d, g, st));
+      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st) : push_gap_second(d, g, st));
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
       break;
@@ -830,18 +943,18 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.wl = s->wavelen;
       g.phi_in = phi_in;
       g.ccl_cell_num = 0;
-      if (gcb > 0) PHASE(HPS_PROF_GAP1, push_gap_first(d, g, st));
+      if (gcb > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st) : push_gap_first(d, g, st));
       sc_apply(c, g.length);
       g.phi_in = phi_out;
       g.ccl_cell_num = s->ccl_cell_num;
-      if (gcb > 0) PHASE(HPS_PROF_GAP2, push_gap_second(d, g, st));
+      if (gcb > 0) PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st) : push_gap_second(d, g, st));
       s->ccl_cell_num++;
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
       break;
     }
     case HPS_ELEM_ROTATION:
-      PHASE(HPS_PROF_OTHER, push_rotation(d, p[HPS_P_ROT_ANGLE], st));
+      PHASE(HPS_PROF_OTHER, f ? push32_rotation(d, p[HPS_P_ROT_ANGLE], st) : push_rotation(d, p[HPS_P_ROT_ANGLE], st));
       break;
     case HPS_ELEM_SPCHCOMP:
       if (s->sc_on && c.sc) c.sc->fraction = p[HPS_P_SPC_FRACTION];
@@ -849,28 +962,36 @@ hps_status visit(Ctx &c, uint32_t i) {
     case HPS_ELEM_APERTURE_C:
     case HPS_ELEM_APERTURE_R:
       if (p[HPS_P_APT_IN] == 0.0) break;
-      PHASE(HPS_PROF_OTHER, beam_update_loss(d, b->scr, st); beam_update_avg_xy(d, b->scr, st);
-                            push_aperture(d, bl->types[i] == HPS_ELEM_APERTURE_R, p, eid, st));
+      PHASE(HPS_PROF_OTHER, beam_update_loss(d, b->scr, st);
+            f ? beam32_update_avg_xy(d, b->scr, st) : beam_update_avg_xy(d, b->scr, st);
+            f ? push32_aperture(d, bl->types[i] == HPS_ELEM_APERTURE_R, p, eid, st)
+              : push_aperture(d, bl->types[i] == HPS_ELEM_APERTURE_R, p, eid, st));
       break;
     case HPS_ELEM_DIAGNOSTICS:
       break;
     case HPS_ELEM_STEERER: {
       double blh = p[HPS_P_STR_BLH], blv = p[HPS_P_STR_BLV];
-      if (blh > 1e-10 || blv > 1e-10) PHASE(HPS_PROF_OTHER, push_steerer(d, blh, blv, st));
+      if (blh > 1e-10 || blv > 1e-10)
+        PHASE(HPS_PROF_OTHER, f ? push32_steerer(d, blh, blv, st) : push_steerer(d, blh, blv, st));
       break;
     }
     case HPS_ELEM_BUNCHER: {
       if (p[HPS_P_BUN_ON] == 0.0) break;
       double bf = p[HPS_P_BUN_FREQ];
       s->wavelen = CLIGHT / bf;
-      PHASE(HPS_PROF_OTHER, push_buncher(d, s->wavelen, s->design_w, bf, p[HPS_P_BUN_VOLTAGE], p[HPS_P_BUN_PHASE],
-                                         p[HPS_P_APERTURE], bf / b->freq, eid, st));
+      PHASE(HPS_PROF_OTHER,
+            f ? push32_buncher(d, s->wavelen, s->design_w, bf, p[HPS_P_BUN_VOLTAGE], p[HPS_P_BUN_PHASE],
+                               p[HPS_P_APERTURE], bf / b->freq, eid, st)
+              : push_buncher(d, s->wavelen, s->design_w, bf, p[HPS_P_BUN_VOLTAGE], p[HPS_P_BUN_PHASE],
+                             p[HPS_P_APERTURE], bf / b->freq, eid, st));
       break;
     }
     case HPS_ELEM_DIPOLE:
-      if (b->blck_size / 4 > 0) PHASE(HPS_PROF_OTHER, push_dipole(d, p, s->wavelen, 0, st));
+      if (b->blck_size / 4 > 0)
+        PHASE(HPS_PROF_OTHER, f ? push32_dipole(d, p, s->wavelen, 0, st) : push_dipole(d, p, s->wavelen, 0, st));
       sc_apply(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE]);
-      if (b->blck_size / 4 > 0) PHASE(HPS_PROF_OTHER, push_dipole(d, p, s->wavelen, 1, st));
+      if (b->blck_size / 4 > 0)
+        PHASE(HPS_PROF_OTHER, f ? push32_dipole(d, p, s->wavelen, 1, st) : push_dipole(d, p, s->wavelen, 1, st));
       break;
     default:
       return fail(HPS_ERR_LATTICE, "unknown element type");
@@ -886,9 +1007,7 @@ hps_status run_range(Ctx &c, int start_index, int end_index, bool monitor) {
       s->cur_id = (uint32_t)i;
       hps_status st = visit(c, (uint32_t)i);
       if (st) return st;
-      if (monitor)
-        PHASE(HPS_PROF_MONITOR, beam_monitor(c.b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr,
-                                             s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i, c.b->scr, c.b->stream));
+      if (monitor) monitor_at(c, (uint32_t)i);
     }
   }
   return last_launch_status("simulate");
@@ -1042,6 +1161,10 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
     key = mixd(key, b->design_w);
     key = mixd(key, c.sc ? c.sc->fraction : 0.0);
     key = mixd(key, c.sc ? c.sc->interval : 0.0);
+    // FP32 beams: the synchronous particle the launch parameters derive from
+    key = mix(key, (uint64_t)b->prec);
+    key = mixd(key, b->d.phi_ref);
+    key = mixd(key, b->d.w_ref);
     key |= 1ull;
   }
   CK(cudaEventRecord(s->ev0, st));
@@ -1050,6 +1173,7 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
     CK(cudaGraphLaunch(g.exec, st));
     s->design_w = g.design_w; s->wavelen = g.wavelen; s->ccl_cell_num = g.ccl_cell_num; s->cur_id = g.cur_id;
     b->freq = g.beam_freq; b->current = g.beam_current; b->design_w = g.beam_design_w;
+    b->d.phi_ref = g.phi_ref; b->d.w_ref = g.w_ref;
     if (c.sc) { c.sc->fraction = g.fraction; c.sc->interval = g.interval; }
     note_launch((int)g.nkernels);  // a replay launches the captured kernels again
   } else if (graph) {
@@ -1070,6 +1194,7 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
     g.key = key;
     g.design_w = s->design_w; g.wavelen = s->wavelen; g.ccl_cell_num = s->ccl_cell_num; g.cur_id = s->cur_id;
     g.beam_freq = b->freq; g.beam_current = b->current; g.beam_design_w = b->design_w;
+    g.phi_ref = b->d.phi_ref; g.w_ref = b->d.w_ref;
     g.fraction = c.sc ? c.sc->fraction : 0.0;
     g.interval = c.sc ? c.sc->interval : 0.0;
     CK(cudaGraphLaunch(g.exec, st));
@@ -1079,9 +1204,7 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
         s->cur_id = (uint32_t)i;
         hps_status e = visit(c, (uint32_t)i);
         if (e) return e;
-        if (monitor)
-          PHASE(HPS_PROF_MONITOR, beam_monitor(b->d, (s->sc_on && c.sc) ? c.sc->d : nullptr,
-                                               s->mon_dev + (size_t)i * HPS_NMON, (uint32_t)i, b->scr, st));
+        if (monitor) monitor_at(c, (uint32_t)i);
         if (host_sync) {
           ScState h;
           CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));

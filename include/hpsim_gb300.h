@@ -193,6 +193,11 @@ hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const 
  * race. */
 hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins_dev, const double *mesh,
                                     double *field_dev, void *stream);
+/* hps_scheff_field through the kernels FP32 beams use (FP32 Green's table
+ * and contraction); same arguments, field returned as doubles.  No
+ * counterpart in the reference: it exposes the FP32 solver's table stage so
+ * that its error against the FP64 table can be stated. */
+hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field);
 
 /* ---- Simulator (src/simulation/inc/simulation_engine.h) ----------------- */
 /* SimulationEngine::InitEngine, simulation_engine.cpp:408-427 (scheff may be NULL) */

@@ -1,0 +1,141 @@
+"""FP32 particle path against the reference's own results (golden fixtures)
+and the FP64 oracle.
+
+FP32 beams keep x, x', y, y' in FP32 and phi, W as FP32 offsets from a
+synchronous particle advanced in FP64 on the host.  Stated tolerances:
+  * loss and longitudinal-loss flags: exact (hence transmission exact);
+  * rms emittances: relative error <= 1e-3 (the stated accuracy target),
+    with an absolute floor of 1e-3 sigma sigma' for collapsed planes (a
+    plane of two particles has emittance 0, and the difference of products
+    that forms it carries sqrt(FP32 epsilon) sigma sigma' of noise);
+  * rms sizes: relative error <= 1e-4;
+  * centroids (x, x', y, y', phi_r, W): |error| <= 1e-4 sigma of that
+    coordinate;
+  * particle 0's energy and phase: relative error <= 1e-6.
+Measured errors on the fixtures and on 165 DTL gaps are below 6e-5 for
+emittances and 1e-5 for sizes and centroids."""
+import numpy as np
+import pytest
+
+from tests import golden_cases as G
+from tests.gpu_runs import COORDS, run_gpu
+
+pytestmark = pytest.mark.gpu
+CASES = G.case_names()
+
+# monitor columns (include/hps_layout.h)
+COUNTS = (0, 1)
+CENTROIDS = {2: 3, 4: 5, 7: 8, 9: 10, 12: 13, 14: 15}  # avg column -> its sigma column
+SIGMAS = (3, 5, 8, 10, 13, 15)
+EMITS = {6: (3, 5), 11: (8, 10), 16: (13, 15)}
+SYNC = (17, 18)
+
+
+def fp32_monitor_errors(m, ref):
+    """Largest error of each group of monitor quantities, in the units the
+    tolerances are stated in."""
+    m, ref = np.asarray(m, float), np.asarray(ref, float)
+    out = {"counts": float(np.max(np.abs(m[:, COUNTS] - ref[:, COUNTS])))}
+    e = 0.0
+    for a, s in CENTROIDS.items():
+        sig = np.abs(ref[:, s])
+        ok = sig > 0
+        if ok.any():
+            e = max(e, float(np.max(np.abs(m[ok, a] - ref[ok, a]) / sig[ok])))
+    out["centroid"] = e
+    e = 0.0
+    for s in SIGMAS:
+        ok = np.abs(ref[:, s]) > 0
+        if ok.any():
+            e = max(e, float(np.max(np.abs(m[ok, s] - ref[ok, s]) / np.abs(ref[ok, s]))))
+    out["sigma"] = e
+    e = 0.0
+    for c, (s1, s2) in EMITS.items():
+        floor = 1e-3 * np.abs(ref[:, s1] * ref[:, s2])
+        d = np.abs(np.nan_to_num(m[:, c]) - np.nan_to_num(ref[:, c]))
+        rel = np.where(d <= floor, 0.0, d / np.maximum(np.abs(ref[:, c]), 1e-300))
+        e = max(e, float(np.max(rel)))
+    out["emittance"] = e
+    out["sync"] = float(np.max(np.abs(m[:, SYNC] - ref[:, SYNC]) / np.maximum(np.abs(ref[:, SYNC]), 1e-300)))
+    return out
+
+
+def assert_fp32_close(m, ref, what):
+    e = fp32_monitor_errors(m, ref)
+    assert e["counts"] == 0, (what, e)
+    assert e["centroid"] <= 1e-4, (what, e)
+    assert e["sigma"] <= 1e-4, (what, e)
+    assert e["emittance"] <= 1e-3, (what, e)
+    assert e["sync"] <= 1e-6, (what, e)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_matches_reference_fixture(name):
+    z, meta = G.load(name)
+    elems = G.elems_of(z, meta)
+    mon, c, _ = run_gpu(elems, meta["n"], spch=meta["spch"], seed=meta["seed"], twiss=tuple(meta["twiss"]),
+                        w0=meta["w0"], phi0=meta["phi0"], freq=meta["freq"], precision="fp32")
+    assert np.array_equal(c["loss"], z["loss"]), (name, np.flatnonzero(c["loss"] != z["loss"])[:10])
+    assert np.array_equal(c["lloss"], z["lloss"]), name
+    assert_fp32_close(mon, z["mon"], name)
+    alive = z["loss"] == 0
+    for k in COORDS:  # per particle: FP32 rounding of O(1e-6) relative to the spread
+        a, b = c[k][alive], z[k][alive]
+        spread = np.std(b) if b.size > 1 else 1.0
+        assert np.max(np.abs(a - b), initial=0.0) <= 1e-4 * max(spread, 1e-12) + 1e-6 * np.max(np.abs(b), initial=0.0), k
+
+
+def test_fp32_dtl_165_gaps_matches_oracle(oracle):
+    """The full DTL-like lattice (165 gaps, 331 elements, SCHEFF 32 x 128 at
+    every gap and quad) with 32768 particles: transmission exact against the
+    FP64 oracle, statistics at every element within the stated tolerances."""
+    from hpsim_gb300 import lattices as L
+    elems = L.dtl_like()
+    mon, c, _ = run_gpu(elems, 32768, spch=dict(nr=32, nz=128), precision="fp32")
+    mo, co = oracle.run(elems, 32768, spch_args=(32, 128, 0.01, 0))
+    assert np.array_equal(c["loss"], co["loss"])
+    assert np.array_equal(c["lloss"], co["lloss"])
+    assert_fp32_close(mon, mo, "dtl165")
+
+
+def test_fp32_ccl_matches_oracle(oracle):
+    from hpsim_gb300 import lattices as L
+    elems = L.ccl_like(modules=1, tanks=8)
+    mon, c, _ = run_gpu(elems, 8192, spch=dict(nr=32, nz=128), w0=100.0, freq=805.0, precision="fp32")
+    mo, co = oracle.run(elems, 8192, spch_args=(32, 128, 0.01, 0), w0=100.0, freq=805.0)
+    assert np.array_equal(c["loss"], co["loss"])
+    assert np.array_equal(c["lloss"], co["lloss"])
+    assert_fp32_close(mon, mo, "ccl")
+
+
+def test_fp32_graph_replay_is_bit_identical():
+    from hpsim_gb300 import lattices as L
+    elems = L.small_fodo()
+    spch = dict(nr=32, nz=128, interval=0.1, remesh_threshold=0.0)
+    _, a, _ = run_gpu(elems, 20000, spch=spch, graph=True, monitor=False, precision="fp32")
+    _, b, _ = run_gpu(elems, 20000, spch=spch, graph=False, monitor=False, precision="fp32")
+    _, c, _ = run_gpu(elems, 20000, spch=spch, graph=True, monitor=False, precision="fp32")
+    for k in COORDS + ("loss", "lloss"):
+        assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(a[k], c[k]), k
+
+
+def test_fp32_restore_and_replay():
+    """Save the initial beam, simulate, restore, simulate again (graph
+    replay with the synchronous particle restored): identical results."""
+    from hpsim_gb300 import HPSim, lattices as L
+    elems = L.dtl_like(n_gaps=12)
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=8192, precision="fp32")
+    beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 7)
+    beam.set_ref_w(0.75)
+    beam.set_ref_phi(0.0)
+    beam.save_initial_beam()
+    sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=elems), HPSim.SpaceCharge(32, 128))
+    sim.simulate()
+    first = {k: beam._coord(k) for k in COORDS}
+    w_end = beam.get_ref_w()
+    beam.restore_initial_beam()
+    sim.simulate()
+    for k in COORDS:
+        assert np.array_equal(beam._coord(k), first[k]), k
+    assert beam.get_ref_w() == w_end

@@ -38,3 +38,41 @@ def test_field_table_32x128_against_oracle(oracle):
     oracle.lib().orc_scheff_contract(s.h)
     _, _, ref = s.tables()
     assert np.allclose(f, ref, rtol=1e-9, atol=1e-12 * np.abs(ref).max())
+
+
+def field_f32(nr, nz, bins, mesh):
+    from hpsim_gb300._capi import call, dptr
+    out = np.zeros((nz + 1) * (nr + 1) * 2)
+    call("hps_scheff_field_f32", nr, nz, dptr(np.ascontiguousarray(bins)), dptr(np.ascontiguousarray(mesh)),
+         dptr(out))
+    return out
+
+
+def _close_per_component(f, ref, tol):
+    """|error| <= tol * max|E| for E_r and E_z separately."""
+    for c in (0, 1):
+        a, b = f[c::2], ref[c::2]
+        assert np.max(np.abs(a - b)) <= tol * np.max(np.abs(b)), (c, np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def test_field_f32_matches_reference():
+    """FP32 Green's table and contraction against the reference's FP64
+    charge -> field pair: |error| <= 2e-5 of the largest field component."""
+    z = np.load(f"{G.GOLDEN}/scheff_tables_8x64.npz")
+    f = field_f32(8, 64, z["bin"], z["mesh"])
+    _close_per_component(f, z["fld2"], 2e-5)
+    assert f[-2:].tolist() == [0.0, 0.0]
+
+
+@pytest.mark.parametrize("adj", [0, 2])
+def test_field_f32_32x128_against_fp64(adj):
+    """A bunched (Gaussian in r and z) charge table on 32 x 128, with and
+    without adjacent-bunch images: FP32 table stage within 2e-5 of the
+    largest component of the FP64 one."""
+    nr, nz = 32, 128
+    r = (np.arange(nr) + 0.5) / nr
+    zz = (np.arange(nz) + 0.5) / nz - 0.5
+    q = np.exp(-(zz[:, None] / 0.15) ** 2 - (r[None, :] / 0.3) ** 2) * 2 * np.pi * r[None, :] * 5000
+    bins = np.round(q * 2 ** 20) / 2 ** 20
+    mesh = np.array([4.0e-4, 2.0e-4, 0.05, 201.25, 65536, 1.6e-5, float(adj)])
+    _close_per_component(field_f32(nr, nz, bins.ravel(), mesh), field(nr, nz, bins.ravel(), mesh), 2e-5)
