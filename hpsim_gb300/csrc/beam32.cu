@@ -32,8 +32,6 @@ __host__ __device__ inline double anchor(const DevBeam &b, int c) {
   return c == HPS_COORD_PHI ? b.phi_ref : c == HPS_COORD_W ? b.w_ref : 0.0;
 }
 
-__device__ inline bool alive(const DevBeam &b, uint32_t i) { return b.loss[i] == 0u; }
-__device__ inline bool good(const DevBeam &b, uint32_t i) { return (uint32_t)(b.loss[i] + b.lloss[i]) == 0u; }
 __device__ inline double surv(const DevBeam &b) { return (double)(uint32_t)(b.n - b.st->num_loss); }
 
 __device__ inline int avg_slot(int c, int g) {
@@ -65,13 +63,15 @@ struct Op32Moment {
   static constexpr int K = 2;
   using Comb = SumComb;
   using Ctx = NoCtx;
+  struct P { uint32_t lo, ll; float v; };
   DevBeam b;
   int coord, good_only, sigma;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &) const {
-    bool keep = good_only ? good(b, i) : alive(b, i);
-    float v = keep ? fcoord(b, coord)[i] : 0.0f;
+  __device__ P load(uint32_t i) const { return {b.loss[i], good_only ? b.lloss[i] : 0u, fcoord(b, coord)[i]}; }
+  __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &) const {
+    bool keep = (uint32_t)(p.lo + p.ll) == 0u;
+    float v = keep ? p.v : 0.0f;
     a[0] += v;
     a[1] += v * v;
   }
@@ -95,14 +95,16 @@ struct Op32Emittance {
   static constexpr int K = 15;
   using Comb = SumComb;
   struct Ctx { float phi0; };
+  struct P { uint32_t lo; float x, xp, y, yp, ph, w; };
   DevBeam b;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {b.fphi[0]}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    float pr = rel_phase_f(b.fphi[i] - c.phi0);
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.fx[i], b.fxp[i], b.fy[i], b.fyp[i], b.fphi[i], b.fw[i]}; }
+  __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
+    float pr = rel_phase_f(p.ph - c.phi0);
     b.fphi_r[i] = pr;
-    if (!alive(b, i)) return;
-    float x = b.fx[i], xp = b.fxp[i], y = b.fy[i], yp = b.fyp[i], w = b.fw[i];
+    if (p.lo != 0u) return;
+    float x = p.x, xp = p.xp, y = p.y, yp = p.yp, w = p.w;
     a[0] += x; a[1] += x * x; a[2] += xp; a[3] += xp * xp; a[4] += x * xp;
     a[5] += y; a[6] += y * y; a[7] += yp; a[8] += yp * yp; a[9] += y * yp;
     a[10] += pr; a[11] += pr * pr; a[12] += w; a[13] += w * w; a[14] += pr * w;
@@ -135,13 +137,15 @@ struct Op32AvgXY {
   static constexpr int K = 2;
   using Comb = SumComb;
   using Ctx = NoCtx;
+  struct P { uint32_t lo; float x, y; };
   DevBeam b;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &) const {
-    if (!alive(b, i)) return;
-    a[0] += b.fx[i];
-    a[1] += b.fy[i];
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.fx[i], b.fy[i]}; }
+  __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &) const {
+    if (p.lo != 0u) return;
+    a[0] += p.x;
+    a[1] += p.y;
   }
   __device__ void finalize(const double *t, int tid, int) const {
     if (tid) return;
@@ -159,11 +163,13 @@ struct Op32MaxRPhi {
   __device__ Ctx setup() const {
     return {(float)b.st->st[X_AVG], (float)b.st->st[Y_AVG], (float)b.st->st[PHI_AVG_R]};
   }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    if (!alive(b, i)) return;
-    float tx = b.fx[i] - c.xa, ty = b.fy[i] - c.ya;
+  struct P { uint32_t lo; float x, y, pr; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.fx[i], b.fy[i], b.fphi_r[i]}; }
+  __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &c) const {
+    if (p.lo != 0u) return;
+    float tx = p.x - c.xa, ty = p.y - c.ya;
     float r2 = tx * tx + ty * ty;
-    float tp = fabsf(b.fphi_r[i] - c.pa);
+    float tp = fabsf(p.pr - c.pa);
     a[0] = fmaxf(a[0], r2);
     a[1] = fmaxf(a[1], tp);
   }
@@ -181,11 +187,13 @@ struct Op32FreqAverages {
   DevBeam b;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {b.fphi[0]}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    float pr = rel_phase_f(b.fphi[i] - c.phi0);
+  struct P { uint32_t lo; float ph; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.fphi[i]}; }
+  __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
+    float pr = rel_phase_f(p.ph - c.phi0);
     b.fphi_r[i] = pr;
-    if (!alive(b, i)) return;
-    a[0] += b.fphi[i];
+    if (p.lo != 0u) return;
+    a[0] += p.ph;
     a[1] += pr;
   }
   __device__ void finalize(const double *t, int tid, int) const {
@@ -205,11 +213,15 @@ struct Op32Monitor {
   uint32_t elem;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {b.fphi[0]}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    if (good(b, i)) a[16] += 1.0f;
-    if (!alive(b, i)) return;
-    float pr = rel_phase_f(b.fphi[i] - c.phi0);
-    float x = b.fx[i], xp = b.fxp[i], y = b.fy[i], yp = b.fyp[i], w = b.fw[i];
+  struct P { uint32_t lo, ll; float x, xp, y, yp, ph, w; };
+  __device__ P load(uint32_t i) const {
+    return {b.loss[i], b.lloss[i], b.fx[i], b.fxp[i], b.fy[i], b.fyp[i], b.fphi[i], b.fw[i]};
+  }
+  __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &c) const {
+    if ((uint32_t)(p.lo + p.ll) == 0u) a[16] += 1.0f;
+    if (p.lo != 0u) return;
+    float pr = rel_phase_f(p.ph - c.phi0);
+    float x = p.x, xp = p.xp, y = p.y, yp = p.yp, w = p.w;
     a[0] += 1.0f;
     a[1] += x; a[2] += x * x; a[3] += xp; a[4] += xp * xp; a[5] += x * xp;
     a[6] += y; a[7] += y * y; a[8] += yp; a[9] += yp * yp; a[10] += y * yp;

@@ -65,6 +65,7 @@ struct ScKickArgs {
   int stats_ok;         // num_particle > 2 (UpdateStatForSpaceCharge runs)
   size_t deposit_smem;  // bytes of the per-block histogram (largest mesh)
   uint32_t nx_max, nz_max;  // largest mesh the solver's tables hold
+  int adj_possible;         // adjacent bunches configured (else r_max never sizes the mesh)
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);

@@ -17,13 +17,18 @@
 
 namespace hps {
 
+// comb() is overloaded for float so that FP32 warp trees stay on the FP32
+// pipes (a float argument promoted to the double overload would run every
+// shuffle step through FP64 arithmetic).
 struct SumComb {
   __device__ static double ident() { return 0.0; }
   __device__ static double comb(double a, double b) { return a + b; }
+  __device__ static float comb(float a, float b) { return a + b; }
 };
 struct MaxComb {  // MaxR2PhiReduceKernel starts from 0 (beam_kernel.cu:809-810)
   __device__ static double ident() { return 0.0; }
   __device__ static double comb(double a, double b) { return a < b ? b : a; }
+  __device__ static float comb(float a, float b) { return a < b ? b : a; }
 };
 
 // Total of the per-block partials, taken by the last block: thread t combines
@@ -111,13 +116,20 @@ inline void launch_pass(const Op &op, uint32_t n, PassScratch scr, cudaStream_t 
 // Same scheme for FP32 particle state: each thread accumulates its particles
 // in FP32 and the warp tree runs in FP32 (FP64 arithmetic on GB300 runs at
 // 1/64 of the FP32 rate, so per-particle FP64 sums would dominate); warps,
-// blocks and the finaliser combine in FP64.  Op::particle takes float
-// accumulators and the constants Op::setup() returns (offsets of device-side
-// averages from the synchronous particle), computed once per block: FP64
-// arithmetic per thread would cost more than the sweep itself.
+// blocks and the finaliser combine in FP64.  Op::setup() returns constants
+// (offsets of device-side averages from the synchronous particle), computed
+// once per block.  A thread takes its particles kPassBatch at a time (2 for
+// ops with many accumulators, to stay within registers): Op::load(i) reads
+// particle i into an Op::P, and Op::use(i, p, acc, ctx)
+// accumulates it (and may write per-particle outputs), so every load of a
+// batch is in flight before the first store.
+constexpr int kPassBatch = 4;
+template <int K> constexpr int pass_batch() { return K > 10 ? 2 : kPassBatch; }
+
 template <class Op>
 __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
   constexpr int K = Op::K;
+  constexpr int B = pass_batch<K>();
   using C = typename Op::Comb;
   if (!op.enabled()) return;
   __shared__ double sm[kBlock / 32][K];
@@ -131,17 +143,26 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = 0.0f;
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) op.particle(i, acc, ctx);
+  for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += B * stride) {
+    typename Op::P p[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const uint32_t i = base + u * stride;
+      if (i < n) p[u] = op.load(i);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const uint32_t i = base + u * stride;
+      if (i < n) op.use(i, p[u], acc, ctx);
+    }
+  }
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     float v = acc[k];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      float o = __shfl_down_sync(0xffffffffu, v, off);
-      v = (float)C::comb(v, o);
-    }
+    for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
     if (lane == 0) sm[warp][k] = (double)v;
   }
   __syncthreads();

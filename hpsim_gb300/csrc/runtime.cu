@@ -808,6 +808,7 @@ void sc_apply(Ctx &c, double length) {
   a.deposit_smem = (size_t)c.sc->nx_max * c.sc->nz_max * sizeof(unsigned long long);
   a.nx_max = c.sc->nx_max;
   a.nz_max = c.sc->nz_max;
+  a.adj_possible = c.sc->adj_bunch != 0;
   if (f32(b)) {
     sc32_configure();
     PHASE(HPS_PROF_SC_STATS, sc32_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
@@ -1042,7 +1043,9 @@ hps_status hps_sim_create(hps_beam_t beam, hps_beamline_t bl, hps_scheff_t schef
 
 hps_status hps_sim_destroy(hps_sim_t s) {
   if (!s) return HPS_OK;
-  if (s->beam) cudaStreamSynchronize(s->beam->stream);
+  // the beam may already be gone (a garbage collector finalises objects in
+  // any order): wait for the device, not for the beam's stream
+  cudaDeviceSynchronize();
   if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
   if (s->mon_dev) cudaFree(s->mon_dev);
   if (s->ev0) cudaEventDestroy(s->ev0);

