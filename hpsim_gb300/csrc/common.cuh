@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/hps_layout.h"
 
 namespace hps {
@@ -28,7 +30,7 @@ enum Stat {
 struct BeamStats {
   double st[NSTAT];
   uint32_t num_loss, num_lloss, num_good;
-  uint32_t pad;
+  uint32_t sc_redo;  // FP32 beams: the fused SCHEFF statistics sweep must be repeated
 };
 
 // Particle storage.  FP64 beams use the double arrays; FP32 beams use the
@@ -143,6 +145,14 @@ inline int pass_blocks(uint32_t n) {
   if (b < 1) b = 1;
   if (b > (uint32_t)kMaxPassBlocks) b = kMaxPassBlocks;
   return (int)b;
+}
+
+// kernel<<<grid, block, smem, st>>>(args...) for kernels named through a
+// template parameter
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args &&...args) {
+  kernel<<<grid, block, smem, st>>>(std::forward<Args>(args)...);
 }
 
 inline int grid_for(uint32_t n) {

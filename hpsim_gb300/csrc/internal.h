@@ -81,17 +81,33 @@ void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
 void sc_green(const ScState *sc, const ScTables &t, uint32_t num_part, double cur_ov_mc2, cudaStream_t st);
 
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
+// An element map fused with the space-charge sweep next to it:
+//  PUSH_GOODPHI     the map, then the good count and <phi>_good of the new
+//                   state (the first statistics sweep of the kick after it);
+//  PUSH_AFTER_KICK  the SCHEFF kick, then the map, in one sweep.
+enum { PUSH_GOODPHI = 1, PUSH_AFTER_KICK = 2 };
+struct PushFuse {
+  int mode;
+  PassScratch scr;      // PUSH_GOODPHI: reduction scratch
+  const ScState *sc;    // PUSH_AFTER_KICK: solver state, tables, skipped set (i & mask == 0)
+  ScTables t;
+  uint64_t skip_mask;
+};
+
 // Launchers that move the synchronous particle update b.phi_ref / b.w_ref.
-void push32_partial_drift(DevBeam &b, double wl, double hf, double aper, uint32_t eid, cudaStream_t st);
-void push32_half_quad(DevBeam &b, double wl, double len, double aper, double grad, uint32_t eid, cudaStream_t st);
+void push32_partial_drift(DevBeam &b, double wl, double hf, double aper, uint32_t eid, cudaStream_t st,
+                          const PushFuse *pf = nullptr);
+void push32_half_quad(DevBeam &b, double wl, double len, double aper, double grad, uint32_t eid, cudaStream_t st,
+                      const PushFuse *pf = nullptr);
 void push32_steerer(DevBeam &b, double blh, double blv, cudaStream_t st);
-void push32_gap_first(DevBeam &b, const GapArgs &g, cudaStream_t st);
-void push32_gap_second(DevBeam &b, const GapArgs &g, cudaStream_t st);
+void push32_gap_first(DevBeam &b, const GapArgs &g, cudaStream_t st, const PushFuse *pf = nullptr);
+void push32_gap_second(DevBeam &b, const GapArgs &g, cudaStream_t st, const PushFuse *pf = nullptr);
 void push32_buncher(DevBeam &b, double wl, double w_ref_design, double freq, double voltage, double phase,
                     double aper, double freq_ratio, uint32_t eid, cudaStream_t st);
 void push32_rotation(DevBeam &b, double angle, cudaStream_t st);
 void push32_aperture(DevBeam &b, int rect, const double *p, uint32_t eid, cudaStream_t st);
-void push32_dipole(DevBeam &b, const double *p, double wl, int second, cudaStream_t st);
+void push32_dipole(DevBeam &b, const double *p, double wl, int second, cudaStream_t st,
+                   const PushFuse *pf = nullptr);
 
 void beam32_update_avg(const DevBeam &b, int coord, int good, PassScratch s, cudaStream_t st);
 void beam32_update_sig(const DevBeam &b, int coord, int good, PassScratch s, cudaStream_t st);
@@ -116,5 +132,10 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                cudaStream_t st);
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
+// the statistics after a PUSH_GOODPHI map: longitudinal-loss test and the
+// SCHEFF moments in one sweep, repeated only when the test flagged a
+// particle (the good set, hence <phi>_good, changed)
+void sc32_stats_after_goodphi(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+                              PassScratch s, cudaStream_t st);
 
 }  // namespace hps

@@ -13,6 +13,8 @@
 // in the same sweep.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace hps {
@@ -126,6 +128,15 @@ inline void launch_pass(const Op &op, uint32_t n, PassScratch scr, cudaStream_t 
 constexpr int kPassBatch = 4;
 template <int K> constexpr int pass_batch() { return K > 10 ? 2 : kPassBatch; }
 
+// An Op with `static constexpr bool kFast = true` has its block and grid
+// partials combined in FP32 (counts stay exact below 2^24 particles); the
+// space-charge statistics that only size the mesh and scale the kick use
+// it, reported beam statistics do not.
+template <class Op, class = void>
+struct op_fast : std::false_type {};
+template <class Op>
+struct op_fast<Op, std::void_t<decltype(Op::kFast)>> : std::integral_constant<bool, Op::kFast> {};
+
 template <class Op>
 __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
   constexpr int K = Op::K;
@@ -158,34 +169,81 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
   }
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if constexpr (op_fast<Op>::value) {
+    // FP32 partials: warps summed in order per block, blocks by warp 0 of
+    // the last block (lane l takes blocks l, l + 32, ...; then a fixed
+    // shuffle tree).  No FP64 arithmetic on the reduction's critical path.
+    __shared__ float smf[kBlock / 32][K];
+    float *partf = (float *)scr.part;
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    float v = acc[k];
+    for (int k = 0; k < K; ++k) {
+      float v = acc[k];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
-    if (lane == 0) sm[warp][k] = (double)v;
+      for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
+      if (lane == 0) smf[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+      float v = 0.0f;
+      for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, smf[w][threadIdx.x]);
+      partf[blockIdx.x * K + threadIdx.x] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    if (warp == 0) {
+      for (int k = 0; k < K; ++k) {
+        float v = 0.0f;
+        for (uint32_t b = lane; b < gridDim.x; b += 32) v = C::comb(v, __ldcg(partf + (size_t)b * K + k));
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
+        if (lane == 0) tot[k] = (double)v;
+      }
+    }
+    __syncthreads();
+  } else {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      float v = acc[k];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
+      if (lane == 0) sm[warp][k] = (double)v;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+      double v = C::ident();
+      for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, sm[w][threadIdx.x]);
+      scr.part[blockIdx.x * K + threadIdx.x] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    combine_partials<C, K>(scr.part, gridDim.x, sm, tot);
   }
-  __syncthreads();
-  if (threadIdx.x < K) {
-    double v = C::ident();
-    for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, sm[w][threadIdx.x]);
-    scr.part[blockIdx.x * K + threadIdx.x] = v;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  combine_partials<C, K>(scr.part, gridDim.x, sm, tot);
   op.finalize(tot, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) *scr.counter = 0u;
 }
 
+// At most two blocks per SM: the last block sums every block's partials in
+// FP64 on one SM (1/64-rate FP64 on GB300), so fewer, fuller blocks keep
+// that tail short; each thread walks more particles in batches instead.
+inline int pass_blocks_f(uint32_t n) {
+  uint32_t b = (n + kPassBatch * kBlock - 1) / (kPassBatch * kBlock);
+  if (b < 1) b = 1;
+  if (b > 2u * 152u) b = 2u * 152u;
+  return (int)b;
+}
+
 template <class Op>
 inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s) {
-  pass_kernel_f<Op><<<pass_blocks(n), kBlock, 0, s>>>(op, n, scr);
+  launch_k(pass_kernel_f<Op>, dim3(pass_blocks_f(n)), dim3(kBlock), 0, s, op, n, scr);
 }
 
 // FP32 version of rel_phase for offsets that are already small

@@ -794,7 +794,33 @@ int T(hps_beamline_t bl, int64_t i) {
   return (i >= 0 && i < (int64_t)bl->types.size()) ? bl->types[i] : 0;
 }
 
-void sc_apply(Ctx &c, double length) {
+// FP32 beams with a solver: the element half before the kick also takes the
+// first statistics sweep (PUSH_GOODPHI), the half after it runs behind the
+// kick in one sweep (PUSH_AFTER_KICK).  Every launch of the unfused
+// sequence is valid from four particles on (blck_size/4 > 0, n > 2).
+struct Fuse32 {
+  bool on;
+  PushFuse pre, post;
+};
+Fuse32 fuse32(Ctx &c) {
+  Fuse32 z{};
+  hps_beam_t b = c.b;
+  const uint64_t stride = (uint64_t)b->grid_size * (b->blck_size / 4);
+  z.on = f32(b) && c.s->sc_on && c.sc && b->n >= 4 && stride != 0 && (stride & (stride - 1)) == 0;
+  if (!z.on) return z;
+  z.pre.mode = PUSH_GOODPHI;
+  z.pre.scr = b->scr;
+  z.post.mode = PUSH_AFTER_KICK;
+  z.post.sc = c.sc->d;
+  z.post.t = c.sc->t;
+  z.post.t.fld2 = nullptr;
+  z.post.skip_mask = stride - 1;
+  return z;
+}
+
+// fused: the statistics after a PUSH_GOODPHI half and the mesh; the kick
+// runs with the next half
+void sc_apply(Ctx &c, double length, bool fused = false) {
   if (!(c.s->sc_on && c.sc)) return;
   hps_beam_t b = c.b;
   ScKickArgs a;
@@ -811,6 +837,11 @@ void sc_apply(Ctx &c, double length) {
   a.adj_possible = c.sc->adj_bunch != 0;
   if (f32(b)) {
     sc32_configure();
+    if (fused) {
+      PHASE(HPS_PROF_SC_STATS, sc32_stats_after_goodphi(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+      PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+      return;
+    }
     PHASE(HPS_PROF_SC_STATS, sc32_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
     PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
     PHASE(HPS_PROF_SC_KICK, sc32_kick(b->d, c.sc->d, c.sc->t, a, b->stream));
@@ -854,6 +885,8 @@ hps_status visit(Ctx &c, uint32_t i) {
   const bool f = f32(b);
   cudaStream_t st = b->stream;
   uint32_t eid = s->cur_id;
+  const Fuse32 z = fuse32(c);
+  const PushFuse *pre = z.on ? &z.pre : nullptr, *post = z.on ? &z.post : nullptr;
   switch (bl->types[i]) {
     case HPS_ELEM_DRIFT: {
       int nk = 1;
@@ -861,10 +894,10 @@ hps_status visit(Ctx &c, uint32_t i) {
       if (s->sc_on && c.sc) nk = (int)std::ceil(length / c.sc->interval);
       double hf = 0.5 * length / nk;
       for (int k = 0; k < nk; ++k) {
-        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st)
+        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, pre)
                                 : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
-        sc_apply(c, 2.0 * hf);
-        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st)
+        sc_apply(c, 2.0 * hf, z.on);
+        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, post)
                                 : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
       }
       break;
@@ -872,12 +905,12 @@ hps_status visit(Ctx &c, uint32_t i) {
     case HPS_ELEM_QUAD:
       if (b->blck_size / 2 > 0)
         PHASE(HPS_PROF_QUAD,
-              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st)
+              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st, pre)
                 : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
-      sc_apply(c, p[HPS_P_LENGTH]);
+      sc_apply(c, p[HPS_P_LENGTH], z.on);
       if (b->blck_size / 2 > 0)
         PHASE(HPS_PROF_QUAD,
-              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st)
+              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st, post)
                 : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       break;
     case HPS_ELEM_RFGAP_DTL: {
@@ -907,9 +940,10 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.ccl_cell_num = 0;
       s->wavelen = CLIGHT / g.frequency;  // d_wavelen written by the first-half kernel
       g.wl = s->wavelen;
-      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st) : push_gap_first(d, g, st));
-      sc_apply(c, g.length);
-      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st) : push_gap_second(d, g, st));
+      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre) : push_gap_first(d, g, st));
+      sc_apply(c, g.length, z.on);
+      if (b->blck_size / 2 > 0)
+        PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
       break;
@@ -944,11 +978,11 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.wl = s->wavelen;
       g.phi_in = phi_in;
       g.ccl_cell_num = 0;
-      if (gcb > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st) : push_gap_first(d, g, st));
-      sc_apply(c, g.length);
+      if (gcb > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre) : push_gap_first(d, g, st));
+      sc_apply(c, g.length, z.on);
       g.phi_in = phi_out;
       g.ccl_cell_num = s->ccl_cell_num;
-      if (gcb > 0) PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st) : push_gap_second(d, g, st));
+      if (gcb > 0) PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
       s->ccl_cell_num++;
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
@@ -989,10 +1023,12 @@ hps_status visit(Ctx &c, uint32_t i) {
     }
     case HPS_ELEM_DIPOLE:
       if (b->blck_size / 4 > 0)
-        PHASE(HPS_PROF_OTHER, f ? push32_dipole(d, p, s->wavelen, 0, st) : push_dipole(d, p, s->wavelen, 0, st));
-      sc_apply(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE]);
+        PHASE(HPS_PROF_OTHER,
+              f ? push32_dipole(d, p, s->wavelen, 0, st, pre) : push_dipole(d, p, s->wavelen, 0, st));
+      sc_apply(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE], z.on);
       if (b->blck_size / 4 > 0)
-        PHASE(HPS_PROF_OTHER, f ? push32_dipole(d, p, s->wavelen, 1, st) : push_dipole(d, p, s->wavelen, 1, st));
+        PHASE(HPS_PROF_OTHER,
+              f ? push32_dipole(d, p, s->wavelen, 1, st, post) : push_dipole(d, p, s->wavelen, 1, st));
       break;
     default:
       return fail(HPS_ERR_LATTICE, "unknown element type");

@@ -5,9 +5,15 @@
 // src/simulation/inc/space_charge_kernel.cu).  Differences:
 //  * statistics sweeps accumulate offsets in FP32 per thread and warp, FP64
 //    across warps and blocks (reduce.cuh: pass_kernel_f);
-//  * the thread that takes the space-charge decision also forms, in FP64,
-//    every constant the FP32 kernels of the kick need (Sc32Consts), so no
-//    particle kernel does FP64 arithmetic (GB300 runs FP64 at 1/64 rate);
+//  * the thread that takes the space-charge decision also forms every
+//    constant the FP32 kernels of the kick need (Sc32Consts), in FP32
+//    arithmetic from host-side constants, so no particle kernel and no
+//    finaliser does FP64 arithmetic beyond a few adds (GB300 runs FP64 at
+//    1/64 rate, and a dependent FP64 divide costs about a microsecond);
+//  * ahead of a kick on four or more particles, the element half before it
+//    takes the first statistics sweep and the loss test and the moments
+//    share one sweep (Op32LlossScStats); the kick runs inside the element
+//    half after it (push32.cu);
 //  * the deposit keeps a 32-bit fixed-point histogram per block in shared
 //    memory (scale chosen from the block's particle count so that no bin can
 //    overflow) and adds it to the 2^-36 global table as integers, so the
@@ -30,6 +36,7 @@
 #include "../../include/hpsim_gb300.h"
 #include "internal.h"
 #include "reduce.cuh"
+#include "sc32_kick.cuh"
 #include "scheff_common.cuh"
 
 namespace hps {
@@ -70,8 +77,8 @@ __device__ inline void mesh_size32(ScState *s, float beta, float wave_len, float
 
 // Scheff::Start's decision (space_charge.cpp:86-138, as scheff_decide) in
 // FP32 arithmetic; relative-change tests as |a - b| > threshold * b
-__device__ void scheff_decide32(const DevBeam &b, ScState *s, const Sc32Host &h, double freq, double frac) {
-  const BeamStats &st = *b.st;
+__device__ void scheff_decide32(const BeamStats &st, const DevBeam &b, ScState *s, const Sc32Host &h, double freq,
+                                double frac) {
   const uint32_t good_cnt = st.num_good;
   const float sigphi = b.n < 2 ? 0.0f : (float)st.st[PHI_SIG_GOOD];
   const float sigx = b.n < 2 ? 0.0f : (float)st.st[X_SIG_GOOD];
@@ -123,8 +130,8 @@ __device__ void scheff_decide32(const DevBeam &b, ScState *s, const Sc32Host &h,
 // (ApplySpchKickKernel, space_charge_kernel.cu:573-620; UpdateFldTbl1Kernel,
 // :39-60; DistributeParticleKernel, :123-150), once per kick.  The only FP64
 // operation is the offset of the synchronous particle from <W>_good.
-__device__ void sc32_consts(const DevBeam &b, const ScState *s, Sc32Consts *c, const Sc32Host &h) {
-  const BeamStats &st = *b.st;
+__device__ void sc32_consts(const BeamStats &st, const DevBeam &b, const ScState *s, Sc32Consts *c,
+                            const Sc32Host &h) {
   const double ke = st.st[W_AVG_GOOD];
   float gmg, beta;
   sc32_kinematics(ke, h.inv_mass, gmg, beta);
@@ -163,9 +170,23 @@ __device__ void sc32_consts(const DevBeam &b, const ScState *s, Sc32Consts *c, c
   c->green_c1 = h.c1;
 }
 
+// The decision and the kick constants on local copies of the solver state:
+// one burst of loads, one burst of stores, and no load waiting behind a
+// store that might alias it.
+__device__ void sc32_decide_consts(const BeamStats &st, const DevBeam &b, ScState *sc, Sc32Consts *c32,
+                                   const Sc32Host &h, double freq, double frac) {
+  ScState s = *sc;
+  Sc32Consts c;
+  scheff_decide32(st, b, &s, h, freq, frac);
+  sc32_consts(st, b, &s, &c, h);
+  *sc = s;
+  *c32 = c;
+}
+
 // UpdateGoodParticleCount + UpdateAvgPhi(true)
 struct Op32GoodPhi {
   static constexpr int K = 2;
+  static constexpr bool kFast = true;
   using Comb = SumComb;
   using Ctx = NoCtx;
   DevBeam b;
@@ -189,6 +210,7 @@ struct Op32GoodPhi {
 // longitudinal-loss test + lloss count + good count + <phi>_good
 struct Op32LlossGoodPhi {
   static constexpr int K = 3;
+  static constexpr bool kFast = true;
   using Comb = SumComb;
   struct Ctx { float lim; };
   DevBeam b;
@@ -216,10 +238,42 @@ struct Op32LlossGoodPhi {
   }
 };
 
+// The SCHEFF moments from their totals s[0..7] (FP32 arithmetic, see
+// Sc32Host), then, with a solver, the decision and the kick's constants
+// (thread 0); the caller zeroes the tables afterwards.
+__device__ void sc_moments_finish(const DevBeam &b, const double *s, ScState *sc, const ScTables &t, double freq,
+                                  double frac, const Sc32Host &h) {
+  BeamStats st = *b.st;  // local copy, written back once
+  const float isv = 1.0f / (float)(uint32_t)(b.n - st.num_loss), ing = 1.0f / (float)st.num_good;
+  st.st[PHI_AVG_R] = (float)s[0] * isv;
+  const float pa = (float)s[1] * ing, pa2 = (float)s[2] * ing;
+  st.st[PHI_SIG_GOOD] = sqrtf(pa2 - pa * pa);
+  const float xa = (float)s[3] * isv, x2 = (float)s[4] * isv, ya = (float)s[5] * isv, y2 = (float)s[6] * isv;
+  st.st[X_AVG_GOOD] = xa;
+  st.st[X_SIG_GOOD] = sqrtf(x2 - xa * xa);
+  st.st[Y_AVG_GOOD] = ya;
+  st.st[Y_SIG_GOOD] = sqrtf(y2 - ya * ya);
+  st.st[W_AVG_GOOD] = st.num_good > 0 ? (double)((float)s[7] * ing) + b.w_ref : -99999;
+  *b.st = st;
+  if (sc) sc32_decide_consts(st, b, sc, t.c32, h, freq, frac);
+}
+
+// accumulate particle p into the SCHEFF moments (pr: its relative phase)
+__device__ inline void sc_moments_add(float (&a)[12], float pr, uint32_t lo, uint32_t ll, float x, float y, float w) {
+  const float alive = lo == 0u ? 1.0f : 0.0f;
+  const float gd = (lo == 0u && ll == 0u) ? 1.0f : 0.0f;
+  a[0] += alive * pr;
+  a[1] += gd * pr; a[2] += gd * pr * pr;
+  a[3] += gd * x; a[4] += gd * x * x; a[5] += gd * y; a[6] += gd * y * y;
+  a[7] += gd * w;
+}
+
 // relative phase about <phi>_good, the SCHEFF moments, the decision and the
-// kick's constants (as OpScStats in scheff.cu)
+// kick's constants (as OpScStats in scheff.cu).  With redo_only it runs only
+// when the fused sweep below found the good set changed.
 struct Op32ScStats {
   static constexpr int K = 8;
+  static constexpr bool kFast = true;
   using Comb = SumComb;
   struct Ctx { float pag; };
   DevBeam b;
@@ -227,37 +281,25 @@ struct Op32ScStats {
   ScTables t;
   double freq, frac;
   Sc32Host h;
-  __device__ bool enabled() const { return true; }
+  int redo_only;
+  __device__ bool enabled() const { return !redo_only || b.st->sc_redo != 0u; }
   __device__ Ctx setup() const { return {(float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref)}; }
   struct P { uint32_t lo, ll; float ph, x, y, w; };
   __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i], b.fx[i], b.fy[i], b.fw[i]}; }
   __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
-    float pr = rel_phase_f(p.ph - c.pag);
+    const float pr = rel_phase_f(p.ph - c.pag);
     b.fphi_r[i] = pr;
-    float alive = p.lo == 0u ? 1.0f : 0.0f;
-    float gd = (p.lo == 0u && p.ll == 0u) ? 1.0f : 0.0f;
+    const float alive = p.lo == 0u ? 1.0f : 0.0f;
+    const float gd = (p.lo == 0u && p.ll == 0u) ? 1.0f : 0.0f;
     a[0] += alive * pr;
     a[1] += gd * pr; a[2] += gd * pr * pr;
     a[3] += gd * p.x; a[4] += gd * p.x * p.x; a[5] += gd * p.y; a[6] += gd * p.y * p.y;
     a[7] += gd * p.w;
   }
   __device__ void finalize(const double *s, int tid, int nth) const {
-    if (tid == 0) {  // FP32 arithmetic on the FP64 totals (see Sc32Host)
-      BeamStats &st = *b.st;
-      const float isv = 1.0f / (float)(uint32_t)(b.n - st.num_loss), ing = 1.0f / (float)st.num_good;
-      st.st[PHI_AVG_R] = (float)s[0] * isv;
-      const float pa = (float)s[1] * ing, pa2 = (float)s[2] * ing;
-      st.st[PHI_SIG_GOOD] = sqrtf(pa2 - pa * pa);
-      const float xa = (float)s[3] * isv, x2 = (float)s[4] * isv, ya = (float)s[5] * isv, y2 = (float)s[6] * isv;
-      st.st[X_AVG_GOOD] = xa;
-      st.st[X_SIG_GOOD] = sqrtf(x2 - xa * xa);
-      st.st[Y_AVG_GOOD] = ya;
-      st.st[Y_SIG_GOOD] = sqrtf(y2 - ya * ya);
-      st.st[W_AVG_GOOD] = st.num_good > 0 ? (double)((float)s[7] * ing) + b.w_ref : -99999;
-      if (sc) {
-        scheff_decide32(b, sc, h, freq, frac);
-        sc32_consts(b, sc, t.c32, h);
-      }
+    if (tid == 0) {
+      sc_moments_finish(b, s, sc, t, freq, frac, h);
+      b.st->sc_redo = 0u;
     }
     if (!sc) return;
     __syncthreads();
@@ -265,8 +307,72 @@ struct Op32ScStats {
   }
 };
 
+// The longitudinal-loss test (UpdateLongitudinalLossCoordinateKernel with the
+// lloss and good counts and <phi>_good, beam.cpp:780-781, 1008-1009) and the
+// SCHEFF moments in one sweep.  The relative phases are taken about the
+// <phi>_good of the sweep before (fused into the element map ahead of the
+// kick); when the test flags no particle of the good set, that is the
+// <phi>_good the separate sweeps would have used, and the totals are the
+// same ones in the same order.  Otherwise the sweep records the new
+// <phi>_good and asks for the moments sweep again (sc_redo).
+struct Op32LlossScStats {
+  static constexpr int K = 12;
+  static constexpr bool kFast = true;
+  using Comb = SumComb;
+  struct Ctx { float lim, pag; };
+  DevBeam b;
+  ScState *sc;
+  ScTables t;
+  double freq, frac;
+  Sc32Host h;
+  __device__ bool enabled() const { return true; }
+  __device__ Ctx setup() const {
+    const double pag = b.st->st[PHI_AVG_GOOD] - b.phi_ref;
+    return {(float)(pag + TWOPI + PI), (float)pag};
+  }
+  struct P { uint32_t lo, ll; float ph, x, y, w; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i], b.fx[i], b.fy[i], b.fw[i]}; }
+  __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
+    uint32_t ll = p.ll;
+    float newly = 0.0f;
+    if (p.ph > c.lim && ll != 1u) {
+      if (p.lo == 0u && ll == 0u) newly = 1.0f;
+      ll = 1u;
+      b.lloss[i] = 1u;
+    }
+    const float pr = rel_phase_f(p.ph - c.pag);
+    b.fphi_r[i] = pr;
+    sc_moments_add(a, pr, p.lo, ll, p.x, p.y, p.w);
+    const bool g = (uint32_t)(p.lo + ll) == 0u;
+    a[8] += ll != 0u ? 1.0f : 0.0f;
+    a[9] += g ? 1.0f : 0.0f;
+    a[10] += g ? p.ph : 0.0f;
+    a[11] += newly;
+  }
+  __device__ void finalize(const double *s, int tid, int nth) const {
+    __shared__ int redo;
+    if (tid == 0) {
+      BeamStats &st = *b.st;
+      const uint32_t ng = (uint32_t)s[9];
+      st.num_lloss = (uint32_t)s[8];
+      st.num_good = ng;
+      redo = s[11] != 0.0;
+      if (redo) {
+        st.st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)s[10] / (float)ng) + b.phi_ref : -99999;
+        st.sc_redo = 1u;
+      } else {
+        sc_moments_finish(b, s, sc, t, freq, frac, h);
+        st.sc_redo = 0u;
+      }
+    }
+    __syncthreads();
+    if (!redo) zero_mesh_tables(sc, t, tid, nth);
+  }
+};
+
 struct Op32AdjMesh {
   static constexpr int K = 2;
+  static constexpr bool kFast = true;
   using Comb = MaxComb;
   struct Ctx { float xa, ya, pa; };
   DevBeam b;
@@ -288,28 +394,23 @@ struct Op32AdjMesh {
   __device__ void finalize(const double *t, int tid, int) const {
     if (tid) return;
     const float rmax = sqrtf((float)t[0]);
-    b.st->st[R_MAX] = rmax;
-    b.st->st[ABS_PHI_MAX] = t[1];
-    mesh_size32(sc, (float)sc->beta, h.wave_len, rmax, 0.0f, 1.0f);
-    sc32_consts(b, sc, c32, h);
+    BeamStats st = *b.st;
+    st.st[R_MAX] = rmax;
+    st.st[ABS_PHI_MAX] = t[1];
+    *b.st = st;
+    ScState s = *sc;
+    Sc32Consts c;
+    mesh_size32(&s, (float)s.beta, h.wave_len, rmax, 0.0f, 1.0f);
+    sc32_consts(st, b, &s, &c, h);
+    *sc = s;
+    *c32 = c;
   }
 };
 
 __global__ void k32_decide_only(DevBeam b, ScState *sc, ScTables t, double freq, double frac, Sc32Host h) {
-  if (threadIdx.x == 0) {
-    scheff_decide32(b, sc, h, freq, frac);
-    sc32_consts(b, sc, t.c32, h);
-  }
+  if (threadIdx.x == 0) sc32_decide_consts(*b.st, b, sc, t.c32, h, freq, frac);
   __syncthreads();
   zero_mesh_tables(sc, t, threadIdx.x, blockDim.x);
-}
-
-// wrap into [-pi, pi] by whole turns (space_charge_kernel.cu:160-166); the
-// relative phases are already wrapped, so one turn at most is removed
-__device__ inline float wrap_turns(float d) {
-  const float pi = 3.14159265358979323846f, twopi = 6.28318530717958647692f;
-  for (int guard = 0; (d > pi || d < -pi) && guard < 64; ++guard) d += d > 0.0f ? -twopi : twopi;
-  return d;
 }
 
 // ---- Green's table ---------------------------------------------------------
@@ -398,7 +499,7 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
   const Sc32Consts &kc = *t.c32;
   const float phimc = kc.phimc, xbar = kc.xbar, ybar = kc.ybar, epsq = kc.epsq, inv_epsq = kc.inv_epsq;
   const float dr = kc.dr0, dzg = kc.dzg0, inv_dr = kc.inv_dr0, inv_dzg = kc.inv_dzg0, hl = kc.hl0, c2 = kc.c2;
-  const float drdr = dr * dr;
+  const float drdr = dr * dr, inv_drdr = inv_dr * inv_dr;
   const long long m = 1ll << q.shift;
   uint32_t cnt = 0;
   for (uint32_t np = bid * blockDim.x + threadIdx.x; np < bm.n; np += nblk * blockDim.x) {
@@ -420,16 +521,18 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
     int j1 = jm1 + 1;
     if (zz < ((float)jm1 - 0.5f) * dzg) j1 = jm1 - 1;
     j1 = min(max(j1, 1), (int)nz);
+    // area weights in units of dr^2 (rmax^2 - rmin^2 = sqrtmp dr^2), and the
+    // z weight with (jm1 - j1) dz = +-dz
     float a = 1.0f;
     if (i1 != i) {
-      float sqrtmp = sqrtf(4.0f * rsq_sh / drdr - 1.0f);
-      float rminsq = 0.25f * drdr * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
-      float rmaxsq = rminsq + sqrtmp * drdr;
-      if (i1 < i) a = (rmaxsq - (float)((i - 1) * (i - 1)) * drdr) / (rmaxsq - rminsq);
-      else a = ((float)((i1 - 1) * (i1 - 1)) * drdr - rminsq) / (rmaxsq - rminsq);
+      const float sqrtmp = sqrtf(4.0f * rsq_sh * inv_drdr - 1.0f);
+      const float rmin_n = 0.25f * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
+      const float rmax_n = rmin_n + sqrtmp;
+      if (i1 < i) a = __fdividef(rmax_n - (float)((i - 1) * (i - 1)), sqrtmp);
+      else a = __fdividef((float)((i1 - 1) * (i1 - 1)) - rmin_n, sqrtmp);
     }
     float cc = 1.0f;
-    if (j1 != jm1) cc = (zz - ((float)j1 - 0.5f) * dzg) / ((float)(jm1 - j1) * dzg);
+    if (j1 != jm1) cc = (zz - ((float)j1 - 0.5f) * dzg) * (j1 < jm1 ? inv_dzg : -inv_dzg);
     float bb = 1.0f - a, d = 1.0f - cc;
     int k00 = (jm1 - 1) * (int)nx + i - 1, k01 = k00 + (i1 - i);
     int k10 = (j1 - 1) * (int)nx + i - 1, k11 = k10 + (i1 - i);
@@ -535,22 +638,31 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
     if (zp > nz) continue;
     for (uint32_t r = lane; r < ntr; r += 32) {
       const uint32_t rs = rs0 + r;
+      // bins zs * nx + rs >= lim are left out: source rows zs < zend
+      const uint32_t zend = !cut ? nz : (lim > rs ? min(nz, (lim - rs + nx - 1) / nx) : 0u);
       // sources below the point: dz = zp - zs - 1, +E_z
-      const uint32_t zb = min(nz, zp);
+      const uint32_t zb = min(zend, zp);
+      const float *q = qs + r;
+      const float2 *g = gs + r;
+#pragma unroll 4
       for (uint32_t zs = 0; zs < zb; ++zs) {
-        float bv = qs[zs * tr + r];
-        if (cut && zs * nx + rs >= lim) bv = 0.0f;
-        const float2 g = gs[(zp - zs - 1) * tr + r];
-        ax0 = fmaf(bv, g.x, ax0);
-        az0 = fmaf(bv, g.y, az0);
+        const float bv = q[zs * tr];
+        const float2 gv = g[(zp - 1 - zs) * tr];
+        ax0 = fmaf(bv, gv.x, ax0);
+        az0 = fmaf(bv, gv.y, az0);
       }
       // sources at or above it (points zp < nz only): dz = zs - zp, -E_z
-      for (uint32_t zs = zp; zs < nz; ++zs) {
-        float bv = qs[zs * tr + r];
-        if (cut && zs * nx + rs >= lim) bv = 0.0f;
-        const float2 g = gs[(zs - zp) * tr + r];
-        ax1 = fmaf(bv, g.x, ax1);
-        az1 = fmaf(-bv, g.y, az1);
+      if (zp < zend) {
+        const float *q1 = qs + (size_t)zp * tr + r;
+        const float2 *g1 = gs + r;
+        const uint32_t cnt = zend - zp;
+#pragma unroll 4
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const float bv = q1[k * tr];
+          const float2 gv = g1[k * tr];
+          ax1 = fmaf(bv, gv.x, ax1);
+          az1 = fmaf(-bv, gv.y, az1);
+        }
       }
     }
   }
@@ -574,88 +686,13 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
 // launch geometry (NextPow2 grid and block) makes the stride a power of two.
 __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc, ScTables t, RefK r,
                                                   uint64_t skip_mask) {
-  const Sc32Consts &kc = *t.c32;
-  const uint32_t nx = sc->nx, nz = sc->nz, adj = sc->adj;
-  const float cbgcoef = kc.cbg_per_onm * (float)sc->num_on_mesh;
-  const float phimc = kc.phimc, xbar = kc.xbar, ybar = kc.ybar, epsq = kc.epsq, inv_epsq = kc.inv_epsq;
-  const float beta = kc.beta, gmg = kc.gmg, inv_dr = kc.inv_dr, inv_dzg = kc.inv_dzg, hl = kc.hl;
-  const float rmesh = kc.rmesh, c2 = kc.c2, xfac = kc.xfac, yfac = kc.yfac, pl = kc.pl;
-  const float er_c3 = kc.er_c3, ez_c3 = kc.ez_c3, dwc = kc.dwc;
-  const uint32_t tbl_sz = (nx + 1) * (nz + 1);
-  const float2 *fld = (const float2 *)t.ffld2;
-  for (uint32_t indx = blockIdx.x * blockDim.x + threadIdx.x; indx < bm.n; indx += gridDim.x * blockDim.x) {
-    const uint32_t lo = bm.loss[indx], ll = bm.lloss[indx];
-    const float x = bm.fx[indx], y = bm.fy[indx], xp = bm.fxp[indx], yp = bm.fyp[indx];
-    const float phi = bm.fphi_r[indx], dw = bm.fw[indx];
-    if (((uint64_t)indx & skip_mask) == 0 || lo != 0u || ll != 0u) continue;
-    float g = fmaf(dw, r.minv, r.g);
-    float gm = g + 1.0f;
-    float bgz = sqrtf(g * (g + 2.0f));
-    float bgx = bgz * xp, bgy = bgz * yp;
-    // p* = gamma_c (bgz - beta gm) without cancellation
-    float dgc = (dw + dwc) * r.minv;  // gm - gamma_c
-    float s0 = dgc * (gm + gmg) / (gmg * (bgz + beta * gm));
-    float xxbar = x - xbar, yybar = y - ybar;
-    float rr = sqrtf(xxbar * xxbar * inv_epsq + yybar * yybar * epsq);
-    if (rr == 0.0f) rr = 1.0e-8f;
-    float inv_rr = 1.0f / rr;
-    float xovr = xxbar * xfac * inv_rr, yovr = yybar * yfac * inv_rr;
-    float z = -c2 * wrap_turns(phi - phimc);
-    float cbgr, cbgzs;
-    if (rr > rmesh || fabsf(z) > hl) {
-      z = -c2 * (phi - phimc);
-      float d = sqrtf(z * z + rr * rr);
-      float invd3 = 1.0f / (d * d * d);
-      float rod3 = rr * invd3, zod3 = z * invd3;
-      for (uint32_t nb = 1; nb <= adj; ++nb) {
-        float xi = (float)nb;
-        for (int lr = 0; lr < 2; ++lr) {
-          float sft = z + xi * pl;
-          d = sqrtf(sft * sft + rr * rr);
-          invd3 = 1.0f / (d * d * d);
-          rod3 += rr * invd3;
-          zod3 += sft * invd3;
-          xi = -xi;
-        }
-      }
-      cbgr = cbgcoef * rod3;
-      cbgzs = cbgcoef * zod3;
-    } else {
-      float ri = rr * inv_dr;
-      uint32_t i = 1 + (int)ri;
-      float a = ri - (float)(i - 1);
-      float bb = 1.0f - a;
-      float zi = (z + hl) * inv_dzg;
-      uint32_t j = 1 + (int)zi;
-      float c = zi - (float)(j - 1);
-      float d = 1.0f - c;
-      uint32_t l = (j - 1) * (nx + 1) + i;
-      uint32_t m = l + (nx + 1);
-      if (m >= tbl_sz) m = tbl_sz - 1;
-      if (l >= tbl_sz || l < 1) l = tbl_sz - 1;
-      if (m < 1) m = 1;
-      float2 fl = fld[l], fl1 = fld[l - 1], fm = fld[m], fm1 = fld[m - 1];
-      cbgr = er_c3 * (d * (a * fl.x + bb * fl1.x) + c * (a * fm.x + bb * fm1.x));
-      cbgzs = ez_c3 * (d * (a * fl.y + bb * fl1.y) + c * (a * fm.y + bb * fm1.y));
-    }
-    bgx += cbgr * xovr;
-    bgy += cbgr * yovr;
-    // bgzf = gamma_c (p* + dp + beta_c (1 + (p* + dp)^2 / 2)) taken as
-    // bgz + (bgzf - bgz): the change is formed without cancellation and bgz
-    // comes straight from the particle's energy
-    const float s2 = s0 * s0;
-    const float dbgz = gmg * (cbgzs + beta * (0.5f * cbgzs * (2.0f * s0 + cbgzs) +
-                                              s2 * s2 / (4.0f * (1.0f + 0.5f * s2 + sqrtf(1.0f + s2)))));
-    const float bgzf = bgz + dbgz;
-    if (bgzf <= 0.0f) {
-      bm.loss[indx] = 9999u;
-    } else {
-      float inv_f = 1.0f / bgzf;
-      bm.fxp[indx] = bgx * inv_f;
-      bm.fyp[indx] = bgy * inv_f;
-      float w = r.w + dw;
-      bm.fw[indx] = dw + w * (gm + 1.0f) * dbgz / (gm * bgz);
-    }
+  const KickEnv e = kick_env(sc, t, r);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bm.n; i += gridDim.x * blockDim.x) {
+    Part p = load_part(bm, i);
+    const uint32_t ll = bm.lloss[i];
+    const float pr = bm.fphi_r[i];
+    if (((uint64_t)i & skip_mask) == 0 || p.lo != 0u || ll != 0u) continue;
+    store_part(bm, i, p, kick_particle(p, pr, e));
   }
 }
 
@@ -683,7 +720,7 @@ void beam32_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st)
   if (b.n <= 2) return;
   launch_pass_f(Op32GoodPhi{b}, b.n, s, st);
   launch_pass_f(Op32LlossGoodPhi{b}, b.n, s, st);
-  launch_pass_f(Op32ScStats{b, nullptr, ScTables{}, 0.0, 0.0, Sc32Host{}}, b.n, s, st);
+  launch_pass_f(Op32ScStats{b, nullptr, ScTables{}, 0.0, 0.0, Sc32Host{}, 0}, b.n, s, st);
   note_launch(3);
 }
 
@@ -709,12 +746,21 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
   if (a.stats_ok) {
     launch_pass_f(Op32GoodPhi{b}, b.n, s, st);
     launch_pass_f(Op32LlossGoodPhi{b}, b.n, s, st);
-    launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st);
+    launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, h, 0}, b.n, s, st);
     note_launch(3);
   } else {
-    k32_decide_only<<<1, kBlock, 0, st>>>(b, sc, u, a.freq, a.frac, h);
+    launch_k(k32_decide_only, dim3(1), dim3(kBlock), 0, st, b, sc, u, a.freq, a.frac, h);
     note_launch();
   }
+}
+
+void sc32_stats_after_goodphi(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+                              PassScratch s, cudaStream_t st) {
+  ScTables u = tables32(t);
+  const Sc32Host h = host32(b, a);
+  launch_pass_f(Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st);
+  launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, h, 1}, b.n, s, st);
+  note_launch(2);
 }
 
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
@@ -737,10 +783,10 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   // Green's table entries of the largest mesh, one per thread
   const uint32_t ngreen = std::min<uint32_t>(
       (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 4u * 152u);
-  k32_green_deposit<<<ndep + ngreen, kBlock, q.smem ? hb : 0, st>>>(b, sc, u, q, ndep, ngreen);
+  launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
   note_launch();
   dim3 cg(a.nx_max + 1, (a.nz_max + 1 + kCZ - 1) / kCZ);
-  k32_contract<<<cg, kContractThreads, contract_smem(a.nx_max, a.nz_max), st>>>(sc, u);
+  launch_k(k32_contract, cg, dim3(kContractThreads), contract_smem(a.nx_max, a.nz_max), st, (const ScState *)sc, u);
   note_launch();
 }
 
@@ -750,7 +796,8 @@ void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
     set_error(HPS_ERR_STATE, "SCHEFF kick: launch stride is not a power of two");
     return;
   }
-  k32_kick<<<grid_for(b.n), kBlock, 0, st>>>(b, sc, tables32(t), make_refk(b.w_ref, b.mass), a.skip_stride - 1);
+  launch_k(k32_kick, dim3(grid_for(b.n)), dim3(kBlock), 0, st, b, (const ScState *)sc, tables32(t),
+             make_refk(b.w_ref, b.mass), (uint64_t)(a.skip_stride - 1));
   note_launch();
 }
 
