@@ -125,20 +125,41 @@ def make_sim(args, elems, seed):
     return beam, bl, sc, sim
 
 
+# Compulsory bytes per particle of one launch of each profiled kernel class:
+# the particle arrays it must read and write.
+#   FP32 beams with SCHEFF (fused sequence per element):
+#     drift / gap1 half before the kick + first statistics sweep: 6 coordinates
+#       and both loss flags in (32 B), x, y, phi out (12 B);
+#     quad half before the kick: 32 B in, x, x', y, y', phi out (20 B);
+#     sc_stats (loss test + SCHEFF moments): flags, phi, x, y, W in (24 B),
+#       relative phase out (4 B);
+#     sc_mesh (deposit; Green's table and contraction are mesh-sized): flags,
+#       x, y, relative phase in (20 B);
+#     sc_kick (kick + element half after it): 6 coordinates, flags and the
+#       relative phase in (36 B), 6 coordinates out (24 B).
+#   FP64 beams: one kernel per class, 8-byte coordinates.
+ALG_BYTES = {
+    "fp32": {"drift": 44, "gap1": 44, "quad": 52, "sc_stats": 28, "sc_mesh": 20, "sc_kick": 60,
+             "gap2": 2 * 6 * 4 + 4, "other": 2 * 6 * 4 + 8, "monitor": 32},
+    "fp64": {"gap2": 2 * 6 * 8 + 4, "gap1": 6 * 8 + 4 + 3 * 8, "quad": 6 * 8 + 4 + 5 * 8, "drift": 5 * 8 + 4 + 3 * 8,
+             "sc_kick": 6 * 8 + 8 + 3 * 8, "sc_stats": 3 * 8 + 4 * 8 + 8 * 2, "sc_mesh": 3 * 8 + 8,
+             "other": 2 * 6 * 8 + 8, "monitor": 64},
+}
+# Minimum traffic of a particle-element step: one read and write of the six
+# coordinates plus both loss flags read (2 * 6 * s + 8 bytes).
+STEP_BYTES = {"fp32": 56, "fp64": 104}
+PHASE_KERNELS = {
+    "fp32": {"quad": "pass_kernel_f<OpPushGoodPhi<QuadMap>>", "gap1": "pass_kernel_f<OpPushGoodPhi<Gap1Map>>",
+             "drift": "pass_kernel_f<OpPushGoodPhi<DriftMap>>",
+             "sc_stats": "pass_kernel_f<Op32LlossScStats> + pass_kernel_f<Op32ScStats> (runs only on a redo)",
+             "sc_mesh": "k32_green_deposit + k32_contract", "sc_kick": "k32_kick_push<QuadMap|Gap2Map|DriftMap>"},
+    "fp64": {},
+}
+
+
 def algorithmic_bytes(phase, n, prec):
-    """Compulsory bytes per launch of a phase (reads + writes of the
-    particle arrays it must touch)."""
-    f = 8 if prec == "fp64" else 4
-    per = {
-        "gap2": 2 * 6 * f + 4,            # 6 coordinates in and out, loss flag in
-        "gap1": 6 * f + 4 + 3 * f,        # 6 in, x/y/phi out
-        "quad": 6 * f + 4 + 5 * f,        # 6 in, x/xp/y/yp/phi out
-        "drift": 5 * f + 4 + 3 * f,       # x/xp/y/yp/w in, x/y/phi out
-        "sc_kick": 6 * f + 8 + 3 * f,     # x/y/xp/yp/phase/w + 2 flags in, xp/yp/w out
-        "sc_stats": 3 * 8 + 4 * f + 8 * 2,
-        "sc_mesh": 3 * f + 8,
-    }
-    return per.get(phase, 2 * 6 * f + 8) * n
+    """Compulsory bytes of one launch of a profiled kernel class."""
+    return ALG_BYTES[prec].get(phase, STEP_BYTES[prec]) * n
 
 
 def load_peaks():
@@ -281,6 +302,8 @@ def main():
     peak, peak_kind = load_peaks()
     achieved = algorithmic_bytes(dom, args.particles, args.precision) / per_launch_s / 1e9
     traffic = load_traffic(dom, args.precision)
+    # the whole step against the minimum traffic of a particle-element step
+    step_gbs = value / ws * STEP_BYTES[args.precision] / 1e9
 
     # end to end through the public API with host buffers
     e2e = None
@@ -335,9 +358,14 @@ def main():
                    "particles": args.particles, "elements": n_elem, "precision": args.precision,
                    "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write)",
                    "wall_s": wall},
-        "roofline": {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel_phase": dom,
+                     "kernels": PHASE_KERNELS[args.precision].get(dom, dom),
+                     "bytes_per_particle": ALG_BYTES[args.precision].get(dom, STEP_BYTES[args.precision]),
+                     "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "launch_ms": per_launch_s * 1000.0,
+                     "step": {"bytes_per_particle_element": STEP_BYTES[args.precision], "achieved": step_gbs,
+                              "frac": step_gbs / peak},
                      "phases_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()}},
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -887,6 +887,8 @@ hps_status visit(Ctx &c, uint32_t i) {
   uint32_t eid = s->cur_id;
   const Fuse32 z = fuse32(c);
   const PushFuse *pre = z.on ? &z.pre : nullptr, *post = z.on ? &z.post : nullptr;
+  // a half that runs behind the kick is timed as the kick
+  auto post_cls = [&](int cls) { return z.on ? (int)HPS_PROF_SC_KICK : cls; };
   switch (bl->types[i]) {
     case HPS_ELEM_DRIFT: {
       int nk = 1;
@@ -897,7 +899,7 @@ hps_status visit(Ctx &c, uint32_t i) {
         PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, pre)
                                 : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
         sc_apply(c, 2.0 * hf, z.on);
-        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, post)
+        PHASE(post_cls(HPS_PROF_DRIFT), f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, post)
                                 : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
       }
       break;
@@ -909,7 +911,7 @@ hps_status visit(Ctx &c, uint32_t i) {
                 : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       sc_apply(c, p[HPS_P_LENGTH], z.on);
       if (b->blck_size / 2 > 0)
-        PHASE(HPS_PROF_QUAD,
+        PHASE(post_cls(HPS_PROF_QUAD),
               f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st, post)
                 : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       break;
@@ -943,7 +945,7 @@ hps_status visit(Ctx &c, uint32_t i) {
       if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre) : push_gap_first(d, g, st));
       sc_apply(c, g.length, z.on);
       if (b->blck_size / 2 > 0)
-        PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
+        PHASE(post_cls(HPS_PROF_GAP2), f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
       break;
@@ -982,7 +984,7 @@ hps_status visit(Ctx &c, uint32_t i) {
       sc_apply(c, g.length, z.on);
       g.phi_in = phi_out;
       g.ccl_cell_num = s->ccl_cell_num;
-      if (gcb > 0) PHASE(HPS_PROF_GAP2, f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
+      if (gcb > 0) PHASE(post_cls(HPS_PROF_GAP2), f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
       s->ccl_cell_num++;
       s->design_w = g.energy_out;
       b->design_w = s->design_w;
@@ -1027,7 +1029,7 @@ hps_status visit(Ctx &c, uint32_t i) {
               f ? push32_dipole(d, p, s->wavelen, 0, st, pre) : push_dipole(d, p, s->wavelen, 0, st));
       sc_apply(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE], z.on);
       if (b->blck_size / 4 > 0)
-        PHASE(HPS_PROF_OTHER,
+        PHASE(post_cls(HPS_PROF_OTHER),
               f ? push32_dipole(d, p, s->wavelen, 1, st, post) : push_dipole(d, p, s->wavelen, 1, st));
       break;
     default:

@@ -49,8 +49,10 @@ typedef enum hps_status {
  *                  build semantics (SCHEFF bins and fields in FP64).
  *   HPS_PREC_FP32: x, x', y, y' in FP32; phase and energy stored in FP32 as
  *                  offsets from an FP64 synchronous (on-axis) particle tracked
- *                  by the host; SCHEFF tables in FP32; moments accumulated in
- *                  FP64. */
+ *                  by the host; SCHEFF tables in FP32; moments summed in FP32
+ *                  per thread and warp and combined in FP64 (the SCHEFF
+ *                  statistics, which only size the mesh and scale the kick,
+ *                  in FP32 throughout). */
 typedef enum hps_precision { HPS_PREC_FP64 = 0, HPS_PREC_FP32 = 1 } hps_precision;
 
 typedef struct hps_beam_s *hps_beam_t;
@@ -231,8 +233,10 @@ hps_status hps_sim_last_time_ms(hps_sim_t sim, double *ms);
 #define HPS_PROF_OTHER 4     /* buncher, steerer, rotation, apertures, dipoles, frequency changes */
 #define HPS_PROF_SC_STATS 5  /* SCHEFF statistics sweeps + remesh decision */
 #define HPS_PROF_SC_MESH 6   /* Green's table, deposit, contraction */
-#define HPS_PROF_SC_KICK 7   /* SCHEFF kick */
+#define HPS_PROF_SC_KICK 7   /* SCHEFF kick (FP32 beams: kick and the element half after it, one sweep) */
 #define HPS_PROF_MONITOR 8   /* per-element monitor records */
+/* FP32 beams with a solver: the element half before a kick also takes the
+ * first statistics sweep and is timed in its element's class. */
 #define HPS_NPROF 9
 hps_status hps_sim_profile(hps_sim_t sim, int on);
 hps_status hps_sim_profile_read(hps_sim_t sim, double *ms /* HPS_NPROF */, uint64_t *count /* HPS_NPROF */,
