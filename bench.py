@@ -128,18 +128,18 @@ def make_sim(args, elems, seed):
 # Compulsory bytes per particle of one launch of each profiled kernel class:
 # the particle arrays it must read and write.
 #   FP32 beams with SCHEFF (fused sequence per element):
-#     drift / gap1 half before the kick + first statistics sweep: 6 coordinates
-#       and both loss flags in (32 B), x, y, phi out (12 B);
+#     drift / gap1 half before the kick + every statistic of the kick: 6
+#       coordinates and both loss flags in (32 B), x, y, phi out (12 B);
 #     quad half before the kick: 32 B in, x, x', y, y', phi out (20 B);
-#     sc_stats (loss test + SCHEFF moments): flags, phi, x, y, W in (24 B),
-#       relative phase out (4 B);
+#     sc_stats: nothing when the half before the kick certified its
+#       statistics (the loss-test and moments sweeps then return at once);
 #     sc_mesh (deposit; Green's table and contraction are mesh-sized): flags,
-#       x, y, relative phase in (20 B);
-#     sc_kick (kick + element half after it): 6 coordinates, flags and the
-#       relative phase in (36 B), 6 coordinates out (24 B).
+#       x, y, phi in (20 B);
+#     sc_kick (kick + element half after it): 6 coordinates and both flags in
+#       (32 B), 6 coordinates out (24 B).
 #   FP64 beams: one kernel per class, 8-byte coordinates.
 ALG_BYTES = {
-    "fp32": {"drift": 44, "gap1": 44, "quad": 52, "sc_stats": 28, "sc_mesh": 20, "sc_kick": 60,
+    "fp32": {"drift": 44, "gap1": 44, "quad": 52, "sc_stats": 0, "sc_mesh": 20, "sc_kick": 56,
              "gap2": 2 * 6 * 4 + 4, "other": 2 * 6 * 4 + 8, "monitor": 32},
     "fp64": {"gap2": 2 * 6 * 8 + 4, "gap1": 6 * 8 + 4 + 3 * 8, "quad": 6 * 8 + 4 + 5 * 8, "drift": 5 * 8 + 4 + 3 * 8,
              "sc_kick": 6 * 8 + 8 + 3 * 8, "sc_stats": 3 * 8 + 4 * 8 + 8 * 2, "sc_mesh": 3 * 8 + 8,
@@ -149,9 +149,10 @@ ALG_BYTES = {
 # coordinates plus both loss flags read (2 * 6 * s + 8 bytes).
 STEP_BYTES = {"fp32": 56, "fp64": 104}
 PHASE_KERNELS = {
-    "fp32": {"quad": "pass_kernel_f<OpPushGoodPhi<QuadMap>>", "gap1": "pass_kernel_f<OpPushGoodPhi<Gap1Map>>",
-             "drift": "pass_kernel_f<OpPushGoodPhi<DriftMap>>",
-             "sc_stats": "pass_kernel_f<Op32LlossScStats> + pass_kernel_f<Op32ScStats> (runs only on a redo)",
+    "fp32": {"quad": "pass_kernel_f<OpPushScStats<QuadMap>>", "gap1": "pass_kernel_f<OpPushScStats<Gap1Map>>",
+             "drift": "pass_kernel_f<OpPushScStats<DriftMap>>",
+             "sc_stats": "pass_kernel_f<Op32LlossScStats> + pass_kernel_f<Op32ScStats> (sweep only without "
+                         "the certificate)",
              "sc_mesh": "k32_green_deposit + k32_contract", "sc_kick": "k32_kick_push<QuadMap|Gap2Map|DriftMap>"},
     "fp64": {},
 }
@@ -272,6 +273,7 @@ def main():
         flush.zero_()
         step()
     launches0 = HPSim.kernel_launch_count()
+    sweeps0 = sc.get_counter("stat_sweeps")
     barrier()
     dev_ms = []
     wall0 = time.perf_counter()
@@ -283,6 +285,7 @@ def main():
     barrier()
     wall = time.perf_counter() - wall0
     launches = HPSim.kernel_launch_count() - launches0
+    stat_sweeps = (sc.get_counter("stat_sweeps") - sweeps0) / args.steps
     t_step = sum(dev_ms) / len(dev_ms) / 1000.0
     if ws > 1:
         t = torch.tensor([t_step], device=f"cuda:{local}", dtype=torch.float64)
@@ -357,7 +360,8 @@ def main():
                                f"particles, waterbag 0.75 MeV, SCHEFF 32x128 full solve at every element",
                    "particles": args.particles, "elements": n_elem, "precision": args.precision,
                    "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write)",
-                   "wall_s": wall},
+                   "wall_s": wall, "sc_kicks_per_step": n_elem,
+                   "sc_uncertified_kicks_per_step": stat_sweeps},
         "roofline": {"bound": "hbm", "kernel_phase": dom,
                      "kernels": PHASE_KERNELS[args.precision].get(dom, dom),
                      "bytes_per_particle": ALG_BYTES[args.precision].get(dom, STEP_BYTES[args.precision]),

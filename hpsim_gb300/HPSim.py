@@ -513,6 +513,14 @@ class SpaceCharge:
     def set_remesh_threshold(self, v):
         self._set("remesh_threshold", v)
 
+    def get_counter(self, name):
+        """Counters kept on the device (not in the reference's API): 'solves'
+        (field solves since creation) or 'stat_sweeps' (kicks of an FP32 beam
+        whose statistics took the separate loss-test and moments sweeps)."""
+        out = C.c_double()
+        call("hps_scheff_get", self._h, {"solves": 8, "stat_sweeps": 9}[name], C.byref(out))
+        return int(out.value)
+
 
 class Simulator:
     """Simulator(beam=, beamline=, spch=None) (wrap_simulator.cpp:27-54).

@@ -30,7 +30,10 @@ enum Stat {
 struct BeamStats {
   double st[NSTAT];
   uint32_t num_loss, num_lloss, num_good;
-  uint32_t sc_redo;  // FP32 beams: the fused SCHEFF statistics sweep must be repeated
+  // FP32 beams, SCHEFF statistics fused into the element map before a kick:
+  // 0 done; 2 the loss test and the moments sweep still have to run; 1 the
+  // loss test changed the good set and the moments sweep runs again
+  uint32_t sc_redo;
 };
 
 // Particle storage.  FP64 beams use the double arrays; FP32 beams use the
@@ -64,13 +67,17 @@ struct ScState {
   double ratio_r, ratio_z, ratio_q, ratio_g;
   uint32_t n_solves;
   int resized;
+  // FP32 beams: kicks whose statistics the element map before them could not
+  // certify (the loss-test and moments sweeps ran)
+  uint32_t n_stat_sweeps;
 };
 
-// Constants of one FP32 SCHEFF kick, formed once per kick in FP64 by the
+// Constants of one FP32 SCHEFF kick, formed once per kick in FP32 by the
 // thread that takes the space-charge decision, read by every FP32 kernel of
 // the kick (FP64 arithmetic per thread or per block would cost more than the
 // particle sweeps themselves on GB300).
 struct Sc32Consts {
+  float pag;                                            // <phi>_good - phi_sync: relative-phase origin
   float phimc, xbar, ybar, epsq, inv_epsq, xfac, yfac;  // bunch centre and aspect
   float beta, gmg, c2, pl;                              // bunch-frame kinematics
   float dr, dzg, inv_dr, inv_dzg, hl, rmesh;            // mesh as seen by the kick (ratio-scaled)
@@ -79,6 +86,18 @@ struct Sc32Consts {
   float er_c3, ez_c3;                                   // interpolated-field scale
   float dwc;                                            // synchronous particle - bunch-frame energy
   float green_c1;                                       // Green's table scale
+};
+
+// Host-side constants of one FP32 kick.  The statistics finalisers run on
+// one thread; on GB300 an FP64 divide or square root there costs about a
+// microsecond, so FP32 beams take the space-charge decision and form the
+// kick's constants in FP32 arithmetic from these (FP64 state fields are kept
+// for the solver's memory).
+struct Sc32Host {
+  float inv_mass;   // 1 / m
+  float wave_len;   // c / f of the beam
+  float c1;         // 5721.67 I frac / (f 1e6 N m): Green's table and far-field scale
+  float length;     // kick length
 };
 
 struct ScTables {

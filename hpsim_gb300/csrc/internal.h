@@ -82,16 +82,21 @@ void sc_green(const ScState *sc, const ScTables &t, uint32_t num_part, double cu
 
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
 // An element map fused with the space-charge sweep next to it:
-//  PUSH_GOODPHI     the map, then the good count and <phi>_good of the new
-//                   state (the first statistics sweep of the kick after it);
+//  PUSH_SCSTATS     the map, then every statistic of the kick after it from
+//                   the new state, the decision and the kick's constants,
+//                   when the sweep can certify them (else sc_redo = 2 and
+//                   sc32_stats_after_push completes them);
 //  PUSH_AFTER_KICK  the SCHEFF kick, then the map, in one sweep.
-enum { PUSH_GOODPHI = 1, PUSH_AFTER_KICK = 2 };
+enum { PUSH_SCSTATS = 1, PUSH_AFTER_KICK = 2 };
 struct PushFuse {
   int mode;
-  PassScratch scr;      // PUSH_GOODPHI: reduction scratch
-  const ScState *sc;    // PUSH_AFTER_KICK: solver state, tables, skipped set (i & mask == 0)
+  PassScratch scr;      // PUSH_SCSTATS: reduction scratch
+  ScState *sc;          // solver state and tables
   ScTables t;
-  uint64_t skip_mask;
+  uint64_t skip_mask;   // PUSH_AFTER_KICK: skipped set (i & mask == 0)
+  Sc32Host h;           // PUSH_SCSTATS: host constants, beam frequency, fraction
+  double freq, frac;
+  int s_last;           // PUSH_SCSTATS: a kick of this simulation call came before
 };
 
 // Launchers that move the synchronous particle update b.phi_ref / b.w_ref.
@@ -132,10 +137,13 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                cudaStream_t st);
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
-// the statistics after a PUSH_GOODPHI map: longitudinal-loss test and the
-// SCHEFF moments in one sweep, repeated only when the test flagged a
-// particle (the good set, hence <phi>_good, changed)
-void sc32_stats_after_goodphi(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
-                              PassScratch s, cudaStream_t st);
+// the statistics after a PUSH_SCSTATS map that could not certify its own:
+// the longitudinal-loss test and the SCHEFF moments in one sweep, repeated
+// only when the test flagged a particle (the good set, hence <phi>_good,
+// changed).  Both sweeps return at once when they are not needed.
+void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+                           PassScratch s, cudaStream_t st);
+// constants of the FP32 kernels of a kick
+Sc32Host sc32_host(const DevBeam &b, const ScKickArgs &a);
 
 }  // namespace hps

@@ -6,16 +6,23 @@
 // after a DTL) and energies never pass through FP32.  Each launcher forms
 // its element's map (push32_maps.cuh) from the synchronous particle before
 // the element, moves the synchronous particle, and launches the map in one
-// of three forms: alone; followed by the good count and <phi>_good of the
-// new state (the first statistics sweep of the space-charge kick that
-// follows); or preceded by the space-charge kick (sc32_kick.cuh), so that a
-// kick and the element half after it are one sweep over the particles.
+// of three forms: alone; followed by the statistics of the space-charge
+// kick that follows, taken from the new state in the same sweep; or preceded
+// by the space-charge kick (sc32_kick.cuh), so that a kick and the element
+// half after it are one sweep over the particles.
+//
+// Lost particles keep their absolute phase and energy (the reference's
+// kernels skip them): every sweep moves their offsets against the
+// synchronous particle's step through the element.
+#include <algorithm>
 #include <cmath>
+#include <unordered_map>
 
 #include "internal.h"
 #include "push32_maps.cuh"
 #include "reduce.cuh"
 #include "sc32_kick.cuh"
+#include "sc32_stats.cuh"
 
 namespace hps {
 
@@ -28,41 +35,154 @@ double beta_of(double w, double mass) {
   return sqrt(gm1 * (gm1 + 2.0)) / (gm1 + 1.0);
 }
 
+// the synchronous particle's step through an element, in FP32
+struct Shift {
+  float dph, dw;
+};
+
+// offsets of a lost particle after the element: absolute phase and energy kept
+__device__ inline uint32_t keep_lost(Part &p, uint32_t w, const Shift &s) {
+  if (s.dph != 0.0f) { p.ph -= s.dph; w |= WR_PH; }
+  if (s.dw != 0.0f) { p.w -= s.dw; w |= WR_W; }
+  return w;
+}
+
+// the map on a live particle, the shift on a lost one (or one the map loses)
 template <class Map>
-__global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m) {
-  PARTICLES(b) {
-    Part p = load_part(b, i);
-    if (p.lo != 0u) continue;
-    store_part(b, i, p, m.apply(p));
+__device__ inline uint32_t step(Part &p, const Map &m, const Shift &s) {
+  if (p.lo != 0u) return keep_lost(p, 0u, s);
+  const uint32_t w = m.apply(p);
+  return p.lo != 0u ? keep_lost(p, w, s) : w;
+}
+
+// Particle sweeps run on a grid that is resident at once (the SMs times the
+// kernel's occupancy); a thread loads kSweepBatch particles before it works
+// on the first, so each SM keeps enough loads in flight to cover latency.
+constexpr int kSweepBatch = 2;
+
+int sweep_grid(const void *kernel, uint32_t n) {
+  static std::unordered_map<const void *, int> resident;
+  static int sms = 0;
+  if (!sms && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) sms = 152;
+  int &r = resident[kernel];
+  if (!r && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kernel, kBlock, 0) != cudaSuccess || r < 1)) r = 1;
+  const uint64_t need = ((uint64_t)n + (uint64_t)kSweepBatch * kBlock - 1) / ((uint64_t)kSweepBatch * kBlock);
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)r * sms));
+}
+
+template <class Map>
+__global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m, Shift sh) {
+  const bool moves = sh.dph != 0.0f || sh.dw != 0.0f;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < b.n; base += kSweepBatch * stride) {
+    Part p[kSweepBatch];
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; ++u)
+      if (base + u * stride < b.n) p[u] = load_part(b, base + u * stride);
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; ++u) {
+      const uint32_t i = base + u * stride;
+      if (i >= b.n || (p[u].lo != 0u && !moves)) continue;
+      store_part(b, i, p[u], step(p[u], m, sh));
+    }
   }
 }
 
-// the map, then UpdateGoodParticleCount + UpdateAvgPhi(true) of the new
-// state (beam.cpp:776-791, 846-852) in the same sweep
+// The map, then every statistic the SCHEFF kick after it takes from the new
+// state (UpdateStatForSpaceCharge and the longitudinal-loss test of
+// Scheff::Start, space_charge.cpp:86-101; beam.cpp:776-852, 1008-1009) in
+// the same sweep, and in the finaliser the decision and the kick's
+// constants.  Phase sums are taken about s, the offset of <phi>_good from
+// the synchronous particle at the last kick of this simulation call (zero at
+// its first), an estimate of the new one: <phi>_good from the raw offsets,
+// sigma_phi and the mean relative phase of the live particles from the
+// phases wrapped about s, shifted.  Two max slots certify that these are the
+// separate sweeps' answers: no particle lies above <phi>_good + 3 pi (the
+// loss test flags none) and no relative phase lies within |<phi>_good - s|
+// of a wrap boundary (it wraps about <phi>_good as about s).  Without the
+// certificate the finaliser records the counts and <phi>_good and sets
+// sc_redo = 2 for the loss-test and moments sweeps; so it does when s lies
+// more than 4 sigma_phi from <phi>_good, where sigma_phi^2 as a difference
+// of FP32 moments about s would lose precision.
 template <class Map>
-struct OpPushGoodPhi {
-  static constexpr int K = 2;
+struct OpPushScStats {
+  // 0 good count, 1 sum d (raw, for <phi>_good), 2-3 sum f, f^2 (wrapped, for
+  // sigma_phi), 4-8 x, x^2, y, y^2, W of the good set; 9 sum f, 10 count of the
+  // live set; 11 lloss count; 12 max |f| over the live set; 13 max phi over
+  // lloss != 1.  d = phi - s, f = wrap(d).
+  static constexpr int K = 14;
+  static constexpr int kMaxFrom = 12;
+  static constexpr int kBatch = 4;
   static constexpr bool kFast = true;
   using Comb = SumComb;
-  struct Ctx {};
+  struct Ctx { float s; };
   struct P { Part p; uint32_t ll; };
   DevBeam b;  // carries the synchronous particle after the element
   Map m;
+  Shift sh;
+  int s_last;  // s from the last kick's <phi>_good offset (else 0)
+  ScState *sc;
+  ScTables tb;
+  double freq, frac;
+  Sc32Host h;
   __device__ bool enabled() const { return true; }
-  __device__ Ctx setup() const { return {}; }
-  __device__ P load(uint32_t i) const { return {load_part(b, i), b.lloss[i]}; }
-  __device__ void use(uint32_t i, const P &q, float (&a)[K], const Ctx &) const {
-    Part p = q.p;
-    if (p.lo == 0u) store_part(b, i, p, m.apply(p));
-    const bool g = (uint32_t)(p.lo + q.ll) == 0u;
-    a[0] += g ? 1.0f : 0.0f;
-    a[1] += g ? p.ph : 0.0f;
+  __device__ Ctx setup() const {
+    const float e = s_last ? tb.c32->pag : 0.0f;
+    return {fabsf(e) < 3.14159265f ? e : 0.0f};
   }
-  __device__ void finalize(const double *t, int tid, int) const {
-    if (tid) return;
-    const uint32_t ng = (uint32_t)t[0];
-    b.st->num_good = ng;
-    b.st->st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)t[1] / (float)ng) + b.phi_ref : -99999;
+  __device__ P load(uint32_t i) const { return {load_part(b, i), b.lloss[i]}; }
+  __device__ void use(uint32_t i, const P &q, float (&a)[K], const Ctx &c) const {
+    Part p = q.p;
+    const uint32_t w = step(p, m, sh);
+    if (w) store_part(b, i, p, w);
+    const bool alive = p.lo == 0u, g = alive && q.ll == 0u;
+    const float d = p.ph - c.s, f = rel_phase_f(d);
+    a[0] += g ? 1.0f : 0.0f;
+    a[1] += g ? d : 0.0f;
+    a[2] += g ? f : 0.0f;
+    a[3] += g ? f * f : 0.0f;
+    a[4] += g ? p.x : 0.0f;
+    a[5] += g ? p.x * p.x : 0.0f;
+    a[6] += g ? p.y : 0.0f;
+    a[7] += g ? p.y * p.y : 0.0f;
+    a[8] += g ? p.w : 0.0f;
+    a[9] += alive ? f : 0.0f;
+    a[10] += alive ? 1.0f : 0.0f;
+    a[11] += q.ll != 0u ? 1.0f : 0.0f;
+    if (alive) a[12] = fmaxf(a[12], fabsf(f));
+    if (q.ll != 1u) a[13] = fmaxf(a[13], p.ph);
+  }
+  __device__ void finalize(const double *t, int tid, int nth) const {
+    __shared__ int ok;
+    if (tid == 0) {
+      BeamStats &st = *b.st;
+      const float s = setup().s;
+      const uint32_t ng = (uint32_t)t[0];
+      const double pag_abs = ng > 0 ? (double)(s + (float)t[1] / (float)ng) + b.phi_ref : -99999.0;
+      st.num_good = ng;
+      st.num_lloss = (uint32_t)t[11];
+      st.st[PHI_AVG_GOOD] = pag_abs;
+      // the loss test's limit and the relative-phase origin, as the sweeps take them
+      const float lim = (float)(pag_abs - b.phi_ref + TWOPI + PI);
+      const float dm = (float)(pag_abs - b.phi_ref) - s;
+      // sigma_phi^2 = <f^2> - <f>^2 keeps FP32 precision while |<f>| <= 4 sigma
+      const float ing = 1.0f / (float)ng, mf = (float)t[2] * ing, var = (float)t[3] * ing - mf * mf;
+      ok = ng > 0 && (float)t[13] <= lim && (float)t[12] < 3.14159265f - fabsf(dm) - 1.0e-3f &&
+           mf * mf <= 16.0f * var;
+      if (ok) {
+        // wrap(phi - <phi>_good) = f - dm on the live set: the totals of the
+        // moments sweep (sigma_phi from the f moments, shift-invariant)
+        double sm[8];
+        sm[0] = (float)t[9] - (float)t[10] * dm;
+        for (int k = 1; k < 8; ++k) sm[k] = t[k + 1];
+        st.sc_redo = 0u;
+        sc_moments_finish(b, sm, sc, tb, freq, frac, h);
+      } else {
+        st.sc_redo = 2u;
+      }
+    }
+    __syncthreads();
+    if (ok) zero_mesh_tables(sc, tb, tid, nth);
   }
 };
 
@@ -70,30 +190,48 @@ struct OpPushGoodPhi {
 // lost, outside the skipped set), then the map on every live particle
 template <class Map>
 __global__ void __launch_bounds__(kBlock) k32_kick_push(DevBeam b, const ScState *sc, ScTables t, RefK rk,
-                                                       uint64_t skip_mask, Map m) {
+                                                       uint64_t skip_mask, Map m, Shift sh) {
   const KickEnv e = kick_env(sc, t, rk);
-  PARTICLES(b) {
-    Part p = load_part(b, i);
-    const uint32_t ll = b.lloss[i];
-    const float pr = b.fphi_r[i];
-    if (p.lo != 0u) continue;
-    uint32_t w = 0;
-    if (ll == 0u && ((uint64_t)i & skip_mask) != 0) w = kick_particle(p, pr, e);
-    if (p.lo == 0u) w |= m.apply(p);
-    store_part(b, i, p, w);
+  const bool moves = sh.dph != 0.0f || sh.dw != 0.0f;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < b.n; base += kSweepBatch * stride) {
+    Part p[kSweepBatch];
+    uint32_t ll[kSweepBatch];
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; ++u) {
+      const uint32_t i = base + u * stride;
+      if (i < b.n) {
+        p[u] = load_part(b, i);
+        ll[u] = b.lloss[i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; ++u) {
+      const uint32_t i = base + u * stride;
+      if (i >= b.n || (p[u].lo != 0u && !moves)) continue;
+      uint32_t w = 0;
+      if (p[u].lo == 0u && ll[u] == 0u && ((uint64_t)i & skip_mask) != 0)
+        w = kick_particle(p[u], rel_phase_f(p[u].ph - e.pag), e);
+      w |= step(p[u], m, sh);
+      store_part(b, i, p[u], w);
+    }
   }
 }
 
 // b carries the synchronous particle after the element; rk is it before
-// (the kick of PUSH_AFTER_KICK happens there)
+// (the kick of PUSH_AFTER_KICK happens there), phi0 / w0 its phase and energy
 template <class Map>
-void launch_map(const DevBeam &b, const Map &m, const RefK &rk, cudaStream_t st, const PushFuse *pf) {
+void launch_map(const DevBeam &b, const Map &m, const RefK &rk, double phi0, double w0, cudaStream_t st,
+                const PushFuse *pf) {
+  const Shift sh{(float)(b.phi_ref - phi0), (float)(b.w_ref - w0)};
   if (!pf) {
-    launch_k(k32_push<Map>, dim3(grid_for(b.n)), dim3(kBlock), 0, st, b, m);
-  } else if (pf->mode == PUSH_GOODPHI) {
-    launch_pass_f(OpPushGoodPhi<Map>{b, m}, b.n, pf->scr, st);
+    launch_k(k32_push<Map>, dim3(sweep_grid((const void *)k32_push<Map>, b.n)), dim3(kBlock), 0, st, b, m, sh);
+  } else if (pf->mode == PUSH_SCSTATS) {
+    launch_pass_f(OpPushScStats<Map>{b, m, sh, pf->s_last, pf->sc, pf->t, pf->freq, pf->frac, pf->h}, b.n, pf->scr,
+                  st);
   } else {
-    launch_k(k32_kick_push<Map>, dim3(grid_for(b.n)), dim3(kBlock), 0, st, b, pf->sc, pf->t, rk, pf->skip_mask, m);
+    launch_k(k32_kick_push<Map>, dim3(sweep_grid((const void *)k32_kick_push<Map>, b.n)), dim3(kBlock), 0, st, b,
+             (const ScState *)pf->sc, pf->t, rk, pf->skip_mask, m, sh);
   }
   note_launch();
 }
@@ -132,14 +270,16 @@ void taylor(const double *a, int na, double b0, double *c) {
 // ---------------------------------------------------------------------------
 void push32_partial_drift(DevBeam &b, double wl, double hf, double aper, uint32_t eid, cudaStream_t st,
                           const PushFuse *pf) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const RefK r = make_refk(b.w_ref, b.mass);
   const DriftMap m{r, (float)hf, (float)(aper * aper), (float)(TWOPI * hf / wl), eid};
   b.phi_ref += TWOPI * hf / (wl * beta_of(b.w_ref, b.mass));
-  launch_map(b, m, r, st, pf);
+  launch_map(b, m, r, phi0, w0, st, pf);
 }
 
 void push32_half_quad(DevBeam &b, double wl, double len, double aper, double grad, uint32_t eid, cudaStream_t st,
                       const PushFuse *pf) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const RefK r = make_refk(b.w_ref, b.mass);
   const double qg = grad * b.charge;
   QuadMap m{};
@@ -162,17 +302,19 @@ void push32_half_quad(DevBeam &b, double wl, double len, double aper, double gra
     m.ch_r = (float)cosh(kds);
   }
   b.phi_ref += TWOPI * len * 0.5 / (wl * beta_of(b.w_ref, b.mass));
-  launch_map(b, m, r, st, pf);
+  launch_map(b, m, r, phi0, w0, st, pf);
 }
 
 void push32_steerer(DevBeam &b, double blh, double blv, cudaStream_t st) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const RefK r = make_refk(b.w_ref, b.mass);
   const float kh = blh > 1e-10 ? (float)(blh * b.charge * CLIGHT / b.mass) : 0.0f;
   const float kv = blv > 1e-10 ? (float)(blv * b.charge * CLIGHT / b.mass) : 0.0f;
-  launch_map(b, SteerMap{r, kh, kv}, r, st, nullptr);
+  launch_map(b, SteerMap{r, kh, kv}, r, phi0, w0, st, nullptr);
 }
 
 void push32_gap_first(DevBeam &b, const GapArgs &g, cudaStream_t st, const PushFuse *pf) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const RefK r = make_refk(b.w_ref, b.mass);
   const double mass = b.mass;
   const double wave_len = CLIGHT / g.frequency;
@@ -205,10 +347,11 @@ void push32_gap_first(DevBeam &b, const GapArgs &g, cudaStream_t st, const PushF
     }
   }
   b.phi_ref += dphi_ref;
-  launch_map(b, Gap1Map{r, (float)dd1, (float)K}, r, st, pf);
+  launch_map(b, Gap1Map{r, (float)dd1, (float)K}, r, phi0, w0, st, pf);
 }
 
 void push32_gap_second(DevBeam &b, const GapArgs &g, cudaStream_t st, const PushFuse *pf) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const double mass = b.mass;
   const RefK rkick = make_refk(b.w_ref, mass);
   Gap2Map G{};
@@ -331,11 +474,12 @@ void push32_gap_second(DevBeam &b, const GapArgs &g, cudaStream_t st, const Push
   G.corr_w = (float)(w_h - w_new);
   b.phi_ref = phi_new;
   b.w_ref = w_new;
-  launch_map(b, G, rkick, st, pf);
+  launch_map(b, G, rkick, phi0, w0, st, pf);
 }
 
 void push32_buncher(DevBeam &b, double wl, double w_ref_design, double freq, double voltage, double phase,
                     double aper, double freq_ratio, uint32_t eid, cudaStream_t st) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const double mass = b.mass;
   BunchMap B{};
   B.r = make_refk(b.w_ref, mass);
@@ -358,11 +502,12 @@ void push32_buncher(DevBeam &b, double wl, double w_ref_design, double freq, dou
   B.aper2 = (float)(aper * aper);
   B.eid = eid;
   b.w_ref += q * voltage * cos(h * b.phi_ref * freq_ratio + phase);
-  launch_map(b, B, B.r, st, nullptr);
+  launch_map(b, B, B.r, phi0, w0, st, nullptr);
 }
 
 void push32_rotation(DevBeam &b, double angle, cudaStream_t st) {
-  launch_map(b, RotMap{(float)cos(angle), (float)sin(angle)}, RefK{}, st, nullptr);
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
+  launch_map(b, RotMap{(float)cos(angle), (float)sin(angle)}, RefK{}, phi0, w0, st, nullptr);
 }
 
 void push32_aperture(DevBeam &b, int rect, const double *p, uint32_t eid, cudaStream_t st) {
@@ -372,6 +517,7 @@ void push32_aperture(DevBeam &b, int rect, const double *p, uint32_t eid, cudaSt
 }
 
 void push32_dipole(DevBeam &b, const double *p, double wl, int second, cudaStream_t st, const PushFuse *pf) {
+  const double phi0 = b.phi_ref, w0 = b.w_ref;
   const double mass = b.mass;
   const RefK rkick = make_refk(b.w_ref, mass);
   const double h = 1.0 / p[HPS_P_DIP_RADIUS];
@@ -406,7 +552,7 @@ void push32_dipole(DevBeam &b, const double *p, double wl, int second, cudaStrea
   d.cdp = (float)cdp; d.dpop_ref = (float)dpop_ref; d.cph = (float)(TWOPI / (beta * wl));
   d.second = second;
   b.phi_ref += TWOPI * (-(r56 * dpop_ref) + dl) / (beta * wl);
-  launch_map(b, d, rkick, st, pf);
+  launch_map(b, d, rkick, phi0, w0, st, pf);
 }
 
 }  // namespace hps

@@ -127,6 +127,11 @@ inline void launch_pass(const Op &op, uint32_t n, PassScratch scr, cudaStream_t 
 // batch is in flight before the first store.
 constexpr int kPassBatch = 4;
 template <int K> constexpr int pass_batch() { return K > 10 ? 2 : kPassBatch; }
+// an Op may set its own batch (`static constexpr int kBatch`)
+template <class Op, class = void>
+struct op_batch : std::integral_constant<int, pass_batch<Op::K>()> {};
+template <class Op>
+struct op_batch<Op, std::void_t<decltype(Op::kBatch)>> : std::integral_constant<int, Op::kBatch> {};
 
 // An Op with `static constexpr bool kFast = true` has its block and grid
 // partials combined in FP32 (counts stay exact below 2^24 particles); the
@@ -137,10 +142,22 @@ struct op_fast : std::false_type {};
 template <class Op>
 struct op_fast<Op, std::void_t<decltype(Op::kFast)>> : std::integral_constant<bool, Op::kFast> {};
 
+// An Op with `static constexpr int kMaxFrom = m` (fast combine only) takes
+// the maximum, not the sum, of accumulators m .. K-1; they start at -inf.
+template <class Op, class = void>
+struct op_max_from : std::integral_constant<int, Op::K> {};
+template <class Op>
+struct op_max_from<Op, std::void_t<decltype(Op::kMaxFrom)>> : std::integral_constant<int, Op::kMaxFrom> {};
+
+template <class C, int MF>
+__device__ inline float comb_k(int k, float a, float b) {
+  return k >= MF ? fmaxf(a, b) : C::comb(a, b);
+}
+
 template <class Op>
 __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
   constexpr int K = Op::K;
-  constexpr int B = pass_batch<K>();
+  constexpr int B = op_batch<Op>::value;
   using C = typename Op::Comb;
   if (!op.enabled()) return;
   __shared__ double sm[kBlock / 32][K];
@@ -150,9 +167,11 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
   if (threadIdx.x == 0) sctx = op.setup();
   __syncthreads();
   const typename Op::Ctx ctx = sctx;
+  constexpr int MF = op_max_from<Op>::value;
+  static_assert(MF == K || op_fast<Op>::value, "max slots need the FP32 combine");
   float acc[K];
 #pragma unroll
-  for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+  for (int k = 0; k < K; ++k) acc[k] = k >= MF ? -INFINITY : 0.0f;
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += B * stride) {
     typename Op::P p[B];
@@ -170,23 +189,25 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if constexpr (op_fast<Op>::value) {
-    // FP32 partials: warps summed in order per block, blocks by warp 0 of
-    // the last block (lane l takes blocks l, l + 32, ...; then a fixed
-    // shuffle tree).  No FP64 arithmetic on the reduction's critical path.
+    // FP32 partials: warps summed in order per block, blocks by the warps of
+    // the last block (slot k by warp k mod 8; lane l takes blocks l, l + 32,
+    // ...; then a fixed shuffle tree).  No FP64 arithmetic on the
+    // reduction's critical path.
     __shared__ float smf[kBlock / 32][K];
     float *partf = (float *)scr.part;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       float v = acc[k];
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
+      for (int off = 16; off > 0; off >>= 1) v = comb_k<C, MF>(k, v, __shfl_down_sync(0xffffffffu, v, off));
       if (lane == 0) smf[warp][k] = v;
     }
     __syncthreads();
     if (threadIdx.x < K) {
-      float v = 0.0f;
-      for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, smf[w][threadIdx.x]);
-      partf[blockIdx.x * K + threadIdx.x] = v;
+      const int k = threadIdx.x;
+      float v = k >= MF ? -INFINITY : 0.0f;
+      for (int w = 0; w < kBlock / 32; ++w) v = comb_k<C, MF>(k, v, smf[w][k]);
+      partf[blockIdx.x * K + k] = v;
     }
     __threadfence();
     __syncthreads();
@@ -194,14 +215,13 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    if (warp == 0) {
-      for (int k = 0; k < K; ++k) {
-        float v = 0.0f;
-        for (uint32_t b = lane; b < gridDim.x; b += 32) v = C::comb(v, __ldcg(partf + (size_t)b * K + k));
+    // warp w combines slots w, w + 8, ...: the slots' chains run side by side
+    for (int k = warp; k < K; k += kBlock / 32) {
+      float v = k >= MF ? -INFINITY : 0.0f;
+      for (uint32_t b = lane; b < gridDim.x; b += 32) v = comb_k<C, MF>(k, v, __ldcg(partf + (size_t)b * K + k));
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v = C::comb(v, __shfl_down_sync(0xffffffffu, v, off));
-        if (lane == 0) tot[k] = (double)v;
-      }
+      for (int off = 16; off > 0; off >>= 1) v = comb_k<C, MF>(k, v, __shfl_down_sync(0xffffffffu, v, off));
+      if (lane == 0) tot[k] = (double)v;
     }
     __syncthreads();
   } else {

@@ -734,6 +734,14 @@ hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
     case 5: *v = s->fraction; break;
     case 6: *v = s->nx; break;
     case 7: *v = s->nz; break;
+    case 8:
+    case 9: {  // counters kept by the kernels
+      ScState h;
+      if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(&h, s->d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(HPS_ERR_CUDA, "scheff_get: reading the solver state failed");
+      *v = param == 8 ? (double)h.n_solves : (double)h.n_stat_sweeps;
+      break;
+    }
     default: return fail(HPS_ERR_INVALID, "scheff_get: unknown parameter");
   }
   return HPS_OK;
@@ -764,6 +772,7 @@ struct Ctx {
   hps_beam_t b;
   hps_beamline_t bl;
   hps_scheff_t sc;
+  bool kicked = false;  // a SCHEFF kick of this simulation call has been issued
 };
 
 const double *P(hps_beamline_t bl, uint32_t i) { return bl->params[i].data(); }
@@ -794,34 +803,8 @@ int T(hps_beamline_t bl, int64_t i) {
   return (i >= 0 && i < (int64_t)bl->types.size()) ? bl->types[i] : 0;
 }
 
-// FP32 beams with a solver: the element half before the kick also takes the
-// first statistics sweep (PUSH_GOODPHI), the half after it runs behind the
-// kick in one sweep (PUSH_AFTER_KICK).  Every launch of the unfused
-// sequence is valid from four particles on (blck_size/4 > 0, n > 2).
-struct Fuse32 {
-  bool on;
-  PushFuse pre, post;
-};
-Fuse32 fuse32(Ctx &c) {
-  Fuse32 z{};
-  hps_beam_t b = c.b;
-  const uint64_t stride = (uint64_t)b->grid_size * (b->blck_size / 4);
-  z.on = f32(b) && c.s->sc_on && c.sc && b->n >= 4 && stride != 0 && (stride & (stride - 1)) == 0;
-  if (!z.on) return z;
-  z.pre.mode = PUSH_GOODPHI;
-  z.pre.scr = b->scr;
-  z.post.mode = PUSH_AFTER_KICK;
-  z.post.sc = c.sc->d;
-  z.post.t = c.sc->t;
-  z.post.t.fld2 = nullptr;
-  z.post.skip_mask = stride - 1;
-  return z;
-}
-
-// fused: the statistics after a PUSH_GOODPHI half and the mesh; the kick
-// runs with the next half
-void sc_apply(Ctx &c, double length, bool fused = false) {
-  if (!(c.s->sc_on && c.sc)) return;
+// the arguments of one SCHEFF kick of the given length
+ScKickArgs kick_args(Ctx &c, double length) {
   hps_beam_t b = c.b;
   ScKickArgs a;
   a.freq = b->freq;
@@ -835,10 +818,59 @@ void sc_apply(Ctx &c, double length, bool fused = false) {
   a.nx_max = c.sc->nx_max;
   a.nz_max = c.sc->nz_max;
   a.adj_possible = c.sc->adj_bunch != 0;
+  return a;
+}
+
+// FP32 beams with a solver: the element half before the kick also takes the
+// kick's statistics (PUSH_SCSTATS), the half after it runs behind the kick
+// in one sweep (PUSH_AFTER_KICK).  Every launch of the unfused sequence is
+// valid from four particles on (blck_size/4 > 0, n > 2).
+struct Fuse32 {
+  bool on;
+  PushFuse pre, post;
+};
+Fuse32 fuse32(Ctx &c) {
+  Fuse32 z{};
+  hps_beam_t b = c.b;
+  const uint64_t stride = (uint64_t)b->grid_size * (b->blck_size / 4);
+  z.on = f32(b) && c.s->sc_on && c.sc && b->n >= 4 && stride != 0 && (stride & (stride - 1)) == 0;
+  if (!z.on) return z;
+  z.pre.mode = PUSH_SCSTATS;
+  z.pre.scr = b->scr;
+  z.pre.sc = c.sc->d;
+  z.pre.t = c.sc->t;
+  z.pre.t.fld2 = nullptr;
+  z.post.mode = PUSH_AFTER_KICK;
+  z.post.sc = c.sc->d;
+  z.post.t = c.sc->t;
+  z.post.t.fld2 = nullptr;
+  z.post.skip_mask = stride - 1;
+  return z;
+}
+
+// the PUSH_SCSTATS form for the half before a kick of the given length
+const PushFuse *pre_for(Ctx &c, const Fuse32 &z, double length, PushFuse *out) {
+  if (!z.on) return nullptr;
+  *out = z.pre;
+  const ScKickArgs a = kick_args(c, length);
+  out->h = sc32_host(c.b->d, a);
+  out->freq = a.freq;
+  out->frac = a.frac;
+  out->s_last = c.kicked;  // results depend on the call's inputs only
+  return out;
+}
+
+// fused: what the PUSH_SCSTATS half left of the statistics, and the mesh;
+// the kick runs with the next half
+void sc_apply(Ctx &c, double length, bool fused = false) {
+  if (!(c.s->sc_on && c.sc)) return;
+  c.kicked = true;
+  hps_beam_t b = c.b;
+  const ScKickArgs a = kick_args(c, length);
   if (f32(b)) {
     sc32_configure();
     if (fused) {
-      PHASE(HPS_PROF_SC_STATS, sc32_stats_after_goodphi(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+      PHASE(HPS_PROF_SC_STATS, sc32_stats_after_push(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
       PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
       return;
     }
@@ -886,7 +918,9 @@ hps_status visit(Ctx &c, uint32_t i) {
   cudaStream_t st = b->stream;
   uint32_t eid = s->cur_id;
   const Fuse32 z = fuse32(c);
-  const PushFuse *pre = z.on ? &z.pre : nullptr, *post = z.on ? &z.post : nullptr;
+  const PushFuse *post = z.on ? &z.post : nullptr;
+  PushFuse pre_buf;
+  auto pre = [&](double length) { return pre_for(c, z, length, &pre_buf); };
   // a half that runs behind the kick is timed as the kick
   auto post_cls = [&](int cls) { return z.on ? (int)HPS_PROF_SC_KICK : cls; };
   switch (bl->types[i]) {
@@ -896,7 +930,7 @@ hps_status visit(Ctx &c, uint32_t i) {
       if (s->sc_on && c.sc) nk = (int)std::ceil(length / c.sc->interval);
       double hf = 0.5 * length / nk;
       for (int k = 0; k < nk; ++k) {
-        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, pre)
+        PHASE(HPS_PROF_DRIFT, f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, pre(2.0 * hf))
                                 : push_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st));
         sc_apply(c, 2.0 * hf, z.on);
         PHASE(post_cls(HPS_PROF_DRIFT), f ? push32_partial_drift(d, s->wavelen, hf, p[HPS_P_APERTURE], eid, st, post)
@@ -907,7 +941,8 @@ hps_status visit(Ctx &c, uint32_t i) {
     case HPS_ELEM_QUAD:
       if (b->blck_size / 2 > 0)
         PHASE(HPS_PROF_QUAD,
-              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st, pre)
+              f ? push32_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st,
+                                   pre(p[HPS_P_LENGTH]))
                 : push_half_quad(d, s->wavelen, p[HPS_P_LENGTH], p[HPS_P_APERTURE], p[HPS_P_GRADIENT], eid, st));
       sc_apply(c, p[HPS_P_LENGTH], z.on);
       if (b->blck_size / 2 > 0)
@@ -942,7 +977,7 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.ccl_cell_num = 0;
       s->wavelen = CLIGHT / g.frequency;  // d_wavelen written by the first-half kernel
       g.wl = s->wavelen;
-      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre) : push_gap_first(d, g, st));
+      if (b->blck_size / 2 > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre(g.length)) : push_gap_first(d, g, st));
       sc_apply(c, g.length, z.on);
       if (b->blck_size / 2 > 0)
         PHASE(post_cls(HPS_PROF_GAP2), f ? push32_gap_second(d, g, st, post) : push_gap_second(d, g, st));
@@ -980,7 +1015,7 @@ hps_status visit(Ctx &c, uint32_t i) {
       g.wl = s->wavelen;
       g.phi_in = phi_in;
       g.ccl_cell_num = 0;
-      if (gcb > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre) : push_gap_first(d, g, st));
+      if (gcb > 0) PHASE(HPS_PROF_GAP1, f ? push32_gap_first(d, g, st, pre(g.length)) : push_gap_first(d, g, st));
       sc_apply(c, g.length, z.on);
       g.phi_in = phi_out;
       g.ccl_cell_num = s->ccl_cell_num;
@@ -1026,7 +1061,7 @@ hps_status visit(Ctx &c, uint32_t i) {
     case HPS_ELEM_DIPOLE:
       if (b->blck_size / 4 > 0)
         PHASE(HPS_PROF_OTHER,
-              f ? push32_dipole(d, p, s->wavelen, 0, st, pre) : push_dipole(d, p, s->wavelen, 0, st));
+              f ? push32_dipole(d, p, s->wavelen, 0, st, pre(p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE])) : push_dipole(d, p, s->wavelen, 0, st));
       sc_apply(c, p[HPS_P_DIP_RADIUS] * p[HPS_P_DIP_ANGLE], z.on);
       if (b->blck_size / 4 > 0)
         PHASE(post_cls(HPS_PROF_OTHER),

@@ -20,6 +20,7 @@ namespace hps {
 struct KickEnv {
   const float2 *fld;
   RefK r;  // synchronous particle at the kick
+  float pag;  // origin of the relative phase: wrap(phi - pag)
   float phimc, xbar, ybar, epsq, inv_epsq, beta, gmg, inv_dr, inv_dzg, hl, rmesh, c2, xfac, yfac, cbgcoef, pl,
       er_c3, ez_c3, dwc;
   uint32_t nx, nz, adj, tbl_sz;
@@ -35,6 +36,7 @@ __device__ inline KickEnv kick_env(const ScState *sc, const ScTables &t, const R
   e.adj = sc->adj;
   e.tbl_sz = (e.nx + 1) * (e.nz + 1);
   e.cbgcoef = kc.cbg_per_onm * (float)sc->num_on_mesh;
+  e.pag = kc.pag;
   e.phimc = kc.phimc; e.xbar = kc.xbar; e.ybar = kc.ybar; e.epsq = kc.epsq; e.inv_epsq = kc.inv_epsq;
   e.beta = kc.beta; e.gmg = kc.gmg; e.inv_dr = kc.inv_dr; e.inv_dzg = kc.inv_dzg; e.hl = kc.hl;
   e.rmesh = kc.rmesh; e.c2 = kc.c2; e.xfac = kc.xfac; e.yfac = kc.yfac; e.pl = kc.pl;

@@ -11,9 +11,13 @@
 //    finaliser does FP64 arithmetic beyond a few adds (GB300 runs FP64 at
 //    1/64 rate, and a dependent FP64 divide costs about a microsecond);
 //  * ahead of a kick on four or more particles, the element half before it
-//    takes the first statistics sweep and the loss test and the moments
-//    share one sweep (Op32LlossScStats); the kick runs inside the element
-//    half after it (push32.cu);
+//    takes every statistics sweep in its own sweep (push32.cu,
+//    OpPushScStats) and certifies that the loss test flags no particle
+//    and that no relative phase wraps; only when it cannot, the loss test
+//    and the moments run here (Op32LlossScStats, then Op32ScStats when the
+//    good set changed).  The kick runs inside the element half after it;
+//  * relative phases are not stored: the deposit and the kick form
+//    wrap(phi - <phi>_good) from the phase offset and Sc32Consts::pag;
 //  * the deposit keeps a 32-bit fixed-point histogram per block in shared
 //    memory (scale chosen from the block's particle count so that no bin can
 //    overflow) and adds it to the 2^-36 global table as integers, so the
@@ -30,6 +34,8 @@
 //    p*^4 / (4 (1 + p*^2/2 + sqrt(1 + p*^2)))]).
 // Particle kernels load a particle's flags and coordinates together and
 // predicate the stores, so each particle costs one memory round trip.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -37,6 +43,7 @@
 #include "internal.h"
 #include "reduce.cuh"
 #include "sc32_kick.cuh"
+#include "sc32_stats.cuh"
 #include "scheff_common.cuh"
 
 namespace hps {
@@ -44,144 +51,6 @@ namespace hps {
 namespace {
 
 struct NoCtx {};
-
-// Host-side constants of one FP32 kick.  The finalisers below run on one
-// thread; on GB300 an FP64 divide or square root there costs about a
-// microsecond, so FP32 beams take the space-charge decision and form the
-// kick's constants in FP32 arithmetic from these (FP64 state fields are kept
-// for the solver's memory).
-struct Sc32Host {
-  float inv_mass;   // 1 / m
-  float wave_len;   // c / f of the beam
-  float c1;         // 5721.67 I frac / (f 1e6 N m): Green's table and far-field scale
-  float length;     // kick length
-};
-
-// gamma, beta of the bunch-frame reference from <W>_good: gamma = 1 + W/m
-// exactly, beta = sqrt(g (g + 2)) / (g + 1) without the 1 - 1/gamma^2
-// cancellation at low energy
-__device__ inline void sc32_kinematics(double ke, float inv_mass, float &gamma, float &beta) {
-  const float g = (float)ke * inv_mass;
-  gamma = 1.0f + g;
-  beta = sqrtf(g * (g + 2.0f)) / gamma;
-}
-
-// UpdateScheffMeshSizeKernel (space_charge_kernel.cu:18-32) in FP32
-__device__ inline void mesh_size32(ScState *s, float beta, float wave_len, float partial_r, float partial_z,
-                                   float coef) {
-  const float bl = beta * wave_len;
-  s->dr = coef * partial_r / (float)s->nx;
-  if (coef == 1.0f) s->dz = bl / (float)s->nz;
-  else s->dz = coef * bl * partial_z / ((float)s->nz * 3.14159265358979f);
-}
-
-// Scheff::Start's decision (space_charge.cpp:86-138, as scheff_decide) in
-// FP32 arithmetic; relative-change tests as |a - b| > threshold * b
-__device__ void scheff_decide32(const BeamStats &st, const DevBeam &b, ScState *s, const Sc32Host &h, double freq,
-                                double frac) {
-  const uint32_t good_cnt = st.num_good;
-  const float sigphi = b.n < 2 ? 0.0f : (float)st.st[PHI_SIG_GOOD];
-  const float sigx = b.n < 2 ? 0.0f : (float)st.st[X_SIG_GOOD];
-  const float sigy = b.n < 2 ? 0.0f : (float)st.st[Y_SIG_GOOD];
-  const double ke = st.st[W_AVG_GOOD];
-  float gamma, beta;
-  sc32_kinematics(ke, h.inv_mass, gamma, beta);
-  const float sigz = sigphi * (0.5f / 3.14159265f) * beta * h.wave_len;
-  const float sigr = sqrtf(sigx * sigx + sigy * sigy);
-  const float cratior = sigr * sigz, cratioz = sigz * sigz * gamma * gamma;
-  const float sro = (float)s->sigr_old, szo = (float)s->sigz_old, gmo = (float)s->gm_old;
-  const float cratior_old = sro * szo, cratioz_old = szo * szo * gmo * gmo;
-  const uint32_t adj = (s->adj_bunch_w == 0.0 || ke < s->adj_bunch_w) ? s->adj_bunch : 0u;
-  s->resized = 0;
-  if (s->mesh_w != 0.0) {
-    if (ke > s->mesh_w && (s->nx != s->nx_init / 2 || s->nz != s->nz_init / 2))
-      set_mesh_size(s, s->nx_init / 2, s->nz_init / 2);
-    else if (ke <= s->mesh_w && (s->nx != s->nx_init || s->nz != s->nz_init))
-      set_mesh_size(s, s->nx_init, s->nz_init);
-    if (ke > s->mesh_w && s->interval != s->interval_init * 4) s->interval = s->interval_init * 4;
-    else if (ke <= s->mesh_w && s->interval != s->interval_init) s->interval = s->interval_init;
-  }
-  s->freq = freq;
-  s->beta = beta;
-  s->frac = frac;
-  s->adj = adj;
-  const float thr = (float)s->remesh_val;
-  if (cratior_old == 0.0f || cratioz_old == 0.0f || fabsf(cratior - cratior_old) > thr * cratior_old ||
-      fabsf(cratioz - cratioz_old) > thr * cratioz_old) {
-    s->sigr_old = sigr;
-    s->sigz_old = sigz;
-    s->gm_old = gamma;
-    s->good_cnt_old = good_cnt;
-    s->remesh = 1;
-    s->n_solves += 1;
-    s->ratio_r = s->ratio_z = s->ratio_q = s->ratio_g = 1.0;
-    // y branch of the pointer comparison (see scheff_decide)
-    if (adj == 0) mesh_size32(s, beta, h.wave_len, sigy, sigphi, 3.0f);
-  } else {
-    s->remesh = 0;
-    s->ratio_r = sigr / sro;
-    s->ratio_z = sigz / szo;
-    s->ratio_q = s->good_cnt_old ? (double)(good_cnt / s->good_cnt_old) : 0.0;
-    s->ratio_g = gamma / gmo;
-  }
-}
-
-// Constants of the kick about to run, from the statistics and the decision
-// (ApplySpchKickKernel, space_charge_kernel.cu:573-620; UpdateFldTbl1Kernel,
-// :39-60; DistributeParticleKernel, :123-150), once per kick.  The only FP64
-// operation is the offset of the synchronous particle from <W>_good.
-__device__ void sc32_consts(const BeamStats &st, const DevBeam &b, const ScState *s, Sc32Consts *c,
-                            const Sc32Host &h) {
-  const double ke = st.st[W_AVG_GOOD];
-  float gmg, beta;
-  sc32_kinematics(ke, h.inv_mass, gmg, beta);
-  const float sx = (float)st.st[X_SIG_GOOD], sy = (float)st.st[Y_SIG_GOOD];
-  const float epsq = sx / sy;
-  const float dr0 = (float)s->dr, dzg0 = (float)s->dz * gmg;
-  const float dr = dr0 * (float)s->ratio_r, dzg = dzg0 * (float)s->ratio_z;
-  const float c3 = h.length / (beta * gmg);
-  const float rr = (float)s->ratio_r, rz = (float)s->ratio_z, rq = (float)s->ratio_q, rg = (float)s->ratio_g;
-  c->phimc = (float)st.st[PHI_AVG_R];
-  c->xbar = (float)st.st[X_AVG_GOOD];
-  c->ybar = (float)st.st[Y_AVG_GOOD];
-  c->epsq = epsq;
-  c->inv_epsq = sy / sx;
-  c->xfac = 2.0f / (epsq + 1.0f);
-  c->yfac = epsq * c->xfac;
-  c->beta = beta;
-  c->gmg = gmg;
-  c->pl = beta * gmg * h.wave_len;
-  c->c2 = c->pl * (1.0f / 6.28318530717958647692f);
-  c->dr = dr;
-  c->dzg = dzg;
-  c->inv_dr = 1.0f / dr;
-  c->inv_dzg = 1.0f / dzg;
-  c->hl = (float)s->nz * 0.5f * dzg;
-  c->rmesh = (float)s->nx * dr;
-  c->dr0 = dr0;
-  c->dzg0 = dzg0;
-  c->inv_dr0 = 1.0f / dr0;
-  c->inv_dzg0 = 1.0f / dzg0;
-  c->hl0 = (float)s->nz * 0.5f * dzg0;
-  c->cbg_per_onm = h.c1 * c3 * (3.14159265358979f * 0.5f);
-  c->er_c3 = rq / (rr * rz * rg * rg) * c3;
-  c->ez_c3 = rq / (rz * rz) * c3;
-  c->dwc = (float)(b.w_ref - ke);  // W_sync - W_c: gamma_c = 1 + <W>_good / m
-  c->green_c1 = h.c1;
-}
-
-// The decision and the kick constants on local copies of the solver state:
-// one burst of loads, one burst of stores, and no load waiting behind a
-// store that might alias it.
-__device__ void sc32_decide_consts(const BeamStats &st, const DevBeam &b, ScState *sc, Sc32Consts *c32,
-                                   const Sc32Host &h, double freq, double frac) {
-  ScState s = *sc;
-  Sc32Consts c;
-  scheff_decide32(st, b, &s, h, freq, frac);
-  sc32_consts(st, b, &s, &c, h);
-  *sc = s;
-  *c32 = c;
-}
 
 // UpdateGoodParticleCount + UpdateAvgPhi(true)
 struct Op32GoodPhi {
@@ -238,26 +107,6 @@ struct Op32LlossGoodPhi {
   }
 };
 
-// The SCHEFF moments from their totals s[0..7] (FP32 arithmetic, see
-// Sc32Host), then, with a solver, the decision and the kick's constants
-// (thread 0); the caller zeroes the tables afterwards.
-__device__ void sc_moments_finish(const DevBeam &b, const double *s, ScState *sc, const ScTables &t, double freq,
-                                  double frac, const Sc32Host &h) {
-  BeamStats st = *b.st;  // local copy, written back once
-  const float isv = 1.0f / (float)(uint32_t)(b.n - st.num_loss), ing = 1.0f / (float)st.num_good;
-  st.st[PHI_AVG_R] = (float)s[0] * isv;
-  const float pa = (float)s[1] * ing, pa2 = (float)s[2] * ing;
-  st.st[PHI_SIG_GOOD] = sqrtf(pa2 - pa * pa);
-  const float xa = (float)s[3] * isv, x2 = (float)s[4] * isv, ya = (float)s[5] * isv, y2 = (float)s[6] * isv;
-  st.st[X_AVG_GOOD] = xa;
-  st.st[X_SIG_GOOD] = sqrtf(x2 - xa * xa);
-  st.st[Y_AVG_GOOD] = ya;
-  st.st[Y_SIG_GOOD] = sqrtf(y2 - ya * ya);
-  st.st[W_AVG_GOOD] = st.num_good > 0 ? (double)((float)s[7] * ing) + b.w_ref : -99999;
-  *b.st = st;
-  if (sc) sc32_decide_consts(st, b, sc, t.c32, h, freq, frac);
-}
-
 // accumulate particle p into the SCHEFF moments (pr: its relative phase)
 __device__ inline void sc_moments_add(float (&a)[12], float pr, uint32_t lo, uint32_t ll, float x, float y, float w) {
   const float alive = lo == 0u ? 1.0f : 0.0f;
@@ -270,7 +119,7 @@ __device__ inline void sc_moments_add(float (&a)[12], float pr, uint32_t lo, uin
 
 // relative phase about <phi>_good, the SCHEFF moments, the decision and the
 // kick's constants (as OpScStats in scheff.cu).  With redo_only it runs only
-// when the fused sweep below found the good set changed.
+// when the loss-test sweep below changed the good set (sc_redo == 1).
 struct Op32ScStats {
   static constexpr int K = 8;
   static constexpr bool kFast = true;
@@ -282,7 +131,7 @@ struct Op32ScStats {
   double freq, frac;
   Sc32Host h;
   int redo_only;
-  __device__ bool enabled() const { return !redo_only || b.st->sc_redo != 0u; }
+  __device__ bool enabled() const { return !redo_only || b.st->sc_redo == 1u; }
   __device__ Ctx setup() const { return {(float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref)}; }
   struct P { uint32_t lo, ll; float ph, x, y, w; };
   __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i], b.fx[i], b.fy[i], b.fw[i]}; }
@@ -309,12 +158,13 @@ struct Op32ScStats {
 
 // The longitudinal-loss test (UpdateLongitudinalLossCoordinateKernel with the
 // lloss and good counts and <phi>_good, beam.cpp:780-781, 1008-1009) and the
-// SCHEFF moments in one sweep.  The relative phases are taken about the
-// <phi>_good of the sweep before (fused into the element map ahead of the
-// kick); when the test flags no particle of the good set, that is the
-// <phi>_good the separate sweeps would have used, and the totals are the
-// same ones in the same order.  Otherwise the sweep records the new
-// <phi>_good and asks for the moments sweep again (sc_redo).
+// SCHEFF moments in one sweep, when the element map before the kick could
+// not certify its own statistics (sc_redo == 2).  The relative phases are
+// taken about the <phi>_good that sweep recorded; when the test flags no
+// particle of the good set, that is the <phi>_good the separate sweeps would
+// have used, and the totals are the same ones in the same order.  Otherwise
+// the sweep records the new <phi>_good and asks for the moments sweep again
+// (sc_redo = 1).
 struct Op32LlossScStats {
   static constexpr int K = 12;
   static constexpr bool kFast = true;
@@ -325,7 +175,7 @@ struct Op32LlossScStats {
   ScTables t;
   double freq, frac;
   Sc32Host h;
-  __device__ bool enabled() const { return true; }
+  __device__ bool enabled() const { return b.st->sc_redo == 2u; }
   __device__ Ctx setup() const {
     const double pag = b.st->st[PHI_AVG_GOOD] - b.phi_ref;
     return {(float)(pag + TWOPI + PI), (float)pag};
@@ -352,6 +202,7 @@ struct Op32LlossScStats {
   __device__ void finalize(const double *s, int tid, int nth) const {
     __shared__ int redo;
     if (tid == 0) {
+      sc->n_stat_sweeps += 1;
       BeamStats &st = *b.st;
       const uint32_t ng = (uint32_t)s[9];
       st.num_lloss = (uint32_t)s[8];
@@ -374,22 +225,22 @@ struct Op32AdjMesh {
   static constexpr int K = 2;
   static constexpr bool kFast = true;
   using Comb = MaxComb;
-  struct Ctx { float xa, ya, pa; };
+  struct Ctx { float xa, ya, pa, pag; };
   DevBeam b;
   ScState *sc;
   Sc32Consts *c32;
   Sc32Host h;
   __device__ bool enabled() const { return sc->remesh && sc->adj != 0u; }
   __device__ Ctx setup() const {
-    return {(float)b.st->st[X_AVG], (float)b.st->st[Y_AVG], (float)b.st->st[PHI_AVG_R]};
+    return {(float)b.st->st[X_AVG], (float)b.st->st[Y_AVG], (float)b.st->st[PHI_AVG_R], c32->pag};
   }
-  struct P { uint32_t lo; float x, y, pr; };
-  __device__ P load(uint32_t i) const { return {b.loss[i], b.fx[i], b.fy[i], b.fphi_r[i]}; }
+  struct P { uint32_t lo; float x, y, ph; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.fx[i], b.fy[i], b.fphi[i]}; }
   __device__ void use(uint32_t, const P &p, float (&a)[K], const Ctx &c) const {
     if (p.lo != 0u) return;
     float tx = p.x - c.xa, ty = p.y - c.ya;
     a[0] = fmaxf(a[0], tx * tx + ty * ty);
-    a[1] = fmaxf(a[1], fabsf(p.pr - c.pa));
+    a[1] = fmaxf(a[1], fabsf(rel_phase_f(p.ph - c.pag) - c.pa));
   }
   __device__ void finalize(const double *t, int tid, int) const {
     if (tid) return;
@@ -486,11 +337,24 @@ struct DepQ {
   int smem;      // per-block histogram in shared memory (else global atomics)
 };
 
+// Deposit blocks run in clusters of kDepCluster CTAs: each CTA fills its own
+// shared-memory histogram, then CTA r of the cluster sums slice r of the
+// cluster's histograms through distributed shared memory and adds it to the
+// global table, so a bin takes one global atomic per cluster, not per block.
+constexpr int kDepCluster = 8;
+constexpr int kDepBatch = 4;  // particles a thread loads before it deposits them
+
+struct DepIn {
+  uint32_t lo, ll;
+  float x, y, ph;
+};
+
 // DistributeParticleKernel (space_charge_kernel.cu:123-224) in FP32, on
-// blocks [0, nblk) of the launch
+// blocks [0, nblk) of the launch (nblk a multiple of kDepCluster)
 __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t, const DepQ &q, uint32_t bid,
                                uint32_t nblk) {
   extern __shared__ int hist32[];
+  namespace cg = cooperative_groups;
   const uint32_t nx = sc->nx, nz = sc->nz, nb = nx * nz;
   if (q.smem) {
     for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) hist32[k] = 0;
@@ -499,72 +363,89 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
   const Sc32Consts &kc = *t.c32;
   const float phimc = kc.phimc, xbar = kc.xbar, ybar = kc.ybar, epsq = kc.epsq, inv_epsq = kc.inv_epsq;
   const float dr = kc.dr0, dzg = kc.dzg0, inv_dr = kc.inv_dr0, inv_dzg = kc.inv_dzg0, hl = kc.hl0, c2 = kc.c2;
+  const float pag = kc.pag;
   const float drdr = dr * dr, inv_drdr = inv_dr * inv_dr;
   const long long m = 1ll << q.shift;
+  const uint32_t stride = nblk * blockDim.x;
   uint32_t cnt = 0;
-  for (uint32_t np = bid * blockDim.x + threadIdx.x; np < bm.n; np += nblk * blockDim.x) {
-    const uint32_t lo = bm.loss[np], ll = bm.lloss[np];
-    const float px = bm.fx[np], py = bm.fy[np], pz = bm.fphi_r[np];
-    float dx = px - xbar, dy = py - ybar;
-    float rsq_sh = dx * dx * inv_epsq + dy * dy * epsq;
-    int i = (int)(sqrtf(rsq_sh) * inv_dr + 1.0f);
-    float z = -c2 * wrap_turns(pz - phimc);
-    if (lo != 0u || ll != 0u) continue;
-    if (!(i >= 1 && (uint32_t)i <= nx)) continue;
-    if (!(fabsf(z) < hl)) continue;
-    float zz = z + hl;
-    int jm1 = (int)(zz * inv_dzg + 1.0f);
-    if (jm1 < 1 || jm1 > (int)nz) continue;
-    int i1 = i + 1;
-    if (rsq_sh < 0.5f * drdr * (float)(i * i + (i - 1) * (i - 1))) i1 = i - 1;
-    i1 = min(max(i1, 1), (int)nx);
-    int j1 = jm1 + 1;
-    if (zz < ((float)jm1 - 0.5f) * dzg) j1 = jm1 - 1;
-    j1 = min(max(j1, 1), (int)nz);
-    // area weights in units of dr^2 (rmax^2 - rmin^2 = sqrtmp dr^2), and the
-    // z weight with (jm1 - j1) dz = +-dz
-    float a = 1.0f;
-    if (i1 != i) {
-      const float sqrtmp = sqrtf(4.0f * rsq_sh * inv_drdr - 1.0f);
-      const float rmin_n = 0.25f * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
-      const float rmax_n = rmin_n + sqrtmp;
-      if (i1 < i) a = __fdividef(rmax_n - (float)((i - 1) * (i - 1)), sqrtmp);
-      else a = __fdividef((float)((i1 - 1) * (i1 - 1)) - rmin_n, sqrtmp);
+  for (uint32_t base = bid * blockDim.x + threadIdx.x; base < bm.n; base += kDepBatch * stride) {
+    DepIn in[kDepBatch];
+#pragma unroll
+    for (int u = 0; u < kDepBatch; ++u) {
+      const uint32_t np = base + u * stride;
+      if (np < bm.n) in[u] = {bm.loss[np], bm.lloss[np], bm.fx[np], bm.fy[np], bm.fphi[np]};
+      else in[u].lo = 1u;
     }
-    float cc = 1.0f;
-    if (j1 != jm1) cc = (zz - ((float)j1 - 0.5f) * dzg) * (j1 < jm1 ? inv_dzg : -inv_dzg);
-    float bb = 1.0f - a, d = 1.0f - cc;
-    int k00 = (jm1 - 1) * (int)nx + i - 1, k01 = k00 + (i1 - i);
-    int k10 = (j1 - 1) * (int)nx + i - 1, k11 = k10 + (i1 - i);
-    int w00 = __float2int_rn(a * cc * q.scale), w01 = __float2int_rn(bb * cc * q.scale);
-    int w10 = __float2int_rn(a * d * q.scale), w11 = __float2int_rn(bb * d * q.scale);
-    if (q.smem) {
-      if (w00) atomicAdd(hist32 + k00, w00);
-      if (w01) atomicAdd(hist32 + k01, w01);
-      if (w10) atomicAdd(hist32 + k10, w10);
-      if (w11) atomicAdd(hist32 + k11, w11);
-    } else {
-      if (w00) atomicAdd(t.bin_fx + k00, (unsigned long long)((long long)w00 * m));
-      if (w01) atomicAdd(t.bin_fx + k01, (unsigned long long)((long long)w01 * m));
-      if (w10) atomicAdd(t.bin_fx + k10, (unsigned long long)((long long)w10 * m));
-      if (w11) atomicAdd(t.bin_fx + k11, (unsigned long long)((long long)w11 * m));
+#pragma unroll
+    for (int u = 0; u < kDepBatch; ++u) {
+      if (in[u].lo != 0u || in[u].ll != 0u) continue;
+      const float pz = rel_phase_f(in[u].ph - pag);
+      float dx = in[u].x - xbar, dy = in[u].y - ybar;
+      float rsq_sh = dx * dx * inv_epsq + dy * dy * epsq;
+      int i = (int)(sqrtf(rsq_sh) * inv_dr + 1.0f);
+      float z = -c2 * wrap_turns(pz - phimc);
+      if (!(i >= 1 && (uint32_t)i <= nx)) continue;
+      if (!(fabsf(z) < hl)) continue;
+      float zz = z + hl;
+      int jm1 = (int)(zz * inv_dzg + 1.0f);
+      if (jm1 < 1 || jm1 > (int)nz) continue;
+      int i1 = i + 1;
+      if (rsq_sh < 0.5f * drdr * (float)(i * i + (i - 1) * (i - 1))) i1 = i - 1;
+      i1 = min(max(i1, 1), (int)nx);
+      int j1 = jm1 + 1;
+      if (zz < ((float)jm1 - 0.5f) * dzg) j1 = jm1 - 1;
+      j1 = min(max(j1, 1), (int)nz);
+      // area weights in units of dr^2 (rmax^2 - rmin^2 = sqrtmp dr^2), and the
+      // z weight with (jm1 - j1) dz = +-dz
+      float a = 1.0f;
+      if (i1 != i) {
+        const float sqrtmp = sqrtf(4.0f * rsq_sh * inv_drdr - 1.0f);
+        const float rmin_n = 0.25f * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
+        const float rmax_n = rmin_n + sqrtmp;
+        if (i1 < i) a = __fdividef(rmax_n - (float)((i - 1) * (i - 1)), sqrtmp);
+        else a = __fdividef((float)((i1 - 1) * (i1 - 1)) - rmin_n, sqrtmp);
+      }
+      float cc = 1.0f;
+      if (j1 != jm1) cc = (zz - ((float)j1 - 0.5f) * dzg) * (j1 < jm1 ? inv_dzg : -inv_dzg);
+      float bb = 1.0f - a, d = 1.0f - cc;
+      int k00 = (jm1 - 1) * (int)nx + i - 1, k01 = k00 + (i1 - i);
+      int k10 = (j1 - 1) * (int)nx + i - 1, k11 = k10 + (i1 - i);
+      int w00 = __float2int_rn(a * cc * q.scale), w01 = __float2int_rn(bb * cc * q.scale);
+      int w10 = __float2int_rn(a * d * q.scale), w11 = __float2int_rn(bb * d * q.scale);
+      if (q.smem) {
+        if (w00) atomicAdd(hist32 + k00, w00);
+        if (w01) atomicAdd(hist32 + k01, w01);
+        if (w10) atomicAdd(hist32 + k10, w10);
+        if (w11) atomicAdd(hist32 + k11, w11);
+      } else {
+        if (w00) atomicAdd(t.bin_fx + k00, (unsigned long long)((long long)w00 * m));
+        if (w01) atomicAdd(t.bin_fx + k01, (unsigned long long)((long long)w01 * m));
+        if (w10) atomicAdd(t.bin_fx + k10, (unsigned long long)((long long)w10 * m));
+        if (w11) atomicAdd(t.bin_fx + k11, (unsigned long long)((long long)w11 * m));
+      }
+      ++cnt;
     }
-    ++cnt;
   }
   for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
   if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&sc->num_on_mesh, cnt);
-  if (!q.smem) return;
-  __syncthreads();
-  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
-    int v = hist32[k];
-    if (v) atomicAdd(t.bin_fx + k, (unsigned long long)((long long)v * m));
+  if (!q.smem) return;  // uniform over the launch
+  cg::cluster_group cl = cg::this_cluster();
+  cl.sync();  // every histogram of the cluster is complete
+  const uint32_t nc = cl.num_blocks(), r = cl.block_rank();
+  const uint32_t per = (nb + nc - 1) / nc, k0 = r * per, k1 = min(nb, k0 + per);
+  for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    long long v = 0;  // up to nc block sums of < 2^30 each
+    for (uint32_t c = 0; c < nc; ++c) v += *cl.map_shared_rank(hist32 + k, c);
+    if (v) atomicAdd(t.bin_fx + k, (unsigned long long)(v * m));
   }
+  cl.sync();  // no CTA leaves while the others read its histogram
 }
 
 // The deposit and the Green's table are independent: one launch, blocks
-// [0, ndep) deposit, blocks [ndep, ndep + ngreen) evaluate the table.
-__global__ void __launch_bounds__(kBlock) k32_green_deposit(DevBeam bm, ScState *sc, ScTables t, DepQ q,
-                                                           uint32_t ndep, uint32_t ngreen) {
+// [0, ndep) deposit, blocks [ndep, ndep + ngreen) evaluate the table (both
+// multiples of the cluster size, so no cluster mixes the two).
+__global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
+    k32_green_deposit(DevBeam bm, ScState *sc, ScTables t, DepQ q, uint32_t ndep, uint32_t ngreen) {
   if (!sc->remesh) return;
   if (blockIdx.x < ndep) deposit_blocks(bm, sc, t, q, blockIdx.x, ndep);
   else green_blocks(sc, t, blockIdx.x - ndep, ngreen);
@@ -627,12 +508,32 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
   const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * fld_sz;  // [dz][rs]
   float ax0 = 0.0f, az0 = 0.0f, ax1 = 0.0f, az1 = 0.0f;
   for (uint32_t rs0 = 0; rs0 < nx; rs0 += tr) {
-    const uint32_t ntr = min(tr, nx - rs0);
+    const uint32_t ntr = min(tr, nx - rs0), ntile = nz * ntr;
     __syncthreads();
-    for (uint32_t e = threadIdx.x; e < nz * ntr; e += blockDim.x) {
-      const uint32_t z = e / ntr, r = e - z * ntr;
-      gs[z * tr + r] = G[(size_t)z * nx + rs0 + r];
-      qs[z * tr + r] = fixed_to_float(t.bin_fx[z * nx + rs0 + r]);
+    // every load of a thread's share is issued before its first store: one
+    // memory round trip per kStage elements, not per element
+    constexpr int kStage = 8;
+    for (uint32_t e0 = threadIdx.x; e0 < ntile; e0 += kStage * blockDim.x) {
+      float2 gv[kStage];
+      unsigned long long bv[kStage];
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const uint32_t e = e0 + u * blockDim.x;
+        if (e < ntile) {
+          const uint32_t z = e / ntr, r = e - z * ntr;
+          gv[u] = __ldg(G + (size_t)z * nx + rs0 + r);
+          bv[u] = __ldg(t.bin_fx + z * nx + rs0 + r);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const uint32_t e = e0 + u * blockDim.x;
+        if (e < ntile) {
+          const uint32_t z = e / ntr, r = e - z * ntr;
+          gs[z * tr + r] = gv[u];
+          qs[z * tr + r] = fixed_to_float(bv[u]);
+        }
+      }
     }
     __syncthreads();
     if (zp > nz) continue;
@@ -690,9 +591,8 @@ __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bm.n; i += gridDim.x * blockDim.x) {
     Part p = load_part(bm, i);
     const uint32_t ll = bm.lloss[i];
-    const float pr = bm.fphi_r[i];
     if (((uint64_t)i & skip_mask) == 0 || p.lo != 0u || ll != 0u) continue;
-    store_part(bm, i, p, kick_particle(p, pr, e));
+    store_part(bm, i, p, kick_particle(p, rel_phase_f(p.ph - e.pag), e));
   }
 }
 
@@ -730,7 +630,7 @@ static ScTables tables32(const ScTables &t) {
   return u;
 }
 
-static Sc32Host host32(const DevBeam &b, const ScKickArgs &a) {
+Sc32Host sc32_host(const DevBeam &b, const ScKickArgs &a) {
   Sc32Host h;
   h.inv_mass = (float)(1.0 / b.mass);
   h.wave_len = (float)(CLIGHT / a.freq);
@@ -742,7 +642,7 @@ static Sc32Host host32(const DevBeam &b, const ScKickArgs &a) {
 void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                 cudaStream_t st) {
   ScTables u = tables32(t);
-  const Sc32Host h = host32(b, a);
+  const Sc32Host h = sc32_host(b, a);
   if (a.stats_ok) {
     launch_pass_f(Op32GoodPhi{b}, b.n, s, st);
     launch_pass_f(Op32LlossGoodPhi{b}, b.n, s, st);
@@ -754,10 +654,10 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
   }
 }
 
-void sc32_stats_after_goodphi(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
-                              PassScratch s, cudaStream_t st) {
+void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+                           PassScratch s, cudaStream_t st) {
   ScTables u = tables32(t);
-  const Sc32Host h = host32(b, a);
+  const Sc32Host h = sc32_host(b, a);
   launch_pass_f(Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st);
   launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, h, 1}, b.n, s, st);
   note_launch(2);
@@ -767,22 +667,24 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
                cudaStream_t st) {
   ScTables u = tables32(t);
   if (a.adj_possible) {  // the mesh is sized from r_max only with adjacent bunches
-    launch_pass_f(Op32AdjMesh{b, sc, u.c32, host32(b, a)}, b.n, s, st);
+    launch_pass_f(Op32AdjMesh{b, sc, u.c32, sc32_host(b, a)}, b.n, s, st);
     note_launch();
   }
   uint32_t ndep = 0;
   size_t hb = 0;
   DepQ q{};
   if (a.deposit_ok) {
-    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, (uint32_t)kMaxPassBlocks);
-    if (ndep < 1) ndep = 1;
+    // two blocks per SM at most, in whole clusters
+    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, 2u * 152u);
+    ndep = (ndep + kDepCluster - 1) / kDepCluster * kDepCluster;
     hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
     if (hb > kMaxHistSmem) hb = 0;
     q = dep_quant(b.n, (int)ndep, hb);
   }
   // Green's table entries of the largest mesh, one per thread
-  const uint32_t ngreen = std::min<uint32_t>(
+  uint32_t ngreen = std::min<uint32_t>(
       (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 4u * 152u);
+  ngreen = (ngreen + kDepCluster - 1) / kDepCluster * kDepCluster;
   launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
   note_launch();
   dim3 cg(a.nx_max + 1, (a.nz_max + 1 + kCZ - 1) / kCZ);

@@ -167,7 +167,10 @@ hps_status hps_beamline_set_param(hps_beamline_t bl, uint32_t index, int slot, d
 hps_status hps_scheff_create(uint32_t nr, uint32_t nz, uint32_t adj_bunch, hps_scheff_t *out);
 hps_status hps_scheff_destroy(hps_scheff_t s);
 /* parameter: 0 interval, 1 adj_bunch, 2 adj_bunch_cutoff_w, 3 mesh_size_cutoff_w,
- *            4 remesh_threshold, 5 fraction, 6 nr, 7 nz (6/7 read-only) */
+ *            4 remesh_threshold, 5 fraction, 6 nr, 7 nz (6/7 read-only);
+ * read-only counters since creation: 8 field solves (remeshes), 9 kicks of an
+ * FP32 beam whose statistics took the separate loss-test and moments sweeps
+ * (the element map before the kick could not certify them) */
 hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
 hps_status hps_scheff_get(hps_scheff_t s, int param, double *value);
 /* SetMeshSize, space_charge.cpp:61-73 */
