@@ -13,6 +13,8 @@
 // in the same sweep.
 #pragma once
 
+#include <algorithm>
+
 #include <type_traits>
 
 #include "common.cuh"
@@ -251,19 +253,31 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
   if (threadIdx.x == 0) *scr.counter = 0u;
 }
 
-// At most two blocks per SM: the last block sums every block's partials in
-// FP64 on one SM (1/64-rate FP64 on GB300), so fewer, fuller blocks keep
-// that tail short; each thread walks more particles in batches instead.
-inline int pass_blocks_f(uint32_t n) {
+// With the FP64 combine, at most two blocks per SM: the last block sums
+// every block's partials in FP64 on one SM (1/64-rate FP64 on GB300), so
+// fewer, fuller blocks keep that tail short; each thread walks more
+// particles in batches instead.  With the FP32 combine, every block the SMs
+// hold at once (up to the scratch's kMaxPassBlocks).
+inline int pass_blocks_f(uint32_t n, int per_sm = 2) {
   uint32_t b = (n + kPassBatch * kBlock - 1) / (kPassBatch * kBlock);
   if (b < 1) b = 1;
-  if (b > 2u * 152u) b = 2u * 152u;
+  const uint32_t cap = std::min<uint32_t>((uint32_t)per_sm * 152u, (uint32_t)kMaxPassBlocks);
+  if (b > cap) b = cap;
   return (int)b;
 }
 
 template <class Op>
+inline int pass_resident() {
+  static int r = 0;  // blocks of this kernel an SM holds at once
+  if (!r && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, pass_kernel_f<Op>, kBlock, 0) != cudaSuccess || r < 1))
+    r = 1;
+  return r;
+}
+
+template <class Op>
 inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s) {
-  launch_k(pass_kernel_f<Op>, dim3(pass_blocks_f(n)), dim3(kBlock), 0, s, op, n, scr);
+  const int per_sm = op_fast<Op>::value ? pass_resident<Op>() : 2;
+  launch_k(pass_kernel_f<Op>, dim3(pass_blocks_f(n, per_sm)), dim3(kBlock), 0, s, op, n, scr);
 }
 
 // FP32 version of rel_phase for offsets that are already small

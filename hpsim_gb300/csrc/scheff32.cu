@@ -454,20 +454,26 @@ __global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
 // ---- contraction -------------------------------------------------------------
 // Ring-to-mesh field sum (UpdateFldTbl2KernelDouble, space_charge_kernel.cu:
 // 472-568) in FP32:  E[zp][rp] = sum over bins (zs, rs) of q(zs, rs) *
-// G[rp][rs][dz(zp, zs)], Ez negated for source bins at or above zp.  For one
-// beam this is a matrix-vector product (one charge vector against the
-// Toeplitz-in-z Green's matrix), so it runs on the FP32 pipes.  One warp per
-// field point (zp, rp), sixteen points of one rp per block: the lanes run over
-// source radii rs, the warp walks the source rows zs below and then above
-// zp, so the sign of E_z and the table row dz are uniform across the warp.
-// The block stages its rp's slice of the Green's table (stored [rp][dz][rs])
-// and the charges, converted to FP32, in shared memory, a tile of source
-// radii at a time; each point's sum ends with a fixed shuffle tree.  The set
-// of bins each point sums is the reference's (its integer partition of the
-// table; see scheff.cu).
-constexpr int kCZ = 16;                    // field points (warps) per block
-constexpr int kContractThreads = kCZ * 32;
-constexpr int kContractSmem = 96 * 1024;   // largest Green's + charge tile
+// g(zp - zs), g(k) = G[rp][k - 1][rs] for sources below the point (k >= 1)
+// and G[rp][-k][rs] with E_z negated for sources at or above it (k <= 0).
+// For each source radius this is a convolution along z.  A block stages its
+// rp's g(k), k = -(nz - 1) .. nz, sign included, and the charges, converted
+// to FP32, in shared memory, a tile of source radii at a time.  A warp
+// computes kCP consecutive field points over half the source rows (two warps
+// per point group, summed in a fixed order): the lanes run over source radii,
+// and as the warp walks the rows the kCP values of g it needs slide by one,
+// kept in a ring of kCP + 1 registers that takes one new shared-memory load
+// per row (one charge and one table load per 2 kCP FMAs).  Each point's sum
+// ends with a fixed shuffle tree.  The set of bins each point sums is the
+// reference's (its integer partition of the table; see scheff.cu): bins
+// zs * nr + rs at or above a limit are left out, which only happens when the
+// mesh has fewer than 1024 bins or a row count that does not divide them.
+constexpr int kCP = 4;                     // field points per warp
+constexpr int kCH = 2;                     // warps sharing the source rows of a point group
+constexpr int kCG = 4;                     // point groups per block
+constexpr int kCZ = kCP * kCG;             // field points per block
+constexpr int kContractThreads = kCG * kCH * 32;
+constexpr int kContractSmem = 96 * 1024;   // largest table + charge tile
 
 // 2^-36 fixed-point charge -> FP32 through two 32-bit conversions (a 64-bit
 // integer conversion runs on the FP64 pipe)
@@ -478,37 +484,58 @@ __device__ inline float fixed_to_float(unsigned long long v) {
   return fmaf((float)hi, 4294967296.0f, (float)lo) * 1.4551915228366852e-11f;  // 2^-36
 }
 
-// shared memory of one contraction block: the rs tile of every z row
+// source radii per staged tile: g(k) (2 nz float2) and charges (nz float)
+__host__ __device__ inline uint32_t contract_tile(uint32_t nx, uint32_t nz) {
+  const uint32_t t = (uint32_t)(kContractSmem / (20 * nz));
+  return t < nx ? t : nx;
+}
+// (bounds the tile of every mesh up to nx_max x nz_max)
 inline size_t contract_smem(uint32_t nx_max, uint32_t nz_max) {
-  return std::min<size_t>(kContractSmem, (size_t)12 * nx_max * nz_max);
+  return std::min<size_t>(kContractSmem, (size_t)20 * nx_max * nz_max);
 }
 
-__global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *sc, ScTables t) {
-  if (!sc->remesh) return;
-  const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
-  const uint32_t rp = blockIdx.x, zp0 = blockIdx.y * kCZ;
-  if (rp > nx || zp0 > nz) return;
-  extern __shared__ float sm[];
-  const uint32_t tr = min(nx, (uint32_t)(kContractSmem / (12 * nz)));  // source radii per tile
-  float2 *gs = (float2 *)sm;       // [dz][tr]
-  float *qs = sm + 2 * nz * tr;    // [zs][tr]
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t zp = zp0 + warp;
-  uint32_t lim;
+// the bin limit of field row zp (the reference's partition of the table)
+__device__ inline uint32_t contract_lim(uint32_t zp, uint32_t rp, uint32_t nx, uint32_t nz) {
+  const uint32_t fld_sz = nx * nz;
   if (zp < nz) {
-    uint32_t gnum = 1024 / nz;
-    lim = gnum ? gnum * (fld_sz / gnum) : 0;
-  } else if (rp < nx) {
-    uint32_t gnum = 1024 / nx;
-    lim = gnum ? gnum * (fld_sz / gnum) : 0;
-  } else {
-    lim = (fld_sz / 1024) * 1024;
+    const uint32_t gnum = 1024 / nz;
+    return gnum ? gnum * (fld_sz / gnum) : 0;
   }
-  const bool cut = lim < fld_sz;  // bins zs * nx + rs >= lim are not summed
+  if (rp < nx) {
+    const uint32_t gnum = 1024 / nx;
+    return gnum ? gnum * (fld_sz / gnum) : 0;
+  }
+  return (fld_sz / 1024) * 1024;
+}
+
+// One block's work; TR > 0 is the tile width known at compile time (nr ==
+// TR, one tile: every shared-memory offset of the row walk is an immediate),
+// TR == 0 the general tiled form.
+template <int TR>
+__device__ __forceinline__ void contract_block(const ScState *sc, const ScTables &t, float *sm,
+                                               float2 (*upper)[kCP]) {
+  const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
+  const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ;
+  const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile(nx, nz);
+  float2 *gz = (float2 *)sm;          // [k + nz - 1][tr], k = -(nz - 1) .. nz
+  float *qs = sm + 4 * nz * tr;       // [zs][tr]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = warp / kCH, half = warp % kCH;
+  const uint32_t zp0 = zb0 + grp * kCP;  // points zp0 .. zp0 + kCP - 1
+  const uint32_t za = half * nz / kCH, zb = (half + 1) * nz / kCH;  // this warp's source rows
+  uint32_t lim[kCP];
+  bool cut = false;
+#pragma unroll
+  for (int j = 0; j < kCP; ++j) {
+    lim[j] = contract_lim(zp0 + j, rp, nx, nz);
+    cut |= zp0 + j <= nz && lim[j] < fld_sz;
+  }
   const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * fld_sz;  // [dz][rs]
-  float ax0 = 0.0f, az0 = 0.0f, ax1 = 0.0f, az1 = 0.0f;
+  float ax[kCP], az[kCP];
+#pragma unroll
+  for (int j = 0; j < kCP; ++j) ax[j] = az[j] = 0.0f;
   for (uint32_t rs0 = 0; rs0 < nx; rs0 += tr) {
-    const uint32_t ntr = min(tr, nx - rs0), ntile = nz * ntr;
+    const uint32_t ntr = TR > 0 ? (uint32_t)TR : min(tr, nx - rs0), ntile = nz * ntr;
     __syncthreads();
     // every load of a thread's share is issued before its first store: one
     // memory round trip per kStage elements, not per element
@@ -530,55 +557,86 @@ __global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *
         const uint32_t e = e0 + u * blockDim.x;
         if (e < ntile) {
           const uint32_t z = e / ntr, r = e - z * ntr;
-          gs[z * tr + r] = gv[u];
+          gz[(nz + z) * tr + r] = gv[u];                                  // k = z + 1
+          gz[(nz - 1 - z) * tr + r] = make_float2(gv[u].x, -gv[u].y);     // k = -z
           qs[z * tr + r] = fixed_to_float(bv[u]);
         }
       }
     }
     __syncthreads();
-    if (zp > nz) continue;
+    if (zp0 > nz) continue;
     for (uint32_t r = lane; r < ntr; r += 32) {
-      const uint32_t rs = rs0 + r;
-      // bins zs * nx + rs >= lim are left out: source rows zs < zend
-      const uint32_t zend = !cut ? nz : (lim > rs ? min(nz, (lim - rs + nx - 1) / nx) : 0u);
-      // sources below the point: dz = zp - zs - 1, +E_z
-      const uint32_t zb = min(zend, zp);
-      const float *q = qs + r;
-      const float2 *g = gs + r;
-#pragma unroll 4
-      for (uint32_t zs = 0; zs < zb; ++zs) {
-        const float bv = q[zs * tr];
-        const float2 gv = g[(zp - 1 - zs) * tr];
-        ax0 = fmaf(bv, gv.x, ax0);
-        az0 = fmaf(bv, gv.y, az0);
-      }
-      // sources at or above it (points zp < nz only): dz = zs - zp, -E_z
-      if (zp < zend) {
-        const float *q1 = qs + (size_t)zp * tr + r;
-        const float2 *g1 = gs + r;
-        const uint32_t cnt = zend - zp;
-#pragma unroll 4
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const float bv = q1[k * tr];
-          const float2 gv = g1[k * tr];
-          ax1 = fmaf(bv, gv.x, ax1);
-          az1 = fmaf(-bv, gv.y, az1);
+      if (!cut) {
+        // ring slot (j - u) mod R holds g(zp0 + j - zs), u = zs - zs0; the
+        // slot (-u - 1) mod R is free at row zs and takes g(zp0 - zs - 1).
+        // gp walks g(zp0 - zs - 1) down the rows, qp the charges up.
+        constexpr int R = kCP + 1;
+        float2 ring[R];
+        const float2 *g = gz + (nz - 1) * tr + r;  // g(k) at g[k * tr]
+#pragma unroll
+        for (int j = 0; j < kCP; ++j) ring[j] = g[min((int)(zp0 + j) - (int)za, (int)nz) * (int)tr];
+        const float2 *gp = g + ((int)zp0 - (int)za - 1) * (int)tr;
+        const float *qp = qs + za * tr + r;
+        for (uint32_t zs0 = za; zs0 < zb; zs0 += R, gp -= R * tr, qp += R * tr) {
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            if (zs0 + u >= zb) break;
+            if (zs0 + u + 1 < zb) ring[(R - 1 - u) % R] = gp[-(int)(u * tr)];
+            const float qv = qp[u * tr];
+#pragma unroll
+            for (int j = 0; j < kCP; ++j) {
+              const float2 gv = ring[(j - u + R) % R];
+              ax[j] = fmaf(qv, gv.x, ax[j]);
+              az[j] = fmaf(qv, gv.y, az[j]);
+            }
+          }
+        }
+      } else {
+        // small meshes: each point sums the source rows below its own limit
+        const float *q = qs + r;
+        const float2 *g = gz + (nz - 1) * tr + r;
+        const uint32_t rs = rs0 + r;
+        for (int j = 0; j < kCP; ++j) {
+          if (zp0 + j > nz) continue;
+          const uint32_t zend = lim[j] > rs ? min(zb, (lim[j] - rs + nx - 1) / nx) : 0u;
+          for (uint32_t zs = za; zs < zend; ++zs) {
+            const float qv = q[zs * tr];
+            const float2 gv = g[((int)(zp0 + j) - (int)zs) * (int)tr];
+            ax[j] = fmaf(qv, gv.x, ax[j]);
+            az[j] = fmaf(qv, gv.y, az[j]);
+          }
         }
       }
     }
   }
-  if (zp > nz) return;
-  float sx = ax0 + ax1, sz = az0 + az1;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    sx += __shfl_down_sync(0xffffffffu, sx, off);
-    sz += __shfl_down_sync(0xffffffffu, sz, off);
+  for (int j = 0; j < kCP; ++j) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      ax[j] += __shfl_down_sync(0xffffffffu, ax[j], off);
+      az[j] += __shfl_down_sync(0xffffffffu, az[j], off);
+    }
   }
-  if (lane == 0) {
-    size_t pt = (size_t)zp * nrow + rp;
-    t.ffld2[2 * pt] = sx;
-    t.ffld2[2 * pt + 1] = sz;
+  if (half == 1 && lane == 0)
+    for (int j = 0; j < kCP; ++j) upper[grp][j] = make_float2(ax[j], az[j]);
+  __syncthreads();
+  if (half != 0 || lane != 0 || zp0 > nz) return;
+  for (int j = 0; j < kCP; ++j) {
+    if (zp0 + j > nz) break;
+    const size_t pt = (size_t)(zp0 + j) * nrow + rp;
+    t.ffld2[2 * pt] = ax[j] + upper[grp][j].x;
+    t.ffld2[2 * pt + 1] = az[j] + upper[grp][j].y;
   }
+}
+
+__global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *sc, ScTables t) {
+  if (!sc->remesh) return;
+  const uint32_t nx = sc->nx, nz = sc->nz;
+  if (blockIdx.x > nx || blockIdx.y * kCZ > nz) return;
+  extern __shared__ float sm[];
+  __shared__ float2 upper[kCG][kCP];  // second halves' sums
+  if (nx == 32 && contract_tile(nx, nz) == 32) contract_block<32>(sc, t, sm, upper);
+  else contract_block<0>(sc, t, sm, upper);
 }
 
 // ---- kick ----------------------------------------------------------------------
@@ -674,16 +732,17 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   size_t hb = 0;
   DepQ q{};
   if (a.deposit_ok) {
-    // two blocks per SM at most, in whole clusters
-    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, 2u * 152u);
+    // three blocks per SM at most, in whole clusters
+    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, 3u * 152u);
     ndep = (ndep + kDepCluster - 1) / kDepCluster * kDepCluster;
     hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
     if (hb > kMaxHistSmem) hb = 0;
     q = dep_quant(b.n, (int)ndep, hb);
   }
-  // Green's table entries of the largest mesh, one per thread
+  // Green's table entries of the largest mesh, a few per thread on one block
+  // per SM, so that the whole launch is resident at once
   uint32_t ngreen = std::min<uint32_t>(
-      (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 4u * 152u);
+      (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 152u);
   ngreen = (ngreen + kDepCluster - 1) / kDepCluster * kDepCluster;
   launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
   note_launch();
