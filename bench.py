@@ -172,11 +172,15 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic(phase, prec):
+def load_traffic(phase, prec, n):
+    """DRAM bytes per launch of a kernel class from an ncu capture at
+    1048576 particles, scaled to n particles (the sweeps' traffic grows in
+    proportion)."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
             t = json.load(fh)
-        return t.get(f"{prec}:{phase}")
+        v = t.get(f"{prec}:{phase}")
+        return None if v is None else v * n / 1048576
     except (OSError, ValueError):
         return None
 
@@ -304,7 +308,7 @@ def main():
     per_launch_s = dom_ms / 1000.0 / max(dom_n, 1)
     peak, peak_kind = load_peaks()
     achieved = algorithmic_bytes(dom, args.particles, args.precision) / per_launch_s / 1e9
-    traffic = load_traffic(dom, args.precision)
+    traffic = load_traffic(dom, args.precision, args.particles)
     # the whole step against the minimum traffic of a particle-element step
     step_gbs = value / ws * STEP_BYTES[args.precision] / 1e9
 

@@ -9,7 +9,10 @@ benchmarks are quoted on:
 * ``small_fodo``: buncher + 40 alternating 0.10 m drifts / 0.05 m quads
   (+-18 T/m), 65,536 particles, SCHEFF 32x128 after every element, FP64.
 * ``dtl_like``: 165 DTL RF gaps (E0 = 2.5 MV/m, phi_s = -26 deg) between 0.04 m
-  quads (+-45 T/m); the cell lengths and RF phase offsets come from tracking
+  quads (+-80 T/m: at +-45 T/m the zero-current phase advance at 0.75 MeV is
+  ~10 deg per period and the 15 mA beam is lost; +-80 T/m gives 60-80 deg and
+  a stable beam through all 331 elements); the cell lengths and RF phase
+  offsets come from tracking
   the synchronous particle through the gap formulas of
   src/simulation/inc/simulation_kernel.cu:226-497 (on axis, FP64).
 * ``ccl_like``: 805 MHz coupled-cavity gaps from 100 MeV with doublets.
