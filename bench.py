@@ -55,6 +55,25 @@ def dist_env():
     return ws, rank, local
 
 
+def slowest(t_local, ws, device=None):
+    """The largest of the ranks' times (every rank gets it); t_local alone
+    when there is one rank."""
+    if ws <= 1:
+        return t_local
+    import torch
+    import torch.distributed as dist
+    x = torch.tensor([t_local], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def job_value(t_step_local, ws, particles, n_elem, device=None):
+    """Whole-job throughput of ws replica beams: every rank's particle-element
+    steps over the slowest rank's step time.  Returns (value, that time)."""
+    t = slowest(t_step_local, ws, device)
+    return ws * particles * n_elem / t, t
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -290,12 +309,8 @@ def main():
     wall = time.perf_counter() - wall0
     launches = HPSim.kernel_launch_count() - launches0
     stat_sweeps = (sc.get_counter("stat_sweeps") - sweeps0) / args.steps
-    t_step = sum(dev_ms) / len(dev_ms) / 1000.0
-    if ws > 1:
-        t = torch.tensor([t_step], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = ws * args.particles * n_elem / t_step
+    value, t_step = job_value(sum(dev_ms) / len(dev_ms) / 1000.0, ws, args.particles, n_elem,
+                              device=f"cuda:{local}")
 
     # per-phase breakdown of one more (untimed) step: dominant kernel + roofline
     sim.profile(True)
@@ -346,8 +361,8 @@ def main():
         for _ in range(ek):
             e2e_step()
         barrier()
-        te = (time.perf_counter() - t0) / ek
-        e2e = {"value": ws * n * n_elem / te, "unit": METRIC, "h2d_bytes_per_step": n * (6 * 8 + 4 + 4),
+        te_value, _ = job_value((time.perf_counter() - t0) / ek, ws, n, n_elem, device=f"cuda:{local}")
+        e2e = {"value": te_value, "unit": METRIC, "h2d_bytes_per_step": n * (6 * 8 + 4 + 4),
                "d2h_bytes_per_step": n * (6 * 8 + 4)}
 
     if rank != 0:
