@@ -329,14 +329,17 @@ class Beam:
 
 
 class DBConnection:
-    """DBConnection(db_file) over Python's sqlite3 (wrap_dbconnection.cpp).
+    """DBConnection(db_file) over Python's sqlite3 (wrap_dbconnection.cpp,
+    sql_utility.cpp:211-367).  The lattice loader is hpsim_gb300/dbloader.py.
 
-    The lattice loader lives in hpsim_gb300/dbloader.py."""
+    ``load_lib`` records the SQL extension's name without loading it: the
+    loader reads the ``*_model`` columns, which do not need it."""
 
     def __init__(self, db_addr):
         from .dbloader import open_connection
         self._conn, self.dbs = open_connection(db_addr)
         self.libs = []
+        self.model_index = {}
 
     def attach_db(self, db_addr, db_name=None):
         from .dbloader import attach
@@ -346,12 +349,24 @@ class DBConnection:
         self.libs.append(lib_name)
 
     def print_dbs(self):
+        if not self.dbs:
+            print("DBConnection is not connected to any db.")
         for name, path in self.dbs:
-            print(name, path)
+            print(f"{name} -> {path}")
 
     def print_libs(self):
+        if not self.libs:
+            print("No lib is loaded for this DBConnection.")
         for name in self.libs:
             print(name)
+
+    def clear_model_index(self):
+        from .dbloader import clear_model_index
+        clear_model_index(self)
+
+    def get_epics_channels(self):
+        from .dbloader import epics_channels
+        return epics_channels(self)
 
 
 class BeamLine:

@@ -12,12 +12,54 @@ import re
 
 import numpy as np
 
-_NUM = re.compile(r"^[\s0-9eE+\-.]+$")
-
 
 def _first_number(line):
-    m = re.search(r"[-+]?\d+(\.\d*)?([eE][-+]?\d+)?", line)
-    return float(m.group(0)) if m else None
+    """GetFirstNumberInString (src/util/src/utility.cpp:31-74): digits with
+    one optional sign (only directly before a digit) and one dot, stopping at
+    the first other character -- no exponent, so '1.5e-05' reads as 1.5."""
+    out, started, dot = [], False, False
+    for i, ch in enumerate(line):
+        if ch in "+-":
+            if not started and i < len(line) - 1 and line[i + 1].isdigit():
+                started = True
+                out.append(ch)
+            elif started:
+                break
+        elif ch == ".":
+            if started and not dot:
+                out.append(ch)
+                dot = True
+            elif dot:
+                break
+        elif ch.isdigit():
+            out.append(ch)
+            started = True
+        elif started:
+            break
+    return _atof("".join(out))
+
+
+def _atof(s):
+    """std::atof: the longest leading number, 0 when there is none."""
+    m = re.match(r"\s*[-+]?(\d+(\.\d*)?|\.\d+)([eE][-+]?\d+)?", s)
+    return float(m.group(0)) if m else 0.0
+
+
+def _atoi(s):
+    m = re.match(r"\s*[-+]?\d+", s)
+    return int(m.group(0)) if m else 0
+
+
+def _contains_numbers(line):
+    return any(ch.isdigit() for ch in line)
+
+
+def _only_numbers(line):
+    """ContainOnlyNumbers (utility.cpp:98-110): with the spaces removed (only
+    spaces), every character is a digit, '.', '-', 'e' or 'E'; a line with a
+    tab or a '+' is not a particle line."""
+    s = line.rstrip("\n").replace(" ", "")
+    return bool(s) and all(ch.isdigit() or ch in ".-eE" for ch in s)
 
 
 def write_beam_file(path, msg, charge, mass, current, freq, cols, loss, lloss):
@@ -34,27 +76,42 @@ def write_beam_file(path, msg, charge, mass, current, freq, cols, loss, lloss):
 
 
 def read_beam_file(path):
-    """Return (mass, charge, current, freq, [x, xp, y, yp, phi, w, loss, lloss])."""
+    """Beam::InitBeamFromFile + UpdateBeamFromFile (beam.cpp:179-298).
+
+    Returns (mass, charge, current, freq, [x, xp, y, yp, phi, w, loss,
+    lloss]).  Header values: the first number of the last line that
+    mentions the key (case-insensitive) and holds a digit.  Particle lines:
+    those of numbers only; the loss columns are read when the *last*
+    particle line has them (a shorter line then gives 0 where the reference
+    leaves the value unset).  The first particle is put on axis."""
     vals = {}
     rows = []
     with open(path) as f:
         for line in f:
             low = line.lower()
             for key in ("charge", "mass", "current", "frequency"):
-                if key in low and re.search(r"\d", line):
+                if key in low and _contains_numbers(line):
                     vals[key] = _first_number(line)
-            if line.strip() and _NUM.match(line):
-                rows.append([float(v) for v in line.split()])
+            if _only_numbers(line):
+                rows.append(line.split())
     for key in ("charge", "mass", "current", "frequency"):
         if key not in vals:
             raise ValueError(f"Beam input file error: must define {key} value!")
-    ncol = max((len(r) for r in rows), default=6)
+    if not rows:
+        raise ValueError("Beam input file error: no particle lines")
     n = len(rows)
-    a = np.zeros((n, max(ncol, 8)))
+    cols = [np.zeros(n) for _ in range(6)]
+    loss = np.zeros(n, dtype=np.uint32)
+    lloss = np.zeros(n, dtype=np.uint32)
     for i, r in enumerate(rows):
-        a[i, :len(r)] = r
-    x, xp, y, yp, phi, w = (a[:, k].copy() for k in range(6))
+        for k in range(6):
+            cols[k][i] = _atof(r[k]) if k < len(r) else 0.0
+        if len(r) > 6:
+            loss[i] = _atoi(r[6]) & 0xffffffff
+        if len(r) > 7:
+            lloss[i] = _atoi(r[7]) & 0xffffffff
+    ncol = len(rows[-1])
+    x, xp, y, yp, phi, w = cols
     x[0] = xp[0] = y[0] = yp[0] = 0.0
-    loss = a[:, 6].astype(np.uint32) if ncol > 6 else None
-    lloss = a[:, 7].astype(np.uint32) if ncol > 7 else None
-    return vals["mass"], vals["charge"], vals["current"], vals["frequency"], [x, xp, y, yp, phi, w, loss, lloss]
+    return (vals["mass"], vals["charge"], vals["current"], vals["frequency"],
+            [x, xp, y, yp, phi, w, loss if ncol > 6 else None, lloss if ncol > 7 else None])

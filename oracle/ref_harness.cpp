@@ -545,6 +545,14 @@ void ref_beam_set_distribution(void *bp, const double *x, const double *xp, cons
   if (lloss) vll.assign(lloss, lloss + n);
   b->InitBeamFromDistribution(vx, vxp, vy, vyp, vp, vw, loss ? &vl : nullptr, lloss ? &vll : nullptr);
 }
+// Beam::PrintToFile and Beam(file) (beam.cpp:47-60, 179-298, 670-707)
+void ref_beam_print(void *b, const char *file, const char *msg) { ((Beam *)b)->PrintToFile(file, msg); }
+void *ref_beam_from_file(const char *file) { return new Beam(std::string(file)); }
+uint ref_beam_size(void *b) { return ((Beam *)b)->num_particle; }
+void ref_beam_scalars(void *bp, double *out) {
+  Beam *b = (Beam *)bp;
+  out[0] = b->mass; out[1] = b->charge; out[2] = b->current; out[3] = b->freq; out[4] = b->design_w;
+}
 void ref_beam_set_ref_w(void *b, double w) { ((Beam *)b)->SetRefEnergy(w); }
 void ref_beam_set_ref_phi(void *b, double p) { ((Beam *)b)->SetRefPhase(p); }
 void ref_beam_set_frequency(void *b, double f) { ((Beam *)b)->freq = f; }
