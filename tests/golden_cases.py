@@ -15,8 +15,10 @@ MON_COLS = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19
 
 
 def case_names():
+    """Tracking cases (fixtures with a run description); distributions,
+    SCHEFF tables, beam files and lattice records have their own tests."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("initial_", "scheff_tables")))
+                  if not os.path.basename(p).startswith(("initial_", "scheff_tables", "beam_files", "db_")))
 
 
 def load(name):
