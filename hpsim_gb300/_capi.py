@@ -67,6 +67,10 @@ def lib():
         "hps_beam_apply_cut": (st, [vp, C.c_char, d, d]),
         "hps_beam_translate": (st, [vp, i32, d]),
         "hps_beam_monitor": (st, [vp, dp]),
+        "hps_plot_points": (st, [vp, i32, i32, vp, i32]),
+        "hps_plot_maxmin": (st, [vp, i32, i32, i32, dp]),
+        "hps_plot_histogram": (st, [vp, i32, u32, d, d, vp, i32]),
+        "hps_plot_histogram2d": (st, [vp, i32, i32, u32, u32, dp, vp, i32]),
         "hps_beamline_create": (st, [pvp]),
         "hps_beamline_destroy": (st, [vp]),
         "hps_beamline_add": (st, [vp, i32, cp, dp]),

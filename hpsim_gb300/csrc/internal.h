@@ -146,4 +146,23 @@ void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, con
 // constants of the FP32 kernels of a kick
 Sc32Host sc32_host(const DevBeam &b, const ScKickArgs &a);
 
+// ---- headless plot data (plot.cu) -----------------------------------------
+// one coordinate of a beam as FP64 values: d[i] (FP64 beams) or
+// off + f[i] (FP32 beams: offset from the synchronous particle)
+struct PlotCoord {
+  const double *d;
+  const float *f;
+  double off;
+};
+void plot_points(const PlotCoord &x, const PlotCoord &y, const uint32_t *loss, uint32_t n, float2 *out,
+                 cudaStream_t st);
+// out (device): xmax, xmin, ymax, ymin; loss == nullptr counts every particle
+void plot_maxmin(const PlotCoord &x, const PlotCoord &y, const uint32_t *loss, uint32_t n, PassScratch scr,
+                 double *out, cudaStream_t st);
+void plot_hist(const PlotCoord &x, const uint32_t *loss, uint32_t n, uint32_t nb, double mn, double mx,
+               uint32_t *hist, cudaStream_t st);
+// mm: xmax, xmin, ymax, ymin (host)
+void plot_hist2d(const PlotCoord &x, const PlotCoord &y, const uint32_t *loss, uint32_t n, const double mm[4],
+                 uint32_t nx, uint32_t ny, uint32_t *hist, cudaStream_t st);
+
 }  // namespace hps

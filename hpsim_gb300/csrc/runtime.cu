@@ -593,6 +593,78 @@ hps_status hps_beam_monitor(hps_beam_t b, double *out) {
   return s;
 }
 
+// ---- headless plot data (src/graphics/src/graphics_kernel_call.cu) ----------
+static PlotCoord plot_coord(hps_beam_t b, int c) {
+  PlotCoord p{};
+  if (f32(b)) {
+    p.f = (const float *)coord_ptr(b, c);
+    p.off = c == HPS_COORD_PHI ? b->d.phi_ref : c == HPS_COORD_W ? b->d.w_ref : 0.0;
+  } else {
+    p.d = (const double *)coord_ptr(b, c);
+  }
+  return p;
+}
+static bool plot_coord_ok(int c) { return c >= 0 && c <= HPS_COORD_PHI_R; }
+
+// a device buffer for a result the caller wants on the host (else theirs)
+static hps_status plot_out(void *user, size_t bytes, int on_device, void **dev) {
+  if (on_device) { *dev = user; return HPS_OK; }
+  CK(cudaMalloc(dev, bytes));
+  return HPS_OK;
+}
+static hps_status plot_finish(hps_beam_t b, void *user, void *dev, size_t bytes, int on_device) {
+  if (!on_device) cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, b->stream);
+  hps_status s = last_launch_status("plot");
+  if (!s) s = sync(b);
+  if (!on_device) cudaFree(dev);
+  return s;
+}
+
+hps_status hps_plot_points(hps_beam_t b, int cx, int cy, float *xy, int on_device) {
+  if (!valid(b) || !xy || !plot_coord_ok(cx) || !plot_coord_ok(cy)) return fail(HPS_ERR_INVALID, "plot_points: bad argument");
+  const size_t bytes = (size_t)b->n * sizeof(float2);
+  void *dev = nullptr;
+  hps_status s = plot_out(xy, bytes, on_device, &dev);
+  if (s) return s;
+  plot_points(plot_coord(b, cx), plot_coord(b, cy), b->d.loss, b->n, (float2 *)dev, b->stream);
+  return plot_finish(b, xy, dev, bytes, on_device);
+}
+
+hps_status hps_plot_maxmin(hps_beam_t b, int cx, int cy, int live_only, double out[4]) {
+  if (!valid(b) || !out || !plot_coord_ok(cx) || !plot_coord_ok(cy)) return fail(HPS_ERR_INVALID, "plot_maxmin: bad argument");
+  void *dev = nullptr;
+  hps_status s = plot_out(out, 4 * sizeof(double), 0, &dev);
+  if (s) return s;
+  plot_maxmin(plot_coord(b, cx), plot_coord(b, cy), live_only ? b->d.loss : nullptr, b->n, b->scr, (double *)dev,
+              b->stream);
+  return plot_finish(b, out, dev, 4 * sizeof(double), 0);
+}
+
+hps_status hps_plot_histogram(hps_beam_t b, int coord, uint32_t nbins, double mn, double mx, uint32_t *hist,
+                              int on_device) {
+  if (!valid(b) || !hist || !plot_coord_ok(coord) || nbins < 1 || nbins > HPS_PLOT_MAX_BINS || !(mx > mn))
+    return fail(HPS_ERR_INVALID, "plot_histogram: bad argument (1 <= nbins <= 12288, max > min)");
+  const size_t bytes = (size_t)nbins * sizeof(uint32_t);
+  void *dev = nullptr;
+  hps_status s = plot_out(hist, bytes, on_device, &dev);
+  if (s) return s;
+  plot_hist(plot_coord(b, coord), b->d.loss, b->n, nbins, mn, mx, (uint32_t *)dev, b->stream);
+  return plot_finish(b, hist, dev, bytes, on_device);
+}
+
+hps_status hps_plot_histogram2d(hps_beam_t b, int cx, int cy, uint32_t nx, uint32_t ny, const double maxmin[4],
+                                uint32_t *hist, int on_device) {
+  if (!valid(b) || !hist || !maxmin || !plot_coord_ok(cx) || !plot_coord_ok(cy) || nx < 1 || ny < 1 ||
+      (uint64_t)nx * ny > (1ull << 26))
+    return fail(HPS_ERR_INVALID, "plot_histogram2d: bad argument");
+  const size_t bytes = (size_t)nx * ny * sizeof(uint32_t);
+  void *dev = nullptr;
+  hps_status s = plot_out(hist, bytes, on_device, &dev);
+  if (s) return s;
+  plot_hist2d(plot_coord(b, cx), plot_coord(b, cy), b->d.loss, b->n, maxmin, nx, ny, (uint32_t *)dev, b->stream);
+  return plot_finish(b, hist, dev, bytes, on_device);
+}
+
 // ---- BeamLine ---------------------------------------------------------------
 hps_status hps_beamline_create(hps_beamline_t *out) {
   if (!out) return fail(HPS_ERR_INVALID, "null output");

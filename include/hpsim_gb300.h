@@ -115,6 +115,28 @@ hps_status hps_beam_translate(hps_beam_t beam, int coord, double value);
 /* side-effect-free statistics record (HPS_MON_*) */
 hps_status hps_beam_monitor(hps_beam_t beam, double *out /* HPS_NMON */);
 
+/* ---- headless plot data (src/graphics/inc/graphics_kernel.cu, launchers
+ * src/graphics/src/graphics_kernel_call.cu) into plain memory instead of GL
+ * buffers.  Coordinates are HPS_COORD_* (x, xp, y, yp, phi, w, phi_r).
+ * Outputs go to host memory, or, with on_device != 0, to caller-allocated
+ * device memory on the current device. */
+#define HPS_PLOT_MAX_BINS 12288
+/* SetPhaseSpaceData / Set2dPhaseSpaceDataKernel: 2*num floats (x, y) per
+ * particle, lost particles at (0, 0) */
+hps_status hps_plot_points(hps_beam_t beam, int cx, int cy, float *xy, int on_device);
+/* FindMaxMin2D / BlockMaxMin2DKernel: out = xmax, xmin, ymax, ymin; with
+ * live_only a lost particle counts as particle 0 (the reference's filler);
+ * NaN values are skipped */
+hps_status hps_plot_maxmin(hps_beam_t beam, int cx, int cy, int live_only, double out[4]);
+/* UpdateHistogram / HistogramKernel + HistogramReduceKernel over live
+ * particles, the reference's bin rule (see plot.cu) */
+hps_status hps_plot_histogram(hps_beam_t beam, int coord, uint32_t nbins, double min, double max,
+                              uint32_t *hist, int on_device);
+/* UpdateHistogram2DKernelCall / Histogram2DKernel: nx*ny counts (row iy),
+ * maxmin as hps_plot_maxmin returns it */
+hps_status hps_plot_histogram2d(hps_beam_t beam, int cx, int cy, uint32_t nx, uint32_t ny,
+                                const double maxmin[4], uint32_t *hist, int on_device);
+
 #define HPS_ST_X_AVG 0
 #define HPS_ST_X_AVG_GOOD 1
 #define HPS_ST_XP_AVG 2
