@@ -70,9 +70,16 @@ struct QuadMap {
     float x = p.x, y = p.y, xp = p.xp, yp = p.yp;
     uint32_t m;
     if (qg == 0.0f) {
-      x = x + xp * len * 0.5f;
-      y = y + yp * len * 0.5f;
+      // the drifted coordinates are stored, but the aperture test below sees
+      // the ones before the half (the reference writes memory and tests its
+      // unchanged locals)
+      p.x = x + xp * len * 0.5f;
+      p.y = y + yp * len * 0.5f;
       m = WR_X | WR_Y;
+      if (aper2 != 0.0f && x * x + y * y > aper2) { p.lo = eid; return m | WR_LOSS; }
+      float g, beta;
+      p.ph = fmaf(c, dinvb(p.w, r, g, beta), p.ph);
+      return m | WR_PH;
     } else {
       const float g = fmaf(p.w, r.minv, r.g);
       const float bg = sqrtf(g * (g + 2.0f) * (1.0f + xp * xp + yp * yp));
