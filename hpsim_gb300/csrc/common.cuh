@@ -125,15 +125,21 @@ __host__ __device__ inline RefK make_refk(double w, double mass) {
 
 // 1/beta_i - 1/beta_ref for a particle dw above the reference, computed from
 // beta_i^2 - beta_r^2 = (gamma_i^2 - gamma_r^2)/(gamma_i^2 gamma_r^2) so the
-// difference keeps FP32 relative precision; also returns g_i = W_i/m and beta_i.
-__device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta) {
+// difference keeps FP32 relative precision:
+//   1/beta_i - 1/beta_r = -(dgamma (gamma_i + gamma_r)) /
+//                          (gamma_i gamma_r^2 (beta_i + beta_r) (beta gamma)_i beta_r)
+// (one division); also returns g_i = W_i/m, beta_i and (beta gamma)_i.
+__device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta, float &bg) {
   g = fmaf(dw, r.minv, r.g);
-  float gam = g + 1.0f;
-  float bg = sqrtf(g * (g + 2.0f));
+  const float gam = g + 1.0f;
+  bg = sqrtf(g * (g + 2.0f));
   beta = bg / gam;
-  float dg = dw * r.minv;
-  float db = dg * (gam + r.gam) / (gam * gam * r.gam * r.gam * (beta + r.beta));
-  return -db / (beta * r.beta);
+  const float dg = dw * r.minv;
+  return -(dg * (gam + r.gam)) / (gam * r.gam * r.gam * (beta + r.beta) * bg * r.beta);
+}
+__device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta) {
+  float bg;
+  return dinvb(dw, r, g, beta, bg);
 }
 
 // deposit weights are accumulated as integers: deterministic in any order

@@ -448,7 +448,8 @@ void push32_gap_second(DevBeam &b, const GapArgs &g, cudaStream_t st, const Push
       phi_h = b.phi_ref + (1.0 - (beta_h - beta_out) / beta_h) * A + prome + dphi_clen - dphi_qlen2;
       K2 = beta_out * A + (dc ? PI * d_cell_len / wave_len : 0.0) - PI * g.q2 / wave_len;
     }
-    G.beta_in = (float)beta_in; G.betag_ccl = (float)betag_ccl; G.gmg = (float)gmg; G.q = (float)q;
+    G.beta_in = (float)beta_in; G.inv_beta_in = (float)(1.0 / beta_in); G.betag_ccl = (float)betag_ccl;
+    G.gmg = (float)gmg; G.inv_gmg = (float)(1.0 / gmg); G.q = (float)q;
     G.efl = (float)efl; G.efl_m = (float)(efl * inv_mass); G.concomm = (float)concomm;
     G.concomm1 = (float)concomm1; G.con1 = (float)con1; G.con2nex = (float)con2nex;
     G.inv_gmg2 = (float)inv_gmg2; G.inv_gmgcl = (float)inv_gmgcl; G.inv_fkis = (float)inv_fkis;

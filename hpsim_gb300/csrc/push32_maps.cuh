@@ -151,14 +151,14 @@ struct Gap1Map {
 __device__ inline float fbessi0c(float x, float *m1) {
   const float ax = fabsf(x);
   if (ax < 3.75f) {
-    float cy = x / 3.75f;
+    float cy = x * (1.0f / 3.75f);
     cy = cy * cy;
     const float s = cy * (3.5156229f + cy * (3.0899424f + cy * (1.2067492f + cy * (0.2659732f +
                     cy * (0.360768e-1f + cy * 0.45813e-2f)))));
     *m1 = s;
     return 1.0f + s;
   }
-  const float cy = 3.75f / ax;
+  const float cy = __fdividef(3.75f, ax);
   const float ans = (expf(ax) * rsqrtf(ax)) * (0.39894228f + cy * (0.1328592e-1f + cy * (0.225319e-2f +
                     cy * (-0.157565e-2f + cy * (0.916281e-2f + cy * (-0.2057706e-1f + cy * (0.2635537e-1f +
                     cy * (-0.1647633e-1f + cy * 0.392377e-2f))))))));
@@ -169,12 +169,12 @@ __device__ inline float fbessi1c(float x) {
   const float ax = fabsf(x);
   float ans;
   if (ax < 3.75f) {
-    float cy = x / 3.75f;
+    float cy = x * (1.0f / 3.75f);
     cy = cy * cy;
     ans = ax * (0.5f + cy * (0.87890594f + cy * (0.51498869f + cy * (0.15084934f + cy * (0.2658733e-1f +
           cy * (0.301532e-2f + cy * 0.32411e-3f))))));
   } else {
-    const float cy = 3.75f / ax;
+    const float cy = __fdividef(3.75f, ax);
     ans = 0.2282967e-1f + cy * (-0.2895312e-1f + cy * (0.1787654e-1f - cy * 0.420059e-2f));
     ans = 0.39894228f + cy * (-0.3988024e-1f + cy * (-0.362018e-2f + cy * (0.163801e-2f + cy *
           (-0.1031555e-1f + cy * ans))));
@@ -193,8 +193,8 @@ struct Gap2Map {
   RefK rin, rh;          // reference before the gap, reference after its (hypothetical) kick
   float dd2, drift_c;    // drift branch: phi += drift_c / beta
   float fbc, fbm, b0, tc[6], sc[6], inv2pifbc;  // T(beta), S(beta) as Taylor series about b0
-  float beta_in, betag_ccl, gmg, q, efl, efl_m, concomm, concomm1, con1, con2nex, inv_gmg2, inv_gmgcl,
-      inv_fkis, fkr, sinps, cosps, X, ccl_dg;
+  float beta_in, inv_beta_in, betag_ccl, gmg, inv_gmg, q, efl, efl_m, concomm, concomm1, con1, con2nex, inv_gmg2,
+      inv_gmgcl, inv_fkis, fkr, sinps, cosps, X, ccl_dg;
   float sinF, cosF, prome1_r, sinP, cosP, tw_r, prome_r, K2;
   float dphi_ref, dw_ref;  // actual reference change
   float corr_phi, corr_w;  // hypothetical minus actual reference after the gap
@@ -203,9 +203,8 @@ struct Gap2Map {
     const Gap2Map &G = *this;
     float x = p.x, y = p.y, xp = p.xp, yp = p.yp;
     const float dphi = p.ph, dw = p.w;
-    float g, beta;
-    const float D = dinvb(dw, G.rin, g, beta);
-    const float bg1 = sqrtf(g * (g + 2.0f));
+    float g, beta, bg1;
+    const float D = dinvb(dw, G.rin, g, beta, bg1);
     // GetTransitTimeFactors (simulation_kernel.cu:290-308) about the reference's beta
     float bcl = beta;
     if (beta > 1.1f * G.fbc) bcl = G.fbc;
@@ -230,7 +229,7 @@ struct Gap2Map {
     }
     float tw, dtw;
     if (G.ccl) {
-      tw = t - F_TWOPI * tp * (G.beta_in / beta - 1.0f) * G.betag_ccl / G.beta_in;
+      tw = t - F_TWOPI * tp * (__fdividef(G.beta_in, beta) - 1.0f) * G.betag_ccl * G.inv_beta_in;
       dtw = tw - G.tw_r;
     } else {
       tw = t;
@@ -255,24 +254,23 @@ struct Gap2Map {
     float b0m1;
     const float b0c = fbessi0c(fkrris, &b0m1);
     const float b1c = fbessi1c(fkrris);
-    const float b1p = fkrris != 0.0f ? b0c - b1c / fkrris : 0.5f;
-    const float bes1covr = ris != 0.0f ? b1c / ris : G.fkr * 0.5f;
-    const float rest =
-        ((tw - F_TWOPI * tp) / G.gmg * bes1covr + tw / G.gmg * G.fkr * b1p - tw * G.gmg * bes1covr) * rrp * sinp;
+    const float b1p = fkrris != 0.0f ? b0c - __fdividef(b1c, fkrris) : 0.5f;
+    const float bes1covr = ris != 0.0f ? __fdividef(b1c, ris) : G.fkr * 0.5f;
+    const float rest = ((tw - F_TWOPI * tp) * G.inv_gmg * bes1covr + tw * G.inv_gmg * G.fkr * b1p -
+                        tw * G.gmg * bes1covr) * rrp * sinp;
     const float ddelte = G.q * G.efl * (tw * b0c * dcos + (dtw * b0c + G.tw_r * b0m1) * G.cosP + rest);
     const float dwh = dw + ddelte;
-    float gh, betah;
-    const float Dh = dinvb(dwh, G.rh, gh, betah);
-    const float bg = sqrtf(gh * (gh + 2.0f));
-    const float bgr = bg1 / bg;
+    float gh, betah, bg;
+    const float Dh = dinvb(dwh, G.rh, gh, betah, bg);
+    const float bgr = __fdividef(bg1, bg);
     const float onema = 1.0f - (con5nex * bes1covr + con5nex1 * b1p + con5nex2 * bes1covr) * cosp;
     const float dovbl = G.con2nex * bes1covr * tw * sinp;
-    const float bgrovonema = bgr / onema;
+    const float bgrovonema = __fdividef(bgr, onema);
     xp = -dovbl * x + bgrovonema * xp;
     x = x * onema + G.dd2 * xp;
     yp = -dovbl * y + bgrovonema * yp;
     y = y * onema + G.dd2 * yp;
-    const float rpris = rs_p > 0.0f ? rrp / ris : 0.0f;
+    const float rpris = rs_p > 0.0f ? __fdividef(rrp, ris) : 0.0f;
     const float prome = 2.0f * G.con1 * (-tp * b0c + ris * tw * b1c * G.inv_gmgcl) * (sinp - G.sinps) -
                         G.efl_m * tw * b1c * rpris * (cosp - G.cosps);
     const float dphih = dphi + G.K2 * Dh + (prome - G.prome_r);
