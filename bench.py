@@ -45,6 +45,10 @@ def parse():
     p.add_argument("--gaps", type=int, default=GAPS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", default="dtl_like", choices=["dtl_like", "batched"],
+                   help="dtl_like: one 1M-particle beam (the headline); batched: 256 beams of the "
+                        "small-FODO topology in one graph launch")
+    p.add_argument("--beams", type=int, default=256)
     return p.parse_args()
 
 
@@ -261,10 +265,79 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args):
+    """Independent beams of uneven sizes with perturbed RF and quad set points
+    (lattices.batched_scan) advanced by one graph launch per step; value =
+    all beams' particle-element steps / step time."""
+    import torch
+    from hpsim_gb300 import HPSim, build, lattices as L
+    build.build()
+    HPSim.set_gpu(0)
+    scan = L.batched_scan(args.beams)
+    objs = []
+    for sb in scan:
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=sb.num, precision=args.precision)
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, sb.seed)
+        beam.set_ref_w(0.75)
+        beam.set_ref_phi(0.0)
+        beam.save_initial_beam()
+        bl = HPSim.BeamLine(elements=L.scan_lattice(sb))
+        sc = HPSim.SpaceCharge(32, 128, 0.1, 0)
+        sc.set_remesh_threshold(0.0)
+        objs.append((beam, bl, sc, HPSim.Simulator(beam, bl, sc)))
+    batch = HPSim.Batch([o[3] for o in objs])
+    n_elem = len(L.small_fodo())
+    total = sum(sb.num for sb in scan)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:0")
+
+    def step():
+        for o in objs:
+            o[0].restore_initial_beam()
+        batch.simulate()
+        return batch.last_time_ms()
+
+    for _ in range(args.warmup):
+        step()
+    launches0 = HPSim.kernel_launch_count()
+    ms = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms.append(step())
+    launches = HPSim.kernel_launch_count() - launches0
+    t = sum(ms) / len(ms) / 1000.0
+    # the same step with one simulate() per beam, one after another (each its
+    # own graph launch), for comparison
+    for o in objs:
+        o[0].restore_initial_beam()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for o in objs:
+        o[3].simulate()
+    t_seq = time.perf_counter() - t0
+    line = {"metric": METRIC, "value": total * n_elem / t, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "config": {"workload": f"batched scan: {args.beams} beams, particles log-uniform in [16384, 524288] "
+                                   f"(total {total}), small-FODO topology ({n_elem} elements) with per-beam RF "
+                                   f"scale, phase offset and quad scale, SCHEFF 32x128 at every element, one "
+                                   f"graph launch per step", "beams": args.beams, "particles": total,
+                       "elements": n_elem, "precision": args.precision,
+                       "l2": "flushed between steps (256 MB write)"},
+            "sequential": {"ms_per_step": 1000 * t_seq, "value": total * n_elem / t_seq,
+                           "note": "one simulate() per beam in turn, wall clock"},
+            "e2e": None, "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "batched":
+        run_batched(args)
         return
     ws, rank, local = dist_env()
     import numpy as np

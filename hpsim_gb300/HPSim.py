@@ -611,3 +611,37 @@ class Simulator:
 
 def kernel_launch_count():
     return int(lib().hps_kernel_launch_count())
+
+
+class Batch:
+    """Addition (no reference counterpart): several simulators, each with its
+    own beam and SpaceCharge, advanced by one graph launch.  ``simulate``
+    takes the same start/end as Simulator.simulate; the results are those of
+    running each simulator alone."""
+
+    def __init__(self, simulators):
+        self._sims = list(simulators)  # keep the simulators (and their beams) alive
+        arr = (C.c_void_p * len(self._sims))(*[s._h.value for s in self._sims])
+        self._h = C.c_void_p()
+        call("hps_batch_create", C.cast(arr, C.POINTER(C.c_void_p)), len(self._sims), C.byref(self._h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().hps_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def simulate(self, start=None, end=None):
+        """Element names resolve in the first simulator's beamline."""
+        bl = self._sims[0].beamline
+        s = -1 if start is None else (bl.index(start) if isinstance(start, str) else int(start))
+        e = -1 if end is None else (bl.index(end) if isinstance(end, str) else int(end))
+        call("hps_batch_simulate", self._h, s, e)
+
+    def last_time_ms(self):
+        v = C.c_double()
+        call("hps_batch_last_time_ms", self._h, C.byref(v))
+        return v.value

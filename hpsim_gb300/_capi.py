@@ -97,6 +97,10 @@ def lib():
         "hps_sim_last_time_ms": (st, [vp, dp]),
         "hps_sim_profile": (st, [vp, i32]),
         "hps_sim_profile_read": (st, [vp, dp, C.POINTER(C.c_uint64), i32]),
+        "hps_batch_create": (st, [pvp, u32, pvp]),
+        "hps_batch_destroy": (st, [vp]),
+        "hps_batch_simulate": (st, [vp, i32, i32]),
+        "hps_batch_last_time_ms": (st, [vp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -94,6 +94,8 @@ struct hps_scheff_s {
 struct GraphEntry {
   uint64_t key = 0;
   cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;  // the captured graph, kept for batches
+  uint64_t serial = 0;          // bumped at every capture
   // host state after the range
   double design_w, wavelen, beam_freq, beam_current, beam_design_w, fraction, interval;
   double phi_ref, w_ref;  // synchronous particle of an FP32 beam
@@ -125,6 +127,17 @@ struct hps_sim_s {
   size_t prof_used = 0;
   double prof_ms[HPS_NPROF] = {};
   uint64_t prof_cnt[HPS_NPROF] = {};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+};
+
+// Many simulators run as one graph launch: each simulator's captured range
+// is a child graph of one parent graph, with no edges between them.
+struct hps_batch_s {
+  std::vector<hps_sim_t> sims;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> serials;  // the child captures the parent was built from
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
 };
@@ -1169,6 +1182,133 @@ uint64_t mixd(uint64_t h, double v) {
   return mix(h, u);
 }
 
+// One simulate(start, end) call of a simulator: the checks and the host
+// state it starts from (SimulationEngine::Simulate, simulation_engine.cpp:
+// 73-95), and whether it runs as a captured graph.
+struct RunPlan {
+  Ctx c{};
+  int n = 0, start_index = 0, end_index = 0;
+  bool empty = false, monitor = false, graph = false, host_sync = false;
+  uint64_t key = 0;
+  double solves0 = 0.0;
+};
+
+hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  p->c = Ctx{s, s->beam, s->bl, s->sc};
+  Ctx &c = p->c;
+  const int n = (int)c.bl->types.size();
+  p->n = n;
+  if (n == 0) { p->empty = true; return HPS_OK; }
+  p->start_index = start < 0 ? 0 : start;
+  p->end_index = end < 0 ? n - 1 : end;
+  if (p->start_index >= n || p->end_index >= n) return fail(HPS_ERR_INVALID, "simulate: element index out of range");
+  if (p->start_index < s->prev_end) hps_sim_reset(s);
+  s->prev_end = p->end_index;
+  hps_beam_t b = c.b;
+  cudaStream_t st = b->stream;
+  p->monitor = s->mon_host && s->mon_cap >= (uint32_t)n;
+  if (p->monitor && s->mon_dev_cap < (uint32_t)n) {
+    if (s->mon_dev) cudaFree(s->mon_dev);
+    s->mon_dev = nullptr;
+    hps_status e = dmalloc(&s->mon_dev, (size_t)n * HPS_NMON);
+    if (e) return e;
+    s->mon_dev_cap = n;
+  }
+  if (p->monitor && c.sc) {
+    ScState h;
+    CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    p->solves0 = h.n_solves;
+  }
+  // graphs need the host-side state to be a function of the inputs; the
+  // mesh-size cut-off reads the solver's interval back after every kick
+  p->host_sync = s->sc_on && c.sc && c.sc->mesh_w != 0.0;
+  p->graph = s->use_graph && !p->host_sync && !s->prof_on;
+  s->prof_used = 0;
+  if (p->graph) {
+    uint64_t key = 0;
+    key = mix(key, (uint64_t)p->start_index);
+    key = mix(key, (uint64_t)p->end_index);
+    key = mix(key, c.bl->version);
+    key = mix(key, (uint64_t)(uintptr_t)c.bl);
+    key = mix(key, c.sc ? c.sc->version : 0);
+    key = mix(key, (uint64_t)s->sc_on);
+    key = mix(key, (uint64_t)p->monitor);
+    key = mix(key, (uint64_t)s->cur_id);
+    key = mix(key, (uint64_t)s->ccl_cell_num);
+    key = mixd(key, s->design_w);
+    key = mixd(key, s->wavelen);
+    key = mixd(key, b->freq);
+    key = mixd(key, b->current);
+    key = mixd(key, b->design_w);
+    key = mixd(key, c.sc ? c.sc->fraction : 0.0);
+    key = mixd(key, c.sc ? c.sc->interval : 0.0);
+    // FP32 beams: the synchronous particle the launch parameters derive from
+    key = mix(key, (uint64_t)b->prec);
+    key = mixd(key, b->d.phi_ref);
+    key = mixd(key, b->d.w_ref);
+    p->key = key | 1ull;
+  }
+  return HPS_OK;
+}
+
+// The simulator's graph for the plan: the cached one when the host state
+// matches (the host state then moves to the end of the range, as a replay
+// does), else a new capture (which moves it while recording).  The graph is
+// kept uninstantiated too, for batches.  Nothing is launched.
+hps_status prepare_graph(RunPlan &p) {
+  Ctx &c = p.c;
+  hps_sim_t s = c.s;
+  hps_beam_t b = c.b;
+  cudaStream_t st = b->stream;
+  GraphEntry &g = s->graph;
+  if (g.exec && g.key == p.key) {
+    s->design_w = g.design_w; s->wavelen = g.wavelen; s->ccl_cell_num = g.ccl_cell_num; s->cur_id = g.cur_id;
+    b->freq = g.beam_freq; b->current = g.beam_current; b->design_w = g.beam_design_w;
+    b->d.phi_ref = g.phi_ref; b->d.w_ref = g.w_ref;
+    if (c.sc) { c.sc->fraction = g.fraction; c.sc->interval = g.interval; }
+    note_launch((int)g.nkernels);  // a replay launches the captured kernels again
+    return HPS_OK;
+  }
+  cudaGraph_t gr;
+  uint64_t launches0 = g_launches.load();
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  hps_status e = run_range(c, p.start_index, p.end_index, p.monitor);
+  g.nkernels = g_launches.load() - launches0;
+  cudaError_t ce = cudaStreamEndCapture(st, &gr);
+  if (e) { if (ce == cudaSuccess) cudaGraphDestroy(gr); return e; }
+  if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g.exec = nullptr;
+  g.graph = gr;
+  g.serial++;
+  cudaError_t ie = cudaGraphInstantiate(&g.exec, gr, 0);
+  if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+  g.key = p.key;
+  g.design_w = s->design_w; g.wavelen = s->wavelen; g.ccl_cell_num = s->ccl_cell_num; g.cur_id = s->cur_id;
+  g.beam_freq = b->freq; g.beam_current = b->current; g.beam_design_w = b->design_w;
+  g.phi_ref = b->d.phi_ref; g.w_ref = b->d.w_ref;
+  g.fraction = c.sc ? c.sc->fraction : 0.0;
+  g.interval = c.sc ? c.sc->interval : 0.0;
+  return HPS_OK;
+}
+
+// the monitor's per-kick solve counts from the solver's cumulative counter
+void finish_monitor(const RunPlan &p) {
+  const Ctx &c = p.c;
+  if (!(p.monitor && c.sc && c.s->sc_on)) return;
+  double prev = p.solves0;
+  for (int i = 0; i <= p.end_index; ++i) {
+    if (!(i >= p.start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP)) continue;
+    double *m = c.s->mon_host + (size_t)i * HPS_NMON;
+    double cum = m[HPS_MON_SC_REMESH];
+    m[HPS_MON_SC_REMESH] = cum - prev;
+    prev = cum;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1192,6 +1332,7 @@ hps_status hps_sim_destroy(hps_sim_t s) {
   // any order): wait for the device, not for the beam's stream
   cudaDeviceSynchronize();
   if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
+  if (s->graph.graph) cudaGraphDestroy(s->graph.graph);
   if (s->mon_dev) cudaFree(s->mon_dev);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
@@ -1257,103 +1398,25 @@ hps_status hps_sim_last_time_ms(hps_sim_t s, double *ms) {
 }
 
 hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
-  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
-  Ctx c{s, s->beam, s->bl, s->sc};
-  int n = (int)c.bl->types.size();
-  if (n == 0) return HPS_OK;
-  int start_index = start < 0 ? 0 : start;
-  int end_index = end < 0 ? n - 1 : end;
-  if (start_index >= n || end_index >= n) return fail(HPS_ERR_INVALID, "simulate: element index out of range");
-  if (start_index < s->prev_end) hps_sim_reset(s);
-  s->prev_end = end_index;
-  hps_beam_t b = c.b;
-  cudaStream_t st = b->stream;
-  bool monitor = s->mon_host && s->mon_cap >= (uint32_t)n;
-  std::vector<double> solves_before;
-  if (monitor) {
-    if (s->mon_dev_cap < (uint32_t)n) {
-      if (s->mon_dev) cudaFree(s->mon_dev);
-      s->mon_dev = nullptr;
-      hps_status e = dmalloc(&s->mon_dev, (size_t)n * HPS_NMON);
-      if (e) return e;
-      s->mon_dev_cap = n;
-    }
-  }
-  double solves0 = 0.0;
-  if (monitor && c.sc) {
-    ScState h;
-    CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    solves0 = h.n_solves;
-  }
-  // graphs need the host-side state to be a function of the inputs; the
-  // mesh-size cut-off reads the solver's interval back after every kick
-  bool host_sync = s->sc_on && c.sc && c.sc->mesh_w != 0.0;
-  bool graph = s->use_graph && !host_sync && !s->prof_on;
-  s->prof_used = 0;
-  uint64_t key = 0;
-  if (graph) {
-    key = mix(key, (uint64_t)start_index);
-    key = mix(key, (uint64_t)end_index);
-    key = mix(key, c.bl->version);
-    key = mix(key, (uint64_t)(uintptr_t)c.bl);
-    key = mix(key, c.sc ? c.sc->version : 0);
-    key = mix(key, (uint64_t)s->sc_on);
-    key = mix(key, (uint64_t)monitor);
-    key = mix(key, (uint64_t)s->cur_id);
-    key = mix(key, (uint64_t)s->ccl_cell_num);
-    key = mixd(key, s->design_w);
-    key = mixd(key, s->wavelen);
-    key = mixd(key, b->freq);
-    key = mixd(key, b->current);
-    key = mixd(key, b->design_w);
-    key = mixd(key, c.sc ? c.sc->fraction : 0.0);
-    key = mixd(key, c.sc ? c.sc->interval : 0.0);
-    // FP32 beams: the synchronous particle the launch parameters derive from
-    key = mix(key, (uint64_t)b->prec);
-    key = mixd(key, b->d.phi_ref);
-    key = mixd(key, b->d.w_ref);
-    key |= 1ull;
-  }
-  CK(cudaEventRecord(s->ev0, st));
-  if (graph && s->graph.exec && s->graph.key == key) {
-    const GraphEntry &g = s->graph;
-    CK(cudaGraphLaunch(g.exec, st));
-    s->design_w = g.design_w; s->wavelen = g.wavelen; s->ccl_cell_num = g.ccl_cell_num; s->cur_id = g.cur_id;
-    b->freq = g.beam_freq; b->current = g.beam_current; b->design_w = g.beam_design_w;
-    b->d.phi_ref = g.phi_ref; b->d.w_ref = g.w_ref;
-    if (c.sc) { c.sc->fraction = g.fraction; c.sc->interval = g.interval; }
-    note_launch((int)g.nkernels);  // a replay launches the captured kernels again
-  } else if (graph) {
-    cudaGraph_t gr;
-    uint64_t launches0 = g_launches.load();
-    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    hps_status e = run_range(c, start_index, end_index, monitor);
-    s->graph.nkernels = g_launches.load() - launches0;
-    cudaError_t ce = cudaStreamEndCapture(st, &gr);
-    if (e) { if (ce == cudaSuccess) cudaGraphDestroy(gr); return e; }
-    if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-    if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
-    s->graph.exec = nullptr;
-    cudaError_t ie = cudaGraphInstantiate(&s->graph.exec, gr, 0);
-    cudaGraphDestroy(gr);
-    if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
-    GraphEntry &g = s->graph;
-    g.key = key;
-    g.design_w = s->design_w; g.wavelen = s->wavelen; g.ccl_cell_num = s->ccl_cell_num; g.cur_id = s->cur_id;
-    g.beam_freq = b->freq; g.beam_current = b->current; g.beam_design_w = b->design_w;
-    g.phi_ref = b->d.phi_ref; g.w_ref = b->d.w_ref;
-    g.fraction = c.sc ? c.sc->fraction : 0.0;
-    g.interval = c.sc ? c.sc->interval : 0.0;
-    CK(cudaGraphLaunch(g.exec, st));
+  RunPlan p;
+  hps_status e = plan_run(s, start, end, &p);
+  if (e || p.empty) return e;
+  hps_sim_t sim = s;
+  Ctx &c = p.c;
+  cudaStream_t st = c.b->stream;
+  CK(cudaEventRecord(sim->ev0, st));
+  if (p.graph) {
+    e = prepare_graph(p);
+    if (e) return e;
+    CK(cudaGraphLaunch(sim->graph.exec, st));
   } else {
-    for (int i = 0; i <= end_index; ++i) {
-      if (i >= start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP) {
-        s->cur_id = (uint32_t)i;
-        hps_status e = visit(c, (uint32_t)i);
+    for (int i = 0; i <= p.end_index; ++i) {
+      if (i >= p.start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP) {
+        sim->cur_id = (uint32_t)i;
+        e = visit(c, (uint32_t)i);
         if (e) return e;
-        if (monitor) monitor_at(c, (uint32_t)i);
-        if (host_sync) {
+        if (p.monitor) monitor_at(c, (uint32_t)i);
+        if (p.host_sync) {
           ScState h;
           CK(cudaMemcpyAsync(&h, c.sc->d, sizeof(h), cudaMemcpyDeviceToHost, st));
           CK(cudaStreamSynchronize(st));
@@ -1364,33 +1427,132 @@ hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
       }
     }
   }
-  CK(cudaEventRecord(s->ev1, st));
-  hps_status e = last_launch_status("simulate");
+  CK(cudaEventRecord(sim->ev1, st));
+  e = last_launch_status("simulate");
   if (e) return e;
-  if (monitor) {
-    CK(cudaMemcpyAsync(s->mon_host, s->mon_dev, (size_t)n * HPS_NMON * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (p.monitor) {
+    CK(cudaMemcpyAsync(sim->mon_host, sim->mon_dev, (size_t)p.n * HPS_NMON * sizeof(double), cudaMemcpyDeviceToHost,
+                       st));
   }
   CK(cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-  s->last_ms = ms;
-  for (size_t k = 0; k < s->prof_used; ++k) {
+  cudaEventElapsedTime(&ms, sim->ev0, sim->ev1);
+  sim->last_ms = ms;
+  for (size_t k = 0; k < sim->prof_used; ++k) {
     float pm = 0.f;
-    cudaEventElapsedTime(&pm, s->prof_pool[2 * k], s->prof_pool[2 * k + 1]);
-    s->prof_ms[s->prof_cls[k]] += pm;
-    s->prof_cnt[s->prof_cls[k]] += 1;
+    cudaEventElapsedTime(&pm, sim->prof_pool[2 * k], sim->prof_pool[2 * k + 1]);
+    sim->prof_ms[sim->prof_cls[k]] += pm;
+    sim->prof_cnt[sim->prof_cls[k]] += 1;
   }
-  s->prof_used = 0;
-  if (monitor && c.sc && s->sc_on) {
-    double prev = solves0;
-    for (int i = 0; i <= end_index; ++i) {
-      if (!(i >= start_index || c.bl->types[i] == HPS_ELEM_SPCHCOMP)) continue;
-      double *m = s->mon_host + (size_t)i * HPS_NMON;
-      double cum = m[HPS_MON_SC_REMESH];
-      m[HPS_MON_SC_REMESH] = cum - prev;
-      prev = cum;
+  sim->prof_used = 0;
+  finish_monitor(p);
+  return HPS_OK;
+}
+
+
+// ---- batches of independent simulators ----------------------------------------
+hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *out) {
+  if (!sims || !count || !out) return fail(HPS_ERR_INVALID, "batch_create: bad argument");
+  std::vector<hps_sim_t> v(sims, sims + count);
+  for (uint32_t i = 0; i < count; ++i) {
+    if (!v[i]) return fail(HPS_ERR_INVALID, "batch_create: null simulator");
+    for (uint32_t j = 0; j < i; ++j) {
+      if (v[j] == v[i] || v[j]->beam == v[i]->beam)
+        return fail(HPS_ERR_INVALID, "batch_create: every simulator of a batch needs its own beam");
+      if (v[i]->sc && v[j]->sc == v[i]->sc)
+        return fail(HPS_ERR_INVALID, "batch_create: every simulator of a batch needs its own SpaceCharge");
     }
   }
+  hps_batch_t bt = new hps_batch_s();
+  bt->sims = v;
+  if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&bt->ev0) != cudaSuccess || cudaEventCreate(&bt->ev1) != cudaSuccess) {
+    hps_batch_destroy(bt);
+    return fail(HPS_ERR_CUDA, "batch_create: stream or events");
+  }
+  *out = bt;
+  return HPS_OK;
+}
+
+hps_status hps_batch_destroy(hps_batch_t bt) {
+  if (!bt) return HPS_OK;
+  if (bt->stream) cudaStreamSynchronize(bt->stream);
+  if (bt->exec) cudaGraphExecDestroy(bt->exec);
+  if (bt->ev0) cudaEventDestroy(bt->ev0);
+  if (bt->ev1) cudaEventDestroy(bt->ev1);
+  if (bt->stream) cudaStreamDestroy(bt->stream);
+  delete bt;
+  return HPS_OK;
+}
+
+// Simulator::Simulate(start, end) on every simulator of the batch in one
+// graph launch.  Each simulator must be able to run as a graph (graphs on,
+// profiling off, no mesh-size cut-off energy).
+hps_status hps_batch_simulate(hps_batch_t bt, int32_t start, int32_t end) {
+  if (!bt) return fail(HPS_ERR_INVALID, "bad batch handle");
+  const size_t m = bt->sims.size();
+  std::vector<RunPlan> plans(m);
+  for (size_t k = 0; k < m; ++k) {
+    CK(cudaStreamSynchronize(bt->sims[k]->beam->stream));  // the beam's own work first
+    hps_status e = plan_run(bt->sims[k], start, end, &plans[k]);
+    if (e) return e;
+    if (!plans[k].empty && !plans[k].graph)
+      return fail(HPS_ERR_STATE, "batch_simulate: a simulator cannot run as a graph (graphs off, profiling on, "
+                                 "or a mesh-size cut-off energy)");
+  }
+  std::vector<uint64_t> serials(m, 0);
+  for (size_t k = 0; k < m; ++k) {
+    if (plans[k].empty) continue;
+    hps_status e = prepare_graph(plans[k]);
+    if (e) return e;
+    serials[k] = bt->sims[k]->graph.serial;
+  }
+  if (!bt->exec || serials != bt->serials) {
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    bt->exec = nullptr;
+    cudaGraph_t parent;
+    CK(cudaGraphCreate(&parent, 0));
+    for (size_t k = 0; k < m; ++k) {
+      if (plans[k].empty) continue;
+      cudaGraphNode_t node;
+      cudaError_t ce = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, bt->sims[k]->graph.graph);
+      if (ce != cudaSuccess) {
+        cudaGraphDestroy(parent);
+        return fail(HPS_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ce));
+      }
+    }
+    cudaError_t ie = cudaGraphInstantiate(&bt->exec, parent, 0);
+    cudaGraphDestroy(parent);
+    if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(ie));
+    bt->serials = serials;
+  }
+  CK(cudaEventRecord(bt->ev0, bt->stream));
+  CK(cudaGraphLaunch(bt->exec, bt->stream));
+  CK(cudaEventRecord(bt->ev1, bt->stream));
+  for (size_t k = 0; k < m; ++k) {
+    const RunPlan &p = plans[k];
+    if (p.empty || !p.monitor) continue;
+    hps_sim_t s = bt->sims[k];
+    CK(cudaMemcpyAsync(s->mon_host, s->mon_dev, (size_t)p.n * HPS_NMON * sizeof(double), cudaMemcpyDeviceToHost,
+                       bt->stream));
+  }
+  hps_status e = last_launch_status("batch_simulate");
+  if (e) return e;
+  CK(cudaStreamSynchronize(bt->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, bt->ev0, bt->ev1);
+  bt->last_ms = ms;
+  for (size_t k = 0; k < m; ++k) {
+    if (plans[k].empty) continue;
+    bt->sims[k]->last_ms = ms;
+    finish_monitor(plans[k]);
+  }
+  return HPS_OK;
+}
+
+hps_status hps_batch_last_time_ms(hps_batch_t bt, double *ms) {
+  if (!bt || !ms) return fail(HPS_ERR_INVALID, "bad argument");
+  *ms = bt->last_ms;
   return HPS_OK;
 }
 

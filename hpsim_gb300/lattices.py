@@ -170,6 +170,45 @@ def small_fodo(aperture=0.0):
     return elems
 
 
+@dataclass
+class ScanBeam:
+    """One beam of a batched scan: its particle count, seed and set-point
+    perturbations of the small-FODO lattice."""
+    num: int
+    seed: int
+    rf_scale: float      # buncher voltage scale
+    phase_offset: float  # buncher phase offset, rad
+    quad_scale: float    # scale of every quad gradient
+
+
+def batched_scan(n_beams=256, seed=2024, n_min=16384, n_max=524288):
+    """Independent beams on the small-FODO topology: particle counts
+    log-uniform in [n_min, n_max], RF amplitude scale U(0.95, 1.05), phase
+    offset U(-3, +3) deg and quad-gradient scale U(0.97, 1.03), from a seed."""
+    rng = np.random.default_rng(seed)
+    nums = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_beams)).astype(np.int64)
+    out = []
+    for k in range(n_beams):
+        out.append(ScanBeam(int(nums[k]), int(seed * 1000 + k), float(rng.uniform(0.95, 1.05)),
+                            float(math.radians(rng.uniform(-3.0, 3.0))), float(rng.uniform(0.97, 1.03))))
+    return out
+
+
+def scan_lattice(sb: ScanBeam, aperture=0.0):
+    """small_fodo with one scan beam's set points."""
+    elems = small_fodo(aperture)
+    out = []
+    for code, name, p in elems:
+        p = p.copy()
+        if code == BUNCHER:
+            p[param_index(BUNCHER, "voltage")] *= sb.rf_scale
+            p[param_index(BUNCHER, "phase")] += sb.phase_offset
+        elif code == QUAD:
+            p[param_index(QUAD, "gradient")] *= sb.quad_scale
+        out.append((code, name, p))
+    return out
+
+
 def _ttf_fit(rng, beta_g, t_nom=0.85, s_nom=0.10, spread=0.05):
     """Cubic T(beta), S(beta) in powers of beta.
 

@@ -59,6 +59,7 @@ typedef struct hps_beam_s *hps_beam_t;
 typedef struct hps_beamline_s *hps_beamline_t;
 typedef struct hps_scheff_s *hps_scheff_t;
 typedef struct hps_sim_s *hps_sim_t;
+typedef struct hps_batch_s *hps_batch_t;
 
 /* ---- library ------------------------------------------------------------ */
 int hps_abi_version(void);
@@ -266,6 +267,18 @@ hps_status hps_sim_last_time_ms(hps_sim_t sim, double *ms);
 hps_status hps_sim_profile(hps_sim_t sim, int on);
 hps_status hps_sim_profile_read(hps_sim_t sim, double *ms /* HPS_NPROF */, uint64_t *count /* HPS_NPROF */,
                                 int reset);
+
+/* ---- batches (no reference counterpart): many independent simulators --
+ * (each with its own beam and SpaceCharge; lattices may differ) run their
+ * Simulate(start, end) in one graph launch: each simulator's captured range
+ * is a child graph of one parent graph with no edges between them, so the
+ * beams advance concurrently.  Results are those of running each simulator
+ * alone.  Simulators must be able to run as graphs (graphs on, profiling
+ * off, no mesh-size cut-off energy). */
+hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *out);
+hps_status hps_batch_destroy(hps_batch_t batch);
+hps_status hps_batch_simulate(hps_batch_t batch, int32_t start, int32_t end);
+hps_status hps_batch_last_time_ms(hps_batch_t batch, double *ms);
 
 #ifdef __cplusplus
 }

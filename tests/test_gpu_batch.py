@@ -1,0 +1,79 @@
+"""Batches (hps_batch_*, HPSim.Batch): beams of uneven sizes and perturbed
+set points advanced in one graph launch give, beam by beam, the results of
+simulating each alone (bit-identical: every kernel is deterministic), and
+one of them matches the FP64 oracle."""
+import numpy as np
+import pytest
+
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+COORDS = ("x", "xp", "y", "yp", "phi", "w")
+
+
+def make(sb, precision, monitor=False):
+    from hpsim_gb300 import HPSim, lattices as L
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=sb.num, precision=precision)
+    beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, sb.seed)
+    beam.set_ref_w(0.75)
+    beam.set_ref_phi(0.0)
+    bl = HPSim.BeamLine(elements=L.scan_lattice(sb, aperture=0.006))
+    sc = HPSim.SpaceCharge(32, 128, 0.1, 0)
+    sc.set_remesh_threshold(0.0)
+    sim = HPSim.Simulator(beam, bl, sc)
+    if monitor:
+        sim.enable_monitor(True)
+    return beam, bl, sc, sim
+
+
+def state(beam):
+    out = {k: beam._coord(k) for k in COORDS}
+    out["loss"], out["lloss"] = beam._loss(0), beam._loss(1)
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batch_equals_each_beam_alone(precision):
+    from hpsim_gb300 import HPSim, lattices as L
+    scan = L.batched_scan(12, seed=5, n_min=2048, n_max=65536)
+    objs = [make(sb, precision, monitor=True) for sb in scan]
+    batch = HPSim.Batch([o[3] for o in objs])
+    batch.simulate()
+    assert batch.last_time_ms() > 0
+    for sb, (beam, _, _, sim) in zip(scan, objs):
+        ref = make(sb, precision, monitor=True)
+        ref[3].simulate()
+        a, b = state(beam), state(ref[0])
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (sb, k)
+        assert np.array_equal(np.nan_to_num(sim.monitor), np.nan_to_num(ref[3].monitor))
+    # a rewound range resets the simulators and captures them again
+    batch.simulate(0, 10)
+    for sb, (beam, *_) in zip(scan, objs):
+        ref = make(sb, precision)
+        ref[3].simulate()
+        ref[3].simulate(0, 10)
+        assert np.array_equal(beam._coord("x"), ref[0]._coord("x")), sb
+
+
+def test_batch_beam_matches_oracle(oracle):
+    from hpsim_gb300 import HPSim, lattices as L
+    scan = L.batched_scan(4, seed=11, n_min=4096, n_max=8192)
+    objs = [make(sb, "fp64", monitor=True) for sb in scan]
+    HPSim.Batch([o[3] for o in objs]).simulate()
+    sb = scan[2]
+    mo, co = oracle.run(L.scan_lattice(sb, aperture=0.006), sb.num, spch_args=(32, 128, 0.1, 0),
+                        spch_set={"remesh_threshold": 0.0}, seed=sb.seed)
+    c = state(objs[2][0])
+    assert np.array_equal(c["loss"], co["loss"])
+    ok = G.monitor_close(objs[2][3].monitor, mo, 1e-6)
+    assert ok.all(), np.argwhere(~ok)[:5]
+
+
+def test_batch_rejects_shared_beams():
+    from hpsim_gb300 import HPSim, lattices as L
+    sb = L.batched_scan(1, seed=3, n_min=1024, n_max=1024)[0]
+    beam, bl, sc, sim = make(sb, "fp32")
+    sim2 = HPSim.Simulator(beam, bl, HPSim.SpaceCharge(32, 128, 0.1, 0))
+    with pytest.raises(Exception):
+        HPSim.Batch([sim, sim2])
