@@ -40,13 +40,15 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    p.add_argument("--particles", type=int, default=N_PART)
+    p.add_argument("--precision", default=None, choices=["fp32", "fp64"])
+    p.add_argument("--particles", type=int, default=None)
     p.add_argument("--gaps", type=int, default=GAPS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="dtl_like", choices=["dtl_like", "batched"],
-                   help="dtl_like: one 1M-particle beam (the headline); batched: 256 beams of the "
+    p.add_argument("--workload", default="dtl_like", choices=["dtl_like", "small_fodo", "ccl_large", "batched"],
+                   help="dtl_like: one 1M-particle beam through 165 DTL gaps (the headline); small_fodo: "
+                        "65,536 particles in FP64 through buncher + 40 FODO elements; ccl_large: 16,777,216 "
+                        "particles through 1024 CCL gaps, SCHEFF 64x256; batched: 256 beams of the "
                         "small-FODO topology in one graph launch")
     p.add_argument("--beams", type=int, default=256)
     return p.parse_args()
@@ -128,21 +130,57 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+# beam and solver of each single-beam workload: particles, precision, W0 [MeV],
+# f [MHz], SCHEFF mesh (nr, nz) and kick interval [m]
+WORKLOADS = {
+    "dtl_like": dict(particles=N_PART, precision="fp32", w0=0.75, freq=201.25, mesh=(32, 128), interval=0.01),
+    "small_fodo": dict(particles=65536, precision="fp64", w0=0.75, freq=201.25, mesh=(32, 128), interval=0.10),
+    "ccl_large": dict(particles=16777216, precision="fp32", w0=100.0, freq=805.0, mesh=(64, 256), interval=0.01),
+}
+
+
+def resolve(args):
+    """Fill the workload's defaults into --particles and --precision."""
+    spec = WORKLOADS.get(args.workload, WORKLOADS["dtl_like"])
+    if args.particles is None:
+        args.particles = spec["particles"] if args.workload in WORKLOADS else N_PART
+    if args.precision is None:
+        args.precision = spec["precision"] if args.workload in WORKLOADS else "fp32"
+    return spec
+
+
 def workload(args):
     from hpsim_gb300 import lattices as L
-    elems = L.dtl_like(n_gaps=args.gaps)
-    return elems
+    if args.workload == "small_fodo":
+        return L.small_fodo()
+    if args.workload == "ccl_large":
+        return L.ccl_like()
+    return L.dtl_like(n_gaps=args.gaps)
+
+
+def describe(args, n_elem):
+    spec = WORKLOADS[args.workload]
+    nr, nz = spec["mesh"]
+    if args.workload == "small_fodo":
+        lat = f"small_fodo: buncher + 20 x (0.10 m drift, 0.05 m quad, +-18 T/m)"
+    elif args.workload == "ccl_large":
+        lat = f"ccl_large: 4 x 32 x 8 CCL gaps at 805 MHz from 100 MeV, doublets between tanks ({n_elem} elements)"
+    else:
+        lat = f"dtl_like: {args.gaps} DTL gaps + {args.gaps + 1} quads"
+    return (f"{lat}, {args.particles} H- particles, waterbag {spec['w0']} MeV, SCHEFF {nr}x{nz} full solve at "
+            f"every element")
 
 
 def make_sim(args, elems, seed):
     from hpsim_gb300 import HPSim, lattices as L
+    spec = WORKLOADS[args.workload]
     beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=args.particles, precision=args.precision)
-    beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, seed)
-    beam.set_ref_w(0.75)
+    beam.set_waterbag(*L.waterbag_twiss(w0=spec["w0"], freq=spec["freq"]), 0.0, spec["w0"], spec["freq"], seed)
+    beam.set_ref_w(spec["w0"])
     beam.set_ref_phi(0.0)
     beam.save_initial_beam()
     bl = HPSim.BeamLine(elements=elems)
-    sc = HPSim.SpaceCharge(32, 128, 0.01, 0)
+    sc = HPSim.SpaceCharge(*spec["mesh"], spec["interval"], 0)
     sc.set_remesh_threshold(0.0)
     sim = HPSim.Simulator(beam, bl, sc)
     return beam, bl, sc, sim
@@ -218,11 +256,12 @@ def cpu_baseline(args, elems, budget_s=12.0, impl_kind="port"):
     threads = os.cpu_count() or 1
     O.lib().orc_set_threads(threads)
     types, params, _ = L.lattice_arrays(elems)
+    spec = WORKLOADS[args.workload]
     b = O.Beam(args.particles)
-    b.set_waterbag(L.waterbag_twiss(), 0.0, 0.75, 201.25, 12345)
-    b.set_ref_w(0.75)
+    b.set_waterbag(L.waterbag_twiss(w0=spec["w0"], freq=spec["freq"]), 0.0, spec["w0"], spec["freq"], 12345)
+    b.set_ref_w(spec["w0"])
     b.set_ref_phi(0.0)
-    sp = O.Scheff(32, 128, 0.01, 0)
+    sp = O.Scheff(*spec["mesh"], spec["interval"], 0)
     sp.set(remesh_threshold=0.0)
     sim = O.Sim(b, types, params, sp)
     done = 0
@@ -256,8 +295,7 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"dtl_like {args.gaps} gaps, {args.particles} particles, SCHEFF 32x128 every "
-                                   f"element (time extrapolated from bounded prefixes)",
+            "config": {"workload": describe(args, len(elems)) + " (time extrapolated from bounded prefixes)",
                        "particles": args.particles, "elements": len(elems)},
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": r["cores"], "kind": "port",
                              "sample": r["sample"]},
@@ -333,6 +371,7 @@ def run_batched(args):
 
 def main():
     args = parse()
+    resolve(args)
     if args.impl == "reference":
         run_reference(args)
         return
@@ -448,8 +487,7 @@ def main():
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * t_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
-        "config": {"workload": f"dtl_like: {args.gaps} DTL gaps + {args.gaps + 1} quads, {args.particles} H- "
-                               f"particles, waterbag 0.75 MeV, SCHEFF 32x128 full solve at every element",
+        "config": {"workload": describe(args, n_elem),
                    "particles": args.particles, "elements": n_elem, "precision": args.precision,
                    "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write)",
                    "wall_s": wall, "sc_kicks_per_step": n_elem,
