@@ -1,0 +1,236 @@
+// contract.cuh -- the SCHEFF ring-to-mesh field sum (UpdateFldTbl2KernelDouble,
+// src/simulation/inc/space_charge_kernel.cu:472-568) for FP32 tables (FP32
+// beams) and FP64 tables (FP64 beams), one kernel template:
+//   E[zp][rp] = sum over bins (zs, rs) of q(zs, rs) g(zp - zs),
+// g(k) = G[rp][k - 1][rs] for sources below the point (k >= 1) and
+// G[rp][-k][rs] with E_z negated for sources at or above it (k <= 0).
+// For each source radius this is a convolution along z.  A block stages its
+// rp's g(k), k = -(nz - 1) .. nz, sign included, and the charges (2^-36
+// fixed point converted to T) in shared memory, a tile of source radii at a
+// time.  A warp computes kCP consecutive field points over half the source
+// rows (two warps per point group, summed in a fixed order): the lanes run
+// over source radii, and as the warp walks the rows the kCP values of g it
+// needs slide by one, kept in a ring of kCP + 1 registers that takes one new
+// shared-memory load per row (one charge and one table load per 2 kCP FMAs).
+// Each point's sum ends with a fixed shuffle tree.  The set of bins each
+// point sums is the reference's (its integer partition of the table): bins
+// zs * nr + rs at or above a limit are left out, which only happens when the
+// mesh has fewer than 1024 bins or a row count that does not divide them.
+#pragma once
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace hps {
+namespace {
+
+constexpr int kCP = 4;                     // field points per warp
+constexpr int kCH = 2;                     // warps sharing the source rows of a point group
+constexpr int kCG = 4;                     // point groups per block
+constexpr int kCZ = kCP * kCG;             // field points per block
+constexpr int kContractThreads = kCG * kCH * 32;
+constexpr int kContractSmem = 96 * 1024;   // largest table + charge tile
+
+// the FP32 and FP64 tables: pair type, table layout, charge conversion
+template <class T> struct CTab;
+template <> struct CTab<float> {
+  using V = float2;
+  // FP32 Green's table [rp][dz][rs] (ScTables::ffld1)
+  static __device__ const V *slice(const ScTables &t, uint32_t rp, uint32_t fld) {
+    return (const V *)t.ffld1 + (size_t)rp * fld;
+  }
+  static __device__ size_t at(uint32_t z, uint32_t rs, uint32_t nx, uint32_t) { return (size_t)z * nx + rs; }
+  static constexpr bool kZFast = false;  // consecutive table entries run over rs
+  // 2^-36 fixed-point charge through two 32-bit conversions (a 64-bit
+  // integer conversion runs on the FP64 pipe)
+  static __device__ float charge(unsigned long long v) {
+    const long long s = (long long)v;
+    const int hi = (int)(s >> 32);
+    const unsigned lo = (unsigned)(v & 0xffffffffull);
+    return fmaf((float)hi, 4294967296.0f, (float)lo) * 1.4551915228366852e-11f;  // 2^-36
+  }
+  static __device__ float *out(const ScTables &t) { return t.ffld2; }
+};
+template <> struct CTab<double> {
+  using V = double2;
+  // FP64 Green's table [rp][rs][dz] (ScTables::fld1)
+  static __device__ const V *slice(const ScTables &t, uint32_t rp, uint32_t fld) {
+    return (const V *)t.fld1 + (size_t)rp * fld;
+  }
+  static __device__ size_t at(uint32_t z, uint32_t rs, uint32_t, uint32_t nz) { return (size_t)rs * nz + z; }
+  static constexpr bool kZFast = true;   // consecutive table entries run over dz
+  static __device__ double charge(unsigned long long v) { return (double)(long long)v * kBinInvScale; }
+  static __device__ double *out(const ScTables &t) { return t.fld2; }
+};
+
+// source radii per staged tile: g(k) (2 nz pairs) and charges (nz values)
+// (5 values of T per row and radius)
+template <class T>
+__host__ __device__ inline uint32_t contract_tile(uint32_t nx, uint32_t nz) {
+  const uint32_t t = (uint32_t)(kContractSmem / (5 * sizeof(T) * nz));
+  return t < nx ? t : nx;
+}
+// (bounds the tile of every mesh up to nx_max x nz_max)
+template <class T>
+inline size_t contract_smem(uint32_t nx_max, uint32_t nz_max) {
+  return std::min<size_t>(kContractSmem, (size_t)5 * sizeof(T) * nx_max * nz_max);
+}
+
+// the bin limit of field row zp (the reference's partition of the table)
+__device__ inline uint32_t contract_lim(uint32_t zp, uint32_t rp, uint32_t nx, uint32_t nz) {
+  const uint32_t fld_sz = nx * nz;
+  if (zp < nz) {
+    const uint32_t gnum = 1024 / nz;
+    return gnum ? gnum * (fld_sz / gnum) : 0;
+  }
+  if (rp < nx) {
+    const uint32_t gnum = 1024 / nx;
+    return gnum ? gnum * (fld_sz / gnum) : 0;
+  }
+  return (fld_sz / 1024) * 1024;
+}
+
+template <class T, class V>
+__device__ inline V cpair(T x, T y) { return V{x, y}; }
+
+// One block's work; TR > 0 is the tile width known at compile time (nr ==
+// TR, one tile: every shared-memory offset of the row walk is an immediate),
+// TR == 0 the general tiled form.
+template <class T, int TR>
+__device__ __forceinline__ void contract_block(const ScState *sc, const ScTables &t, T *sm,
+                                               typename CTab<T>::V (*upper)[kCP]) {
+  using V = typename CTab<T>::V;
+  const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
+  const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ;
+  const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile<T>(nx, nz);
+  V *gz = (V *)sm;                 // [k + nz - 1][tr], k = -(nz - 1) .. nz
+  T *qs = sm + 4 * nz * tr;        // [zs][tr]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = warp / kCH, half = warp % kCH;
+  const uint32_t zp0 = zb0 + grp * kCP;  // points zp0 .. zp0 + kCP - 1
+  const uint32_t za = half * nz / kCH, zb = (half + 1) * nz / kCH;  // this warp's source rows
+  uint32_t lim[kCP];
+  bool cut = false;
+#pragma unroll
+  for (int j = 0; j < kCP; ++j) {
+    lim[j] = contract_lim(zp0 + j, rp, nx, nz);
+    cut |= zp0 + j <= nz && lim[j] < fld_sz;
+  }
+  const V *G = CTab<T>::slice(t, rp, fld_sz);
+  T ax[kCP], az[kCP];
+#pragma unroll
+  for (int j = 0; j < kCP; ++j) ax[j] = az[j] = T(0);
+  for (uint32_t rs0 = 0; rs0 < nx; rs0 += tr) {
+    const uint32_t ntr = TR > 0 ? (uint32_t)TR : min(tr, nx - rs0), ntile = nz * ntr;
+    __syncthreads();
+    // every load of a thread's share is issued before its first store: one
+    // memory round trip per kStage elements, not per element; thread order
+    // follows the table's fast index
+    constexpr int kStage = 8;
+    for (uint32_t e0 = threadIdx.x; e0 < ntile; e0 += kStage * blockDim.x) {
+      V gv[kStage];
+      unsigned long long bv[kStage];
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const uint32_t e = e0 + u * blockDim.x;
+        if (e < ntile) {
+          const uint32_t z = CTab<T>::kZFast ? e % nz : e / ntr, r = CTab<T>::kZFast ? e / nz : e % ntr;
+          gv[u] = __ldg(G + CTab<T>::at(z, rs0 + r, nx, nz));
+          bv[u] = __ldg(t.bin_fx + z * nx + rs0 + r);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kStage; ++u) {
+        const uint32_t e = e0 + u * blockDim.x;
+        if (e < ntile) {
+          const uint32_t z = CTab<T>::kZFast ? e % nz : e / ntr, r = CTab<T>::kZFast ? e / nz : e % ntr;
+          gz[(nz + z) * tr + r] = gv[u];                                // k = z + 1
+          gz[(nz - 1 - z) * tr + r] = cpair<T, V>(gv[u].x, -gv[u].y);   // k = -z
+          qs[z * tr + r] = CTab<T>::charge(bv[u]);
+        }
+      }
+    }
+    __syncthreads();
+    if (zp0 > nz) continue;
+    for (uint32_t r = lane; r < ntr; r += 32) {
+      if (!cut) {
+        // ring slot (j - u) mod R holds g(zp0 + j - zs), u = zs - zs0; the
+        // slot (-u - 1) mod R is free at row zs and takes g(zp0 - zs - 1).
+        // gp walks g(zp0 - zs - 1) down the rows, qp the charges up.
+        constexpr int R = kCP + 1;
+        V ring[R];
+        const V *g = gz + (nz - 1) * tr + r;  // g(k) at g[k * tr]
+#pragma unroll
+        for (int j = 0; j < kCP; ++j) ring[j] = g[min((int)(zp0 + j) - (int)za, (int)nz) * (int)tr];
+        const V *gp = g + ((int)zp0 - (int)za - 1) * (int)tr;
+        const T *qp = qs + za * tr + r;
+        for (uint32_t zs0 = za; zs0 < zb; zs0 += R, gp -= R * tr, qp += R * tr) {
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            if (zs0 + u >= zb) break;
+            if (zs0 + u + 1 < zb) ring[(R - 1 - u) % R] = gp[-(int)(u * tr)];
+            const T qv = qp[u * tr];
+#pragma unroll
+            for (int j = 0; j < kCP; ++j) {
+              const V gv = ring[(j - u + R) % R];
+              ax[j] = fma(qv, gv.x, ax[j]);
+              az[j] = fma(qv, gv.y, az[j]);
+            }
+          }
+        }
+      } else {
+        // small meshes: each point sums the source rows below its own limit
+        const T *q = qs + r;
+        const V *g = gz + (nz - 1) * tr + r;
+        const uint32_t rs = rs0 + r;
+        for (int j = 0; j < kCP; ++j) {
+          if (zp0 + j > nz) continue;
+          const uint32_t zend = lim[j] > rs ? min(zb, (lim[j] - rs + nx - 1) / nx) : 0u;
+          for (uint32_t zs = za; zs < zend; ++zs) {
+            const T qv = q[zs * tr];
+            const V gv = g[((int)(zp0 + j) - (int)zs) * (int)tr];
+            ax[j] = fma(qv, gv.x, ax[j]);
+            az[j] = fma(qv, gv.y, az[j]);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kCP; ++j) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      ax[j] += __shfl_down_sync(0xffffffffu, ax[j], off);
+      az[j] += __shfl_down_sync(0xffffffffu, az[j], off);
+    }
+  }
+  if (half == 1 && lane == 0)
+    for (int j = 0; j < kCP; ++j) upper[grp][j] = cpair<T, V>(ax[j], az[j]);
+  __syncthreads();
+  if (half != 0 || lane != 0 || zp0 > nz) return;
+  T *out = CTab<T>::out(t);
+  for (int j = 0; j < kCP; ++j) {
+    if (zp0 + j > nz) break;
+    const size_t pt = (size_t)(zp0 + j) * nrow + rp;
+    out[2 * pt] = ax[j] + upper[grp][j].x;
+    out[2 * pt + 1] = az[j] + upper[grp][j].y;
+  }
+}
+
+// grid (nr_max + 1, ceil((nz_max + 1) / kCZ)), kContractThreads threads,
+// contract_smem<T>(nr_max, nz_max) bytes
+template <class T>
+__global__ void __launch_bounds__(kContractThreads) k_contract_t(const ScState *sc, ScTables t) {
+  if (!sc->remesh) return;
+  const uint32_t nx = sc->nx, nz = sc->nz;
+  if (blockIdx.x > nx || blockIdx.y * kCZ > nz) return;
+  extern __shared__ __align__(16) unsigned char contract_raw[];
+  __shared__ typename CTab<T>::V upper[kCG][kCP];  // second halves' sums
+  T *sm = (T *)contract_raw;
+  if (nx == 32 && contract_tile<T>(nx, nz) == 32) contract_block<T, 32>(sc, t, sm, upper);
+  else contract_block<T, 0>(sc, t, sm, upper);
+}
+
+}  // namespace
+}  // namespace hps

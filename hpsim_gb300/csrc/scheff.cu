@@ -15,6 +15,7 @@
 
 #include "../../include/hpsim_gb300.h"
 #include "internal.h"
+#include "contract.cuh"
 #include "reduce.cuh"
 #include "scheff_common.cuh"
 
@@ -296,57 +297,6 @@ __global__ void k_deposit(DevBeam bm, ScState *sc, ScTables t) {
   }
 }
 
-__device__ inline double bin_value(const ScTables &t, uint32_t k) {
-  return (double)(long long)t.bin_fx[k] * kBinInvScale;
-}
-
-// UpdateFldTbl2KernelDouble, space_charge_kernel.cu:472-568 launched as
-// <<<nr + 2, 1024>>>: one warp per field point; the set of bins each point
-// sums is the reference's (its integer partition of the table can leave
-// bins out on small meshes, and leaves the (nz, nr) corner at zero below
-// 1024 bins).
-__global__ void k_contract(const ScState *sc, ScTables t) {
-  if (!sc->remesh) return;
-  const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
-  const uint32_t npts = (nz + 1) * nrow;
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t pt = warp; pt < npts; pt += nwarps) {
-    uint32_t zp = pt / nrow, rp = pt % nrow;
-    uint32_t lim;
-    if (zp < nz) {
-      uint32_t gnum = 1024 / nz;
-      lim = gnum ? gnum * (fld_sz / gnum) : 0;
-    } else if (rp < nx) {
-      uint32_t gnum = 1024 / nx;
-      lim = gnum ? gnum * (fld_sz / gnum) : 0;
-    } else {
-      lim = (fld_sz / 1024) * 1024;
-    }
-    double ax = 0.0, az = 0.0;
-    for (uint32_t bi = lane; bi < lim; bi += 32) {
-      double bv = bin_value(t, bi);
-      if (bv == 0.0) continue;
-      uint32_t rs = bi % nx, zs = bi / nx;
-      double sign = 1.0;
-      uint32_t dz;
-      if (zp < nz && zs >= zp) { dz = zs - zp; sign = -1.0; }
-      else dz = zp - zs - 1;
-      size_t f1 = dz + (size_t)rs * nz + (size_t)rp * fld_sz;
-      ax += bv * t.fld1[2 * f1];
-      az += sign * bv * t.fld1[2 * f1 + 1];
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      ax += __shfl_down_sync(0xffffffffu, ax, off);
-      az += __shfl_down_sync(0xffffffffu, az, off);
-    }
-    if (lane == 0) {
-      t.fld2[2 * pt] += ax;
-      t.fld2[2 * pt + 1] += az;
-    }
-  }
-}
 
 // ApplySpchKickKernel, space_charge_kernel.cu:573-706.  The reference's
 // grid-stride loop `while (indx > 0 && ...)` ends thread 0 before its first
@@ -473,6 +423,18 @@ void sc_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs
   }
 }
 
+// UpdateFldTbl2KernelDouble (space_charge_kernel.cu:472-568) on the FP64
+// tables: contract.cuh's ring-convolution kernel, grid and shared memory
+// sized for the largest mesh the solver takes
+void contract64(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max, cudaStream_t st) {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_contract_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  });
+  dim3 cg(nx_max + 1, (nz_max + 1 + kCZ - 1) / kCZ);
+  k_contract_t<double><<<cg, kContractThreads, contract_smem<double>(nx_max, nz_max), st>>>(sc, t);
+}
+
 void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
              cudaStream_t st) {
   launch_pass(OpAdjMesh{b, sc}, b.n, s, st);
@@ -484,7 +446,7 @@ void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs 
     k_deposit<<<grid_for(b.n), kBlock, a.deposit_smem, st>>>(b, sc, t);
     note_launch();
   }
-  k_contract<<<2 * 152, kBlock, 0, st>>>(sc, t);
+  contract64(sc, t, a.nx_max, a.nz_max, st);
   note_launch();
 }
 
@@ -547,7 +509,7 @@ void sc_field_solve(ScState *sc, unsigned long long *fx, double *fld1, double *f
   t.fld1 = fld1;
   t.fld2 = fld2;
   k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, (uint32_t)mesh[4], mesh[5]);
-  k_contract<<<2 * 152, kBlock, 0, st>>>(sc, t);
+  contract64(sc, t, nr, nz, st);
   note_launch(4);
 }
 

@@ -43,6 +43,7 @@
 #include "internal.h"
 #include "reduce.cuh"
 #include "sc32_kick.cuh"
+#include "contract.cuh"
 #include "sc32_stats.cuh"
 #include "scheff_common.cuh"
 
@@ -451,194 +452,6 @@ __global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
   else green_blocks(sc, t, blockIdx.x - ndep, ngreen);
 }
 
-// ---- contraction -------------------------------------------------------------
-// Ring-to-mesh field sum (UpdateFldTbl2KernelDouble, space_charge_kernel.cu:
-// 472-568) in FP32:  E[zp][rp] = sum over bins (zs, rs) of q(zs, rs) *
-// g(zp - zs), g(k) = G[rp][k - 1][rs] for sources below the point (k >= 1)
-// and G[rp][-k][rs] with E_z negated for sources at or above it (k <= 0).
-// For each source radius this is a convolution along z.  A block stages its
-// rp's g(k), k = -(nz - 1) .. nz, sign included, and the charges, converted
-// to FP32, in shared memory, a tile of source radii at a time.  A warp
-// computes kCP consecutive field points over half the source rows (two warps
-// per point group, summed in a fixed order): the lanes run over source radii,
-// and as the warp walks the rows the kCP values of g it needs slide by one,
-// kept in a ring of kCP + 1 registers that takes one new shared-memory load
-// per row (one charge and one table load per 2 kCP FMAs).  Each point's sum
-// ends with a fixed shuffle tree.  The set of bins each point sums is the
-// reference's (its integer partition of the table; see scheff.cu): bins
-// zs * nr + rs at or above a limit are left out, which only happens when the
-// mesh has fewer than 1024 bins or a row count that does not divide them.
-constexpr int kCP = 4;                     // field points per warp
-constexpr int kCH = 2;                     // warps sharing the source rows of a point group
-constexpr int kCG = 4;                     // point groups per block
-constexpr int kCZ = kCP * kCG;             // field points per block
-constexpr int kContractThreads = kCG * kCH * 32;
-constexpr int kContractSmem = 96 * 1024;   // largest table + charge tile
-
-// 2^-36 fixed-point charge -> FP32 through two 32-bit conversions (a 64-bit
-// integer conversion runs on the FP64 pipe)
-__device__ inline float fixed_to_float(unsigned long long v) {
-  const long long s = (long long)v;
-  const int hi = (int)(s >> 32);
-  const unsigned lo = (unsigned)(v & 0xffffffffull);
-  return fmaf((float)hi, 4294967296.0f, (float)lo) * 1.4551915228366852e-11f;  // 2^-36
-}
-
-// source radii per staged tile: g(k) (2 nz float2) and charges (nz float)
-__host__ __device__ inline uint32_t contract_tile(uint32_t nx, uint32_t nz) {
-  const uint32_t t = (uint32_t)(kContractSmem / (20 * nz));
-  return t < nx ? t : nx;
-}
-// (bounds the tile of every mesh up to nx_max x nz_max)
-inline size_t contract_smem(uint32_t nx_max, uint32_t nz_max) {
-  return std::min<size_t>(kContractSmem, (size_t)20 * nx_max * nz_max);
-}
-
-// the bin limit of field row zp (the reference's partition of the table)
-__device__ inline uint32_t contract_lim(uint32_t zp, uint32_t rp, uint32_t nx, uint32_t nz) {
-  const uint32_t fld_sz = nx * nz;
-  if (zp < nz) {
-    const uint32_t gnum = 1024 / nz;
-    return gnum ? gnum * (fld_sz / gnum) : 0;
-  }
-  if (rp < nx) {
-    const uint32_t gnum = 1024 / nx;
-    return gnum ? gnum * (fld_sz / gnum) : 0;
-  }
-  return (fld_sz / 1024) * 1024;
-}
-
-// One block's work; TR > 0 is the tile width known at compile time (nr ==
-// TR, one tile: every shared-memory offset of the row walk is an immediate),
-// TR == 0 the general tiled form.
-template <int TR>
-__device__ __forceinline__ void contract_block(const ScState *sc, const ScTables &t, float *sm,
-                                               float2 (*upper)[kCP]) {
-  const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
-  const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ;
-  const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile(nx, nz);
-  float2 *gz = (float2 *)sm;          // [k + nz - 1][tr], k = -(nz - 1) .. nz
-  float *qs = sm + 4 * nz * tr;       // [zs][tr]
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int grp = warp / kCH, half = warp % kCH;
-  const uint32_t zp0 = zb0 + grp * kCP;  // points zp0 .. zp0 + kCP - 1
-  const uint32_t za = half * nz / kCH, zb = (half + 1) * nz / kCH;  // this warp's source rows
-  uint32_t lim[kCP];
-  bool cut = false;
-#pragma unroll
-  for (int j = 0; j < kCP; ++j) {
-    lim[j] = contract_lim(zp0 + j, rp, nx, nz);
-    cut |= zp0 + j <= nz && lim[j] < fld_sz;
-  }
-  const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * fld_sz;  // [dz][rs]
-  float ax[kCP], az[kCP];
-#pragma unroll
-  for (int j = 0; j < kCP; ++j) ax[j] = az[j] = 0.0f;
-  for (uint32_t rs0 = 0; rs0 < nx; rs0 += tr) {
-    const uint32_t ntr = TR > 0 ? (uint32_t)TR : min(tr, nx - rs0), ntile = nz * ntr;
-    __syncthreads();
-    // every load of a thread's share is issued before its first store: one
-    // memory round trip per kStage elements, not per element
-    constexpr int kStage = 8;
-    for (uint32_t e0 = threadIdx.x; e0 < ntile; e0 += kStage * blockDim.x) {
-      float2 gv[kStage];
-      unsigned long long bv[kStage];
-#pragma unroll
-      for (int u = 0; u < kStage; ++u) {
-        const uint32_t e = e0 + u * blockDim.x;
-        if (e < ntile) {
-          const uint32_t z = e / ntr, r = e - z * ntr;
-          gv[u] = __ldg(G + (size_t)z * nx + rs0 + r);
-          bv[u] = __ldg(t.bin_fx + z * nx + rs0 + r);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kStage; ++u) {
-        const uint32_t e = e0 + u * blockDim.x;
-        if (e < ntile) {
-          const uint32_t z = e / ntr, r = e - z * ntr;
-          gz[(nz + z) * tr + r] = gv[u];                                  // k = z + 1
-          gz[(nz - 1 - z) * tr + r] = make_float2(gv[u].x, -gv[u].y);     // k = -z
-          qs[z * tr + r] = fixed_to_float(bv[u]);
-        }
-      }
-    }
-    __syncthreads();
-    if (zp0 > nz) continue;
-    for (uint32_t r = lane; r < ntr; r += 32) {
-      if (!cut) {
-        // ring slot (j - u) mod R holds g(zp0 + j - zs), u = zs - zs0; the
-        // slot (-u - 1) mod R is free at row zs and takes g(zp0 - zs - 1).
-        // gp walks g(zp0 - zs - 1) down the rows, qp the charges up.
-        constexpr int R = kCP + 1;
-        float2 ring[R];
-        const float2 *g = gz + (nz - 1) * tr + r;  // g(k) at g[k * tr]
-#pragma unroll
-        for (int j = 0; j < kCP; ++j) ring[j] = g[min((int)(zp0 + j) - (int)za, (int)nz) * (int)tr];
-        const float2 *gp = g + ((int)zp0 - (int)za - 1) * (int)tr;
-        const float *qp = qs + za * tr + r;
-        for (uint32_t zs0 = za; zs0 < zb; zs0 += R, gp -= R * tr, qp += R * tr) {
-#pragma unroll
-          for (int u = 0; u < R; ++u) {
-            if (zs0 + u >= zb) break;
-            if (zs0 + u + 1 < zb) ring[(R - 1 - u) % R] = gp[-(int)(u * tr)];
-            const float qv = qp[u * tr];
-#pragma unroll
-            for (int j = 0; j < kCP; ++j) {
-              const float2 gv = ring[(j - u + R) % R];
-              ax[j] = fmaf(qv, gv.x, ax[j]);
-              az[j] = fmaf(qv, gv.y, az[j]);
-            }
-          }
-        }
-      } else {
-        // small meshes: each point sums the source rows below its own limit
-        const float *q = qs + r;
-        const float2 *g = gz + (nz - 1) * tr + r;
-        const uint32_t rs = rs0 + r;
-        for (int j = 0; j < kCP; ++j) {
-          if (zp0 + j > nz) continue;
-          const uint32_t zend = lim[j] > rs ? min(zb, (lim[j] - rs + nx - 1) / nx) : 0u;
-          for (uint32_t zs = za; zs < zend; ++zs) {
-            const float qv = q[zs * tr];
-            const float2 gv = g[((int)(zp0 + j) - (int)zs) * (int)tr];
-            ax[j] = fmaf(qv, gv.x, ax[j]);
-            az[j] = fmaf(qv, gv.y, az[j]);
-          }
-        }
-      }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < kCP; ++j) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      ax[j] += __shfl_down_sync(0xffffffffu, ax[j], off);
-      az[j] += __shfl_down_sync(0xffffffffu, az[j], off);
-    }
-  }
-  if (half == 1 && lane == 0)
-    for (int j = 0; j < kCP; ++j) upper[grp][j] = make_float2(ax[j], az[j]);
-  __syncthreads();
-  if (half != 0 || lane != 0 || zp0 > nz) return;
-  for (int j = 0; j < kCP; ++j) {
-    if (zp0 + j > nz) break;
-    const size_t pt = (size_t)(zp0 + j) * nrow + rp;
-    t.ffld2[2 * pt] = ax[j] + upper[grp][j].x;
-    t.ffld2[2 * pt + 1] = az[j] + upper[grp][j].y;
-  }
-}
-
-__global__ void __launch_bounds__(kContractThreads) k32_contract(const ScState *sc, ScTables t) {
-  if (!sc->remesh) return;
-  const uint32_t nx = sc->nx, nz = sc->nz;
-  if (blockIdx.x > nx || blockIdx.y * kCZ > nz) return;
-  extern __shared__ float sm[];
-  __shared__ float2 upper[kCG][kCP];  // second halves' sums
-  if (nx == 32 && contract_tile(nx, nz) == 32) contract_block<32>(sc, t, sm, upper);
-  else contract_block<0>(sc, t, sm, upper);
-}
-
 // ---- kick ----------------------------------------------------------------------
 // ApplySpchKickKernel (space_charge_kernel.cu:573-706) in FP32.  The skipped
 // set (i % skip_stride == 0) is tested as i & skip_mask == 0: the reference's
@@ -747,7 +560,8 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
   note_launch();
   dim3 cg(a.nx_max + 1, (a.nz_max + 1 + kCZ - 1) / kCZ);
-  launch_k(k32_contract, cg, dim3(kContractThreads), contract_smem(a.nx_max, a.nz_max), st, (const ScState *)sc, u);
+  launch_k(k_contract_t<float>, cg, dim3(kContractThreads), contract_smem<float>(a.nx_max, a.nz_max), st,
+           (const ScState *)sc, u);
   note_launch();
 }
 
@@ -767,7 +581,7 @@ void sc32_configure() {
   if (done) return;
   done = true;
   cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
-  cudaFuncSetAttribute(k32_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_t<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
 }
 
 namespace {
@@ -833,7 +647,7 @@ hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, co
     t.c32 = c32;
     k32_green<<<4 * 152, kBlock>>>(sc, t);
     dim3 cg(nr + 1, (nz + 1 + kCZ - 1) / kCZ);
-    k32_contract<<<cg, kContractThreads, contract_smem(nr, nz)>>>(sc, t);
+    k_contract_t<float><<<cg, kContractThreads, contract_smem<float>(nr, nz)>>>(sc, t);
     note_launch(4);
     e = cudaGetLastError();
   }
