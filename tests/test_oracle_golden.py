@@ -105,7 +105,8 @@ def test_field_from_charge_table(oracle):
     s = oracle.Scheff(8, 64, 0.02, 0)
     s.s.dr, s.s.dz = m[0], m[1]
     oracle.lib().orc_scheff_green_table(s.h, m[2], m[3], int(m[4]), m[5], int(m[6]))
-    C.memmove(s.s.bin, z["bin"].ctypes.data, z["bin"].nbytes)
+    bins = np.ascontiguousarray(z["bin"])  # every z[...] reads a new array: keep this one alive
+    C.memmove(s.s.bin, bins.ctypes.data, bins.nbytes)
     C.memset(s.s.fld2, 0, z["fld2"].nbytes)
     oracle.lib().orc_scheff_contract(s.h)
     _, fld1, fld2 = s.tables()
