@@ -536,6 +536,35 @@ class SpaceCharge:
         call("hps_scheff_get", self._h, {"solves": 8, "stat_sweeps": 9}[name], C.byref(out))
         return int(out.value)
 
+    def set_surrogate(self, net, tol=0.02, n_samples=64):
+        """Attach a trained field surrogate (not in the reference's API):
+        `net` is a surrogate.Network or its saved state (dict / npz).  FP64
+        beams' kicks on the network's mesh then take the network's field when
+        its relative residual against the plain sum at n_samples spot points
+        is <= tol, and the plain contraction otherwise."""
+        from . import surrogate
+        ex = surrogate.export(net.state() if hasattr(net, "state") else net)
+        n = len(ex["weights"])
+        arch = np.ascontiguousarray(ex["arch"], np.int32).reshape(-1)
+        skip = np.ascontiguousarray(ex["skip"], np.int32)
+        wts = [np.ascontiguousarray(w, np.uint16) for w in ex["weights"]]
+        bis = [np.ascontiguousarray(b, np.float32) for b in ex["biases"]]
+        wp = (C.c_void_p * n)(*[w.ctypes.data for w in wts])
+        bp = (C.c_void_p * n)(*[b.ctypes.data for b in bis])
+        call("hps_scheff_set_surrogate", self._h, n, arch.ctypes.data_as(C.POINTER(C.c_int)), int(ex["gmean_after"]),
+             skip.ctypes.data_as(C.POINTER(C.c_int)), wp, bp, int(ex["nr"]), int(ex["nz"]), float(ex["out_scale"]),
+             float(tol), int(n_samples))
+
+    def clear_surrogate(self):
+        call("hps_scheff_clear_surrogate", self._h)
+
+    def surrogate_stats(self):
+        """(kicks whose field the surrogate gave, kicks that fell back to the
+        plain contraction, the last spot residual)."""
+        a, r, res = C.c_double(), C.c_double(), C.c_double()
+        call("hps_scheff_surrogate_stats", self._h, C.byref(a), C.byref(r), C.byref(res))
+        return int(a.value), int(r.value), res.value
+
 
 class Simulator:
     """Simulator(beam=, beamline=, spch=None) (wrap_simulator.cpp:27-54).

@@ -83,6 +83,10 @@ def lib():
         "hps_scheff_set": (st, [vp, i32, d]),
         "hps_scheff_get": (st, [vp, i32, dp]),
         "hps_scheff_set_mesh_size": (st, [vp, u32, u32]),
+        "hps_scheff_snapshot": (st, [vp, i32, dp, dp, dp]),
+        "hps_scheff_set_surrogate": (st, [vp, i32, ip, i32, ip, C.POINTER(vp), C.POINTER(vp), u32, u32, d, d, u32]),
+        "hps_scheff_clear_surrogate": (st, [vp]),
+        "hps_scheff_surrogate_stats": (st, [vp, dp, dp, dp]),
         "hps_scheff_field": (st, [u32, u32, dp, dp, dp]),
         "hps_scheff_field_noalloc": (st, [u32, u32, vp, dp, vp, vp]),
         "hps_scheff_field_f32": (st, [u32, u32, dp, dp, dp]),
@@ -97,6 +101,14 @@ def lib():
         "hps_sim_last_time_ms": (st, [vp, dp]),
         "hps_sim_profile": (st, [vp, i32]),
         "hps_sim_profile_read": (st, [vp, dp, C.POINTER(C.c_uint64), i32]),
+        "hps_nn_conv_forward": (st, [ip, vp, vp, vp, i32, vp, vp, vp]),
+        "hps_nn_conv_backward": (st, [ip, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]),
+        "hps_nn_gmean_forward": (st, [vp, i32, i32, vp]),
+        "hps_nn_gmean_backward": (st, [vp, i32, i32, vp]),
+        "hps_nn_mse": (st, [vp, vp, C.c_int64, vp, C.c_int64, vp, vp, i32, vp]),
+        "hps_nn_add": (st, [vp, vp, vp, C.c_int64, i32, vp]),
+        "hps_nn_adam": (st, [vp, vp, vp, vp, vp, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]),
+        "hps_nn_convert": (st, [vp, vp, C.c_int64, i32, vp]),
         "hps_batch_create": (st, [pvp, u32, pvp]),
         "hps_batch_destroy": (st, [vp]),
         "hps_batch_simulate": (st, [vp, i32, i32]),

@@ -70,6 +70,8 @@ struct ScState {
   // FP32 beams: kicks whose statistics the element map before them could not
   // certify (the loss-test and moments sweeps ran)
   uint32_t n_stat_sweeps;
+  // FP64 beams with a field surrogate: this kick's field came from it
+  int sur_accepted;
 };
 
 // Constants of one FP32 SCHEFF kick, formed once per kick in FP32 by the

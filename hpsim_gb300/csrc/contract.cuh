@@ -222,7 +222,7 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
 // contract_smem<T>(nr_max, nz_max) bytes
 template <class T>
 __global__ void __launch_bounds__(kContractThreads) k_contract_t(const ScState *sc, ScTables t) {
-  if (!sc->remesh) return;
+  if (!sc->remesh || sc->sur_accepted) return;
   const uint32_t nx = sc->nx, nz = sc->nz;
   if (blockIdx.x > nx || blockIdx.y * kCZ > nz) return;
   extern __shared__ __align__(16) unsigned char contract_raw[];

@@ -5,6 +5,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
+#include <string>
+#include <vector>
+
 #include "common.cuh"
 
 namespace hps {
@@ -73,12 +77,46 @@ void sc_configure(size_t max_deposit_smem);
 // table, deposit, contraction; no-ops unless remeshing), kick
 void sc_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
               cudaStream_t st);
+struct SurNet;
 void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
-             cudaStream_t st);
+             cudaStream_t st, const SurNet *sur = nullptr);
 void sc_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
 void beam_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
 // Green's table (k_green) for a solver whose state says "remesh"
 void sc_green(const ScState *sc, const ScTables &t, uint32_t num_part, double cur_ov_mc2, cudaStream_t st);
+
+// ---- SCHEFF field surrogate (nn.cu, surrogate.cu) ------------------------
+// dims = {batch, c_in, c_out, h_in, w_in, stride, up}; skip may be null
+void nn_conv_forward(const int32_t *dims, const void *x, const void *w, const float *bias, int relu,
+                     const void *skip, void *y, cudaStream_t st);
+void nn_gmean_forward(void *y, int planes, int hw, cudaStream_t st);
+
+// A trained network attached to a solver, its device buffers (batch of one)
+// and its acceptance test
+struct SurNet {
+  std::vector<std::array<int, 5>> arch;  // c_in, c_out, stride, up, relu
+  std::vector<int32_t> dims;             // 7 per layer
+  std::vector<int> hw, skip;             // output plane size; layer whose output is added (-1: none)
+  int gmean_after = -1;
+  std::vector<void *> w, act;            // BF16 weights and outputs
+  std::vector<float *> b;
+  void *x = nullptr, *spot = nullptr, *d = nullptr;
+  uint32_t nr = 0, nz = 0, n_samples = 0;
+  double out_scale = 1.0, tol = 0.0;
+  SurNet() = default;
+  SurNet(const SurNet &) = delete;
+  SurNet &operator=(const SurNet &) = delete;
+  ~SurNet();
+};
+// 0 ok, 1 invalid (err says why), 2 device error
+int sur_build(SurNet &n, int n_layers, const int32_t *arch, int gmean_after, const int32_t *skip,
+              const uint16_t *const *weights, const float *const *biases, uint32_t nr, uint32_t nz, double out_scale,
+              double tol, uint32_t n_samples, std::string &err);
+// after the deposit of an FP64 kick: the network's field, checked at spot
+// points, accepted into the field table or left to the contraction
+void sur_solve(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, const SurNet &n,
+               cudaStream_t st);
+int sur_read(const SurNet &n, double *accepted, double *rejected, double *residual);
 
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
 // An element map fused with the space-charge sweep next to it:

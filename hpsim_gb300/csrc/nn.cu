@@ -1,0 +1,500 @@
+// nn.cu -- the layers of the SCHEFF field surrogate: 3x3 convolutions with
+// stride 1 or 2 and an optional nearest 2x upsampling of their input, bias
+// and ReLU, a global-mean broadcast, the squared-error loss and Adam, forward
+// and backward.  Activations and the weights the forward pass reads are
+// BF16; every sum is FP32 (one thread owns each output and sums in a fixed
+// order, so results do not depend on scheduling); master weights and
+// gradients are FP32.
+//
+// Tensors are [batch][channel][z][r] (row-major, r fastest).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cooperative_groups.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/hpsim_gb300.h"
+#include "internal.h"
+
+namespace hps {
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+constexpr int kNnBlock = 256;
+constexpr int kCoTile = 8;  // output channels per thread in the forward conv
+constexpr int kMaxCi = 512;  // input channels of one layer (weights staged in shared memory)
+constexpr int kConvSmemMax = (kMaxCi * 9 * kCoTile + 2 * kCoTile * kNnBlock) * 4;
+
+struct ConvShape {
+  int B, Ci, Co, Hi, Wi, Ho, Wo, stride, up;  // up: 1 or 2 (nearest upsampling of the input first)
+};
+
+__device__ inline float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
+
+// input value at upsampled coordinates (Y, X) of channel plane p (zero outside)
+__device__ inline float in_at(const __nv_bfloat16 *p, int Y, int X, int Hi, int Wi, int up) {
+  const int Hu = Hi * up, Wu = Wi * up;
+  if (Y < 0 || X < 0 || Y >= Hu || X >= Wu) return 0.0f;
+  return bf(p[(Y / up) * Wi + X / up]);
+}
+
+// in_at with the upsampling factor known at compile time
+template <int U>
+__device__ inline float in_at_u(const __nv_bfloat16 *p, int Y, int X, int Hi, int Wi) {
+  if (Y < 0 || X < 0 || Y >= Hi * U || X >= Wi * U) return 0.0f;
+  return bf(p[(Y / U) * Wi + X / U]);
+}
+
+// out[b][co][oy][ox] = bias[co] + sum_ci sum_ky,kx w[co][ci][ky][kx] in_up[b][ci][oy*S+ky-1][ox*S+kx-1],
+// then ReLU when relu != 0, then (skip != null) BF16-rounded and added to
+// skip[b][co][oy][ox].
+// A cluster of `cl` CTAs (consecutive in x) shares one (pixel tile,
+// kCoTile output channels, batch) and splits the input channels into cl
+// contiguous ranges; inside a CTA `split` slices of threads take the range's
+// channels in turn over P = kNnBlock / split pixels, each thread kCoTile
+// sums.  A CTA stages its weights (contiguous runs of [co][ci][3][3], read
+// coalesced) in shared memory as FP32 [ci][tap][co], so one input channel's
+// 72 weights are read as broadcasts.  Slice partials are added in slice
+// order, then rank 0 adds the other CTAs' sums through distributed shared
+// memory in rank order: the result depends only on the launch shape.
+template <int S, int U>
+__global__ void __launch_bounds__(kNnBlock) k_conv_fwd(ConvShape s, int split, int cl, const __nv_bfloat16 *x,
+                                                       const __nv_bfloat16 *w, const float *bias, int relu,
+                                                       const __nv_bfloat16 *skip, __nv_bfloat16 *y) {
+  extern __shared__ float conv_smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int P = kNnBlock / split;
+  const int co0 = blockIdx.y * kCoTile, b = blockIdx.z;
+  const int nco = min(kCoTile, s.Co - co0);
+  const int cpr = (s.Ci + cl - 1) / cl;                 // input channels per rank
+  const int ci_lo = min(s.Ci, rank * cpr), ci_hi = min(s.Ci, ci_lo + cpr);
+  const int nci = ci_hi - ci_lo;
+  float *ws = conv_smem;                                // [cpr][9][kCoTile]
+  float *part = conv_smem + (size_t)cpr * 9 * kCoTile;  // [split][kCoTile][P]
+  float *csum = part + (size_t)split * kCoTile * P;     // [kCoTile][P]: this CTA's sums
+  if (nco < kCoTile)
+    for (int i = threadIdx.x; i < nci * 9 * kCoTile; i += blockDim.x) ws[i] = 0.0f;
+  __syncthreads();
+  const int run = nci * 9;  // each output channel's weights of this range are contiguous
+  for (int j = threadIdx.x; j < nco * run; j += blockDim.x) {
+    const int k = j / run, r = j - k * run;
+    ws[r * kCoTile + k] = bf(w[((size_t)(co0 + k) * s.Ci + ci_lo) * 9 + r]);
+  }
+  __syncthreads();
+  const int slice = threadIdx.x / P, lp = threadIdx.x % P;
+  const int npix = s.Ho * s.Wo;
+  const int pix = (blockIdx.x / cl) * P + lp;
+  float acc[kCoTile];
+#pragma unroll
+  for (int k = 0; k < kCoTile; ++k) acc[k] = 0.0f;
+  if (pix < npix) {
+    const int oy = pix / s.Wo, ox = pix % s.Wo;
+    const int Y0 = oy * S - 1, X0 = ox * S - 1;
+    const size_t plane = (size_t)s.Hi * s.Wi;
+    const __nv_bfloat16 *xb = x + ((size_t)b * s.Ci + ci_lo) * plane;
+#pragma unroll 2
+    for (int c = slice; c < nci; c += split) {
+      const __nv_bfloat16 *p = xb + c * plane;
+      const float *wc = ws + c * 9 * kCoTile;
+      float v[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) v[t] = in_at_u<U>(p, Y0 + t / 3, X0 + t % 3, s.Hi, s.Wi);
+#pragma unroll
+      for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int k = 0; k < kCoTile; ++k) acc[k] = fmaf(wc[t * kCoTile + k], v[t], acc[k]);
+    }
+  }
+  if (split > 1) {
+#pragma unroll
+    for (int k = 0; k < kCoTile; ++k) part[((size_t)slice * kCoTile + k) * P + lp] = acc[k];
+    __syncthreads();
+    if (slice == 0) {
+#pragma unroll
+      for (int k = 0; k < kCoTile; ++k) {
+        float a = part[(size_t)k * P + lp];
+        for (int sl = 1; sl < split; ++sl) a += part[((size_t)sl * kCoTile + k) * P + lp];
+        acc[k] = a;
+      }
+    }
+  }
+  if (cl > 1) {
+    if (slice == 0)
+#pragma unroll
+      for (int k = 0; k < kCoTile; ++k) csum[k * P + lp] = acc[k];
+    cluster.sync();
+    if (rank == 0 && slice == 0)
+      for (int r = 1; r < cl; ++r) {
+        const float *rs = cluster.map_shared_rank(csum, r);
+#pragma unroll
+        for (int k = 0; k < kCoTile; ++k) acc[k] += rs[k * P + lp];
+      }
+    cluster.sync();  // the other CTAs' sums stay until rank 0 has read them
+  }
+  if (rank != 0 || slice != 0 || pix >= npix) return;
+  for (int k = 0; k < nco; ++k) {
+    float a = acc[k] + bias[co0 + k];
+    if (relu && a < 0.0f) a = 0.0f;
+    const size_t o = ((size_t)b * s.Co + co0 + k) * npix + pix;
+    y[o] = skip ? __float2bfloat16_rn(bf(__float2bfloat16_rn(a)) + bf(skip[o])) : __float2bfloat16_rn(a);
+  }
+}
+
+// dy masked by the ReLU of the forward output (y > 0), in FP32
+__global__ void k_relu_bwd(const float *dy, const __nv_bfloat16 *y, int relu, float *dz, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dz[i] = (!relu || bf(y[i]) > 0.0f) ? dy[i] : 0.0f;
+}
+
+// dx[b][ci][iy][ix] = sum over the outputs that read input (iy, ix) through
+// the upsampling and the 3x3 window of w[co][ci][ky][kx] dz[b][co][oy][ox]
+__global__ void __launch_bounds__(kNnBlock) k_conv_bwd_data(ConvShape s, const float *dz, const __nv_bfloat16 *w,
+                                                            float *dx) {
+  const long long total = (long long)s.B * s.Ci * s.Hi * s.Wi;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(g % s.Wi);
+    const int iy = (int)((g / s.Wi) % s.Hi);
+    const int ci = (int)((g / ((long long)s.Wi * s.Hi)) % s.Ci);
+    const int b = (int)(g / ((long long)s.Wi * s.Hi * s.Ci));
+    float acc = 0.0f;
+    for (int uy = 0; uy < s.up; ++uy)
+      for (int ux = 0; ux < s.up; ++ux) {
+        const int Y = iy * s.up + uy, X = ix * s.up + ux;  // upsampled position
+        for (int ky = 0; ky < 3; ++ky) {
+          const int ny = Y - ky + 1;  // = oy * stride
+          if (ny < 0 || ny % s.stride) continue;
+          const int oy = ny / s.stride;
+          if (oy >= s.Ho) continue;
+          for (int kx = 0; kx < 3; ++kx) {
+            const int nx = X - kx + 1;
+            if (nx < 0 || nx % s.stride) continue;
+            const int ox = nx / s.stride;
+            if (ox >= s.Wo) continue;
+            for (int co = 0; co < s.Co; ++co)
+              acc = fmaf(bf(w[((size_t)co * s.Ci + ci) * 9 + ky * 3 + kx]),
+                         dz[(((size_t)b * s.Co + co) * s.Ho + oy) * s.Wo + ox], acc);
+          }
+        }
+      }
+    dx[g] = acc;
+  }
+}
+
+// dw[co][ci][ky][kx] = sum_b,oy,ox dz[b][co][oy][ox] in_up[b][ci][oy*s+ky-1][ox*s+kx-1];
+// db[co] = sum dz.  One block per (co, ci), a fixed tree over its threads.
+__global__ void __launch_bounds__(kNnBlock) k_conv_bwd_weight(ConvShape s, const float *dz, const __nv_bfloat16 *x,
+                                                              float *dw, float *db) {
+  __shared__ float red[10][kNnBlock];
+  const int co = blockIdx.x / s.Ci, ci = blockIdx.x % s.Ci;
+  float acc[10];
+#pragma unroll
+  for (int t = 0; t < 10; ++t) acc[t] = 0.0f;
+  const int npix = s.Ho * s.Wo;
+  for (int g = threadIdx.x; g < s.B * npix; g += blockDim.x) {
+    const int b = g / npix, pix = g % npix;
+    const int oy = pix / s.Wo, ox = pix % s.Wo;
+    const float d = dz[((size_t)b * s.Co + co) * npix + pix];
+    if (d == 0.0f) continue;
+    const __nv_bfloat16 *p = x + ((size_t)b * s.Ci + ci) * s.Hi * s.Wi;
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx)
+        acc[ky * 3 + kx] = fmaf(d, in_at(p, oy * s.stride + ky - 1, ox * s.stride + kx - 1, s.Hi, s.Wi, s.up),
+                                acc[ky * 3 + kx]);
+    acc[9] += d;
+  }
+#pragma unroll
+  for (int t = 0; t < 10; ++t) red[t][threadIdx.x] = acc[t];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+#pragma unroll
+      for (int t = 0; t < 10; ++t) red[t][threadIdx.x] += red[t][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x < 9) dw[((size_t)co * s.Ci + ci) * 9 + threadIdx.x] = red[threadIdx.x][0];
+  if (threadIdx.x == 9 && ci == 0) {
+    // every (co, ci) block summed the same dz: the bias gradient once, from ci 0
+    db[co] = red[9][0];
+  }
+}
+
+// y[b][c] += mean over the plane of y[b][c] (in place, BF16): each plane by
+// one block, a fixed tree
+__global__ void __launch_bounds__(kNnBlock) k_gmean_fwd(__nv_bfloat16 *y, int planes, int hw) {
+  __shared__ float red[kNnBlock];
+  __shared__ float mean;
+  __nv_bfloat16 *p = y + (size_t)blockIdx.x * hw;
+  float a = 0.0f;
+  for (int i = threadIdx.x; i < hw; i += blockDim.x) a += bf(p[i]);
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mean = red[0] / (float)hw;
+  __syncthreads();
+  for (int i = threadIdx.x; i < hw; i += blockDim.x) p[i] = __float2bfloat16_rn(bf(p[i]) + mean);
+}
+
+// backward of y' = y + mean(y): dy = dy' + mean(dy') (in place, FP32)
+__global__ void __launch_bounds__(kNnBlock) k_gmean_bwd(float *d, int planes, int hw) {
+  __shared__ float red[kNnBlock];
+  __shared__ float mean;
+  float *p = d + (size_t)blockIdx.x * hw;
+  float a = 0.0f;
+  for (int i = threadIdx.x; i < hw; i += blockDim.x) a += p[i];
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mean = red[0] / (float)hw;
+  __syncthreads();
+  for (int i = threadIdx.x; i < hw; i += blockDim.x) p[i] += mean;
+}
+
+// loss partial sums of wt (pred - target)^2 per block and dpred = 2 wt (pred -
+// target) / n, wt = weight[i / per_sample] (1 without weights)
+__global__ void __launch_bounds__(kNnBlock) k_mse(const __nv_bfloat16 *pred, const float *target, long long n,
+                                                  const float *weight, long long per_sample, float *dpred,
+                                                  float *partial) {
+  __shared__ float red[kNnBlock];
+  float a = 0.0f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float e = bf(pred[i]) - target[i];
+    const float wt = weight ? weight[i / per_sample] : 1.0f;
+    a = fmaf(wt * e, e, a);
+    dpred[i] = 2.0f * wt * e / (float)n;
+  }
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// Adam on FP32 master weights, then their BF16 copy for the forward pass
+__global__ void k_adam(float *w, __nv_bfloat16 *wb, const float *g, float *m, float *v, long long n, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+// y = a + b elementwise (skip connections: BF16 activations, FP32 gradients)
+__global__ void k_add_bf16(const __nv_bfloat16 *a, const __nv_bfloat16 *b, __nv_bfloat16 *y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = __float2bfloat16_rn(bf(a[i]) + bf(b[i]));
+}
+__global__ void k_add_f32(const float *a, const float *b, float *y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = a[i] + b[i];
+}
+
+__global__ void k_to_bf16(const float *a, __nv_bfloat16 *b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = __float2bfloat16_rn(a[i]);
+}
+__global__ void k_to_f32(const __nv_bfloat16 *a, float *b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = bf(a[i]);
+}
+
+int nn_grid(long long n) {
+  long long g = (n + kNnBlock - 1) / kNnBlock;
+  if (g < 1) g = 1;
+  if (g > 152 * 8) g = 152 * 8;
+  return (int)g;
+}
+
+ConvShape shape(const int32_t *d) {
+  ConvShape s;
+  s.B = d[0]; s.Ci = d[1]; s.Co = d[2]; s.Hi = d[3]; s.Wi = d[4]; s.stride = d[5]; s.up = d[6];
+  s.Ho = (s.Hi * s.up - 1) / s.stride + 1;
+  s.Wo = (s.Wi * s.up - 1) / s.stride + 1;
+  return s;
+}
+
+bool shape_ok(const int32_t *d) {
+  return d && d[0] > 0 && d[0] <= 65535 && d[1] > 0 && d[1] <= kMaxCi && d[2] > 0 && d[3] > 0 && d[4] > 0 &&
+         (d[5] == 1 || d[5] == 2) && (d[6] == 1 || d[6] == 2);
+}
+
+}  // namespace
+
+// pixels per block: 32, or 16 for planes of at most 16 pixels (their
+// blocks then split the input channels 16 ways)
+int conv_pixels(int npix) { return npix <= 16 ? 16 : 32; }
+
+int conv_split(int ci, int P) {
+  int sp = 1;
+  while (sp < kNnBlock / P && sp * 2 <= ci) sp *= 2;
+  return sp;
+}
+
+// CTAs per cluster: up to 8, until a layer has about four CTAs per SM,
+// keeping at least 8 input channels per CTA
+int conv_cluster(long long blocks, int ci) {
+  int cl = 1;
+  while (cl < 8 && blocks * cl < 4 * 152 && ci / (cl * 2) >= 8) cl *= 2;
+  return cl;
+}
+
+size_t conv_smem(int cpr, int split) {
+  return ((size_t)cpr * 9 * kCoTile + (size_t)kCoTile * kNnBlock + (size_t)kCoTile * (kNnBlock / split)) *
+         sizeof(float);
+}
+
+template <int S, int U>
+void conv_launch(const ConvShape &s, const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *bias, int relu,
+                 const __nv_bfloat16 *skip, __nv_bfloat16 *y, cudaStream_t st) {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_conv_fwd<S, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
+  });
+  const int npix = s.Ho * s.Wo;
+  const int P0 = conv_pixels(npix);
+  const int ntiles = (npix + P0 - 1) / P0, nct = (s.Co + kCoTile - 1) / kCoTile;
+  const int cl = conv_cluster((long long)ntiles * nct * s.B, s.Ci);
+  const int cpr = (s.Ci + cl - 1) / cl;
+  const int split = conv_split(cpr, P0), P = kNnBlock / split;
+  const int ptiles = (npix + P - 1) / P;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ptiles * cl, nct, s.B);
+  cfg.blockDim = dim3(kNnBlock);
+  cfg.dynamicSmemBytes = conv_smem(cpr, split);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_conv_fwd<S, U>, s, split, cl, x, w, bias, relu, skip, y);
+}
+
+void nn_conv_forward(const int32_t *dims, const void *x, const void *w, const float *bias, int relu,
+                     const void *skip, void *y, cudaStream_t st) {
+  const ConvShape s = shape(dims);
+  auto xb = (const __nv_bfloat16 *)x, wb = (const __nv_bfloat16 *)w, kb = (const __nv_bfloat16 *)skip;
+  auto yb = (__nv_bfloat16 *)y;
+  if (s.stride == 1 && s.up == 1) conv_launch<1, 1>(s, xb, wb, bias, relu, kb, yb, st);
+  else if (s.stride == 2 && s.up == 1) conv_launch<2, 1>(s, xb, wb, bias, relu, kb, yb, st);
+  else if (s.stride == 1) conv_launch<1, 2>(s, xb, wb, bias, relu, kb, yb, st);
+  else conv_launch<2, 2>(s, xb, wb, bias, relu, kb, yb, st);
+  note_launch();
+}
+
+void nn_gmean_forward(void *y, int planes, int hw, cudaStream_t st) {
+  k_gmean_fwd<<<planes, kNnBlock, 0, st>>>((__nv_bfloat16 *)y, planes, hw);
+  note_launch();
+}
+
+}  // namespace hps
+
+extern "C" {
+
+using namespace hps;
+
+static hps_status nn_status(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(e)).c_str());
+  return HPS_OK;
+}
+
+hps_status hps_nn_conv_forward(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,
+                               const void *skip, void *y, void *stream) {
+  if (!shape_ok(dims) || !x || !w || !bias || !y) return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_forward: bad argument");
+  nn_conv_forward(dims, x, w, bias, relu, skip, y, (cudaStream_t)stream);
+  return nn_status("nn_conv_forward");
+}
+
+hps_status hps_nn_conv_backward(const int32_t dims[7], const void *x, const void *w, const void *y, int relu,
+                                const float *dy, float *dz, float *dx, float *dw, float *db, void *stream) {
+  if (!shape_ok(dims) || !x || !w || !y || !dy || !dz || !dw || !db)
+    return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_backward: bad argument");
+  const ConvShape s = shape(dims);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long nout = (long long)s.B * s.Co * s.Ho * s.Wo;
+  k_relu_bwd<<<nn_grid(nout), kNnBlock, 0, st>>>(dy, (const __nv_bfloat16 *)y, relu, dz, nout);
+  k_conv_bwd_weight<<<s.Co * s.Ci, kNnBlock, 0, st>>>(s, dz, (const __nv_bfloat16 *)x, dw, db);
+  note_launch(2);
+  if (dx) {
+    const long long nin = (long long)s.B * s.Ci * s.Hi * s.Wi;
+    k_conv_bwd_data<<<nn_grid(nin), kNnBlock, 0, st>>>(s, dz, (const __nv_bfloat16 *)w, dx);
+    note_launch();
+  }
+  return nn_status("nn_conv_backward");
+}
+
+hps_status hps_nn_gmean_forward(void *y, int32_t planes, int32_t hw, void *stream) {
+  if (!y || planes <= 0 || hw <= 0) return (hps_status)set_error(HPS_ERR_INVALID, "nn_gmean_forward: bad argument");
+  nn_gmean_forward(y, planes, hw, (cudaStream_t)stream);
+  return nn_status("nn_gmean_forward");
+}
+
+hps_status hps_nn_gmean_backward(float *d, int32_t planes, int32_t hw, void *stream) {
+  if (!d || planes <= 0 || hw <= 0) return (hps_status)set_error(HPS_ERR_INVALID, "nn_gmean_backward: bad argument");
+  k_gmean_bwd<<<planes, kNnBlock, 0, (cudaStream_t)stream>>>(d, planes, hw);
+  note_launch();
+  return nn_status("nn_gmean_backward");
+}
+
+hps_status hps_nn_mse(const void *pred, const float *target, int64_t n, const float *weight, int64_t per_sample,
+                      float *dpred, float *partial, int32_t nblocks, void *stream) {
+  if (!pred || !target || !dpred || !partial || n <= 0 || nblocks <= 0 || (weight && per_sample <= 0))
+    return (hps_status)set_error(HPS_ERR_INVALID, "nn_mse: bad argument");
+  k_mse<<<nblocks, kNnBlock, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)pred, target, n, weight, per_sample,
+                                                        dpred, partial);
+  note_launch();
+  return nn_status("nn_mse");
+}
+
+hps_status hps_nn_adam(float *w, void *w_bf16, const float *g, float *m, float *v, int64_t n, float lr, float b1,
+                       float b2, float eps, int32_t step, void *stream) {
+  if (!w || !g || !m || !v || n <= 0 || step < 1) return (hps_status)set_error(HPS_ERR_INVALID, "nn_adam: bad argument");
+  const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+  k_adam<<<nn_grid(n), kNnBlock, 0, (cudaStream_t)stream>>>(w, (__nv_bfloat16 *)w_bf16, g, m, v, n, lr, b1, b2, eps,
+                                                             c1, c2);
+  note_launch();
+  return nn_status("nn_adam");
+}
+
+hps_status hps_nn_add(const void *a, const void *b, void *y, int64_t n, int bf16, void *stream) {
+  if (!a || !b || !y || n <= 0) return (hps_status)set_error(HPS_ERR_INVALID, "nn_add: bad argument");
+  if (bf16) k_add_bf16<<<nn_grid(n), kNnBlock, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)a,
+                                                                            (const __nv_bfloat16 *)b,
+                                                                            (__nv_bfloat16 *)y, n);
+  else k_add_f32<<<nn_grid(n), kNnBlock, 0, (cudaStream_t)stream>>>((const float *)a, (const float *)b, (float *)y, n);
+  note_launch();
+  return nn_status("nn_add");
+}
+
+hps_status hps_nn_convert(const void *src, void *dst, int64_t n, int to_bf16, void *stream) {
+  if (!src || !dst || n <= 0) return (hps_status)set_error(HPS_ERR_INVALID, "nn_convert: bad argument");
+  if (to_bf16) k_to_bf16<<<nn_grid(n), kNnBlock, 0, (cudaStream_t)stream>>>((const float *)src, (__nv_bfloat16 *)dst, n);
+  else k_to_f32<<<nn_grid(n), kNnBlock, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)src, (float *)dst, n);
+  note_launch();
+  return nn_status("nn_convert");
+}
+
+}  // extern "C"

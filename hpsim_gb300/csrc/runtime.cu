@@ -89,6 +89,7 @@ struct hps_scheff_s {
   ScState *d = nullptr;
   ScTables t{};
   uint64_t version = 0;
+  SurNet *sur = nullptr;  // field surrogate (FP64 beams), owned
 };
 
 struct GraphEntry {
@@ -790,6 +791,7 @@ hps_status hps_scheff_destroy(hps_scheff_t s) {
   if (s->t.ffld1) cudaFree(s->t.ffld1);
   if (s->t.ffld2) cudaFree(s->t.ffld2);
   if (s->t.c32) cudaFree(s->t.c32);
+  delete s->sur;
   delete s;
   return HPS_OK;
 }
@@ -831,6 +833,31 @@ hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
   }
   return HPS_OK;
 }
+// The solver's tables after its last kick: charge (nr*nz, bin (zs, rs) at
+// zs*nr + rs), field ((nz+1)*(nr+1) pairs) of the FP32 or FP64 tables, and
+// mesh = {nr, nz, dr, dz, beta, num_on_mesh, remesh}; arrays sized for the
+// largest mesh.
+hps_status hps_scheff_snapshot(hps_scheff_t s, int fp32, double *bins, double *field, double *mesh) {
+  if (!s || !bins || !field || !mesh) return fail(HPS_ERR_INVALID, "scheff_snapshot: bad argument");
+  CK(cudaDeviceSynchronize());
+  ScState h;
+  CK(cudaMemcpy(&h, s->d, sizeof(h), cudaMemcpyDeviceToHost));
+  const size_t nb = (size_t)h.nx * h.nz, nf = (size_t)(h.nz + 1) * (h.nx + 1) * 2;
+  std::vector<unsigned long long> fx(nb);
+  CK(cudaMemcpy(fx.data(), s->t.bin_fx, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  for (size_t k = 0; k < nb; ++k) bins[k] = (double)(long long)fx[k] * kBinInvScale;
+  if (fp32) {
+    std::vector<float> f(nf);
+    CK(cudaMemcpy(f.data(), s->t.ffld2, nf * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < nf; ++k) field[k] = f[k];
+  } else {
+    CK(cudaMemcpy(field, s->t.fld2, nf * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  mesh[0] = h.nx; mesh[1] = h.nz; mesh[2] = h.dr; mesh[3] = h.dz; mesh[4] = h.beta;
+  mesh[5] = h.num_on_mesh; mesh[6] = h.remesh;
+  return HPS_OK;
+}
+
 // Scheff::SetMeshSize, space_charge.cpp:61-73 (tables reallocated and zeroed)
 hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz) {
   if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
@@ -843,6 +870,41 @@ hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz) {
   hps_status st = scheff_alloc_tables(s);
   if (st) return st;
   return scheff_upload(s);
+}
+
+hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int32_t *arch, int32_t gmean_after,
+                                    const int32_t *skip, const uint16_t *const *weights, const float *const *biases,
+                                    uint32_t nr, uint32_t nz, double out_scale, double tol, uint32_t n_samples) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  CK(cudaDeviceSynchronize());
+  SurNet *n = new SurNet();
+  std::string err;
+  const int r = sur_build(*n, n_layers, arch, gmean_after, skip, weights, biases, nr, nz, out_scale, tol, n_samples,
+                          err);
+  if (r) {
+    delete n;
+    return fail(r == 1 ? HPS_ERR_INVALID : HPS_ERR_CUDA, ("scheff_set_surrogate: " + err).c_str());
+  }
+  delete s->sur;
+  s->sur = n;
+  s->version++;
+  return HPS_OK;
+}
+
+hps_status hps_scheff_clear_surrogate(hps_scheff_t s) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  if (!s->sur) return HPS_OK;
+  CK(cudaDeviceSynchronize());
+  delete s->sur;
+  s->sur = nullptr;
+  s->version++;
+  return HPS_OK;
+}
+
+hps_status hps_scheff_surrogate_stats(hps_scheff_t s, double *accepted, double *rejected, double *residual) {
+  if (!s || !s->sur) return fail(HPS_ERR_INVALID, "scheff_surrogate_stats: no surrogate attached");
+  if (sur_read(*s->sur, accepted, rejected, residual)) return fail(HPS_ERR_CUDA, "scheff_surrogate_stats: read failed");
+  return HPS_OK;
 }
 
 }  // extern "C"
@@ -967,7 +1029,7 @@ void sc_apply(Ctx &c, double length, bool fused = false) {
   ScTables t = c.sc->t;
   t.ffld2 = nullptr;  // FP64 beams use fld2
   PHASE(HPS_PROF_SC_STATS, sc_stats(b->d, c.sc->d, t, a, b->scr, b->stream));
-  PHASE(HPS_PROF_SC_MESH, sc_mesh(b->d, c.sc->d, t, a, b->scr, b->stream));
+  PHASE(HPS_PROF_SC_MESH, sc_mesh(b->d, c.sc->d, t, a, b->scr, b->stream, c.sc->sur));
   PHASE(HPS_PROF_SC_KICK, sc_kick(b->d, c.sc->d, t, a, b->stream));
 }
 
@@ -1203,6 +1265,10 @@ hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
   p->start_index = start < 0 ? 0 : start;
   p->end_index = end < 0 ? n - 1 : end;
   if (p->start_index >= n || p->end_index >= n) return fail(HPS_ERR_INVALID, "simulate: element index out of range");
+  // prev_end_element_index_ is an int set to UINT_MAX, i.e. -1
+  // (simulation_engine.cpp:51, simulation_engine.h:66): the first call does
+  // not reset, so the design energy and wavelength are the beam's at the
+  // simulator's creation
   if (p->start_index < s->prev_end) hps_sim_reset(s);
   s->prev_end = p->end_index;
   hps_beam_t b = c.b;

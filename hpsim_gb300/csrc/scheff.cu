@@ -436,7 +436,7 @@ void contract64(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t 
 }
 
 void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
-             cudaStream_t st) {
+             cudaStream_t st, const SurNet *sur) {
   launch_pass(OpAdjMesh{b, sc}, b.n, s, st);
   note_launch();
   // mesh kernels are sized for the largest mesh this solver can take
@@ -446,6 +446,8 @@ void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs 
     k_deposit<<<grid_for(b.n), kBlock, a.deposit_smem, st>>>(b, sc, t);
     note_launch();
   }
+  // an accepted surrogate field makes the contraction return at once
+  if (sur) sur_solve(b, sc, t, a, *sur, st);
   contract64(sc, t, a.nx_max, a.nz_max, st);
   note_launch();
 }

@@ -1,0 +1,296 @@
+// surrogate.cu -- the learned SCHEFF field surrogate inside an FP64 beam's
+// space-charge kick, with a spot-solve residual check and fallback to the
+// plain contraction.  Launch sequence of a kick that remeshes (after the
+// Green's table and the deposit, before the contraction):
+//   k_sur_input   charge / total and log cell aspect as the network input
+//                 (BF16), the field scale, the acceptance flag cleared;
+//   the network   its 3x3 convolution layers (nn.cu) with the skip additions
+//                 fused and the plane-mean broadcast, on a batch of one;
+//   k_sur_spot    the exact field (the plain method's sum over every bin of
+//                 charge times Green's table) at the mesh's last row and
+//                 column, which the network does not predict, and at
+//                 n_samples interior points drawn per solve;
+//   k_sur_apply   the relative residual of the network's field at the
+//                 sample points; within tolerance, the field table gets the
+//                 network's interior and the exact boundary, and the solver
+//                 state says so: the contraction then returns at once.
+// Kicks that do not remesh, meshes other than the trained one and empty
+// meshes leave everything to the plain path.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/hpsim_gb300.h"
+#include "internal.h"
+
+namespace hps {
+
+namespace {
+
+constexpr int kSurBlock = 256;
+
+struct SurDev {
+  int active;          // this kick is the surrogate's to try
+  double total;        // charge on the mesh (bin units)
+  double scale;        // field = network output * scale
+  double residual;     // relative residual of the last check
+  uint32_t n_accepted, n_rejected;
+};
+
+__device__ inline uint32_t mix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7feb352du;
+  h ^= h >> 15;
+  h *= 0x846ca68bu;
+  h ^= h >> 16;
+  return h;
+}
+
+// field point of spot index k: the last row (zp = nz, rp = 0..nr), the last
+// column (rp = nr, zp = 0..nz-1), then the interior samples of this solve
+__device__ inline void spot_point(uint32_t k, uint32_t nr, uint32_t nz, uint32_t solve, uint32_t &zp,
+                                  uint32_t &rp) {
+  if (k <= nr) { zp = nz; rp = k; return; }
+  k -= nr + 1;
+  if (k < nz) { zp = k; rp = nr; return; }
+  k -= nz;
+  const uint32_t h = mix32(solve * 0x9e3779b9u + k * 0x85ebca6bu + 0x632be5abu);
+  zp = h % nz;
+  rp = (h >> 16) % nr;
+}
+
+__global__ void __launch_bounds__(1024) k_sur_input(ScState *sc, ScTables t, SurDev *sd, __nv_bfloat16 *x,
+                                                    uint32_t nr, uint32_t nz, double out_scale, uint32_t num_part,
+                                                    double cur_ov_mc2) {
+  __shared__ unsigned long long red[1024];
+  __shared__ int go;
+  if (threadIdx.x == 0) {
+    sc->sur_accepted = 0;
+    go = sc->remesh && sc->nx == nr && sc->nz == nz;
+  }
+  __syncthreads();
+  if (!go) {
+    if (threadIdx.x == 0) sd->active = 0;
+    return;
+  }
+  const uint32_t nb = nr * nz;
+  unsigned long long a = 0;
+  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) a += t.bin_fx[k];
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  const double total = (double)(long long)red[0] * kBinInvScale;
+  const double gm = rsqrt(1.0 - sc->beta * sc->beta);
+  const double dzg = sc->dz * gm;
+  if (threadIdx.x == 0) {
+    const double c1 = 5721.67 * cur_ov_mc2 / (sc->freq * 1e6 * (double)num_part);
+    sd->active = total > 0.0;
+    sd->total = total;
+    sd->scale = c1 * total / (out_scale * sc->dr * dzg);
+  }
+  if (!(total > 0.0)) return;
+  const float qs = (float)((double)nb / total);
+  const __nv_bfloat16 la = __float2bfloat16_rn((float)log(dzg / sc->dr));
+  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
+    x[k] = __float2bfloat16_rn((float)((double)(long long)t.bin_fx[k] * kBinInvScale) * qs);
+    x[nb + k] = la;
+  }
+}
+
+// exact field at one spot point per block (FP64 table, FP64 sums in a fixed
+// order): E_r += q G_r, E_z += +-q G_z over every bin, as the contraction
+__global__ void __launch_bounds__(kSurBlock) k_sur_spot(const ScState *sc, ScTables t, const SurDev *sd,
+                                                        double2 *spot, uint32_t nr, uint32_t nz) {
+  if (!sd->active) return;
+  __shared__ double rx[kSurBlock], rz[kSurBlock];
+  uint32_t zp, rp;
+  spot_point(blockIdx.x, nr, nz, sc->n_solves, zp, rp);
+  const uint32_t nb = nr * nz;
+  const double2 *g = (const double2 *)t.fld1 + (size_t)rp * nb;
+  double ax = 0.0, az = 0.0;
+  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
+    const unsigned long long v = t.bin_fx[k];
+    if (!v) continue;
+    const double q = (double)(long long)v * kBinInvScale;
+    const uint32_t rs = k % nr, zs = k / nr;
+    const bool above = zs >= zp;
+    const uint32_t dz = above ? zs - zp : zp - zs - 1;
+    const double2 e = g[(size_t)rs * nz + dz];
+    ax = fma(q, e.x, ax);
+    az = above ? fma(-q, e.y, az) : fma(q, e.y, az);
+  }
+  rx[threadIdx.x] = ax;
+  rz[threadIdx.x] = az;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      rx[threadIdx.x] += rx[threadIdx.x + off];
+      rz[threadIdx.x] += rz[threadIdx.x + off];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) spot[blockIdx.x] = make_double2(rx[0], rz[0]);
+}
+
+// every block forms the residual over the samples (same values, same order)
+// and, when it is within tolerance, writes its share of the field table
+__global__ void __launch_bounds__(kSurBlock) k_sur_apply(ScState *sc, ScTables t, SurDev *sd,
+                                                         const __nv_bfloat16 *out, const double2 *spot, uint32_t nr,
+                                                         uint32_t nz, uint32_t n_samples, double tol) {
+  if (!sd->active) return;
+  __shared__ double rn[kSurBlock], rd[kSurBlock];
+  const double scale = sd->scale;
+  const uint32_t nb = nr * nz, base = nr + 1 + nz;
+  double num = 0.0, den = 0.0;
+  for (uint32_t k = threadIdx.x; k < n_samples; k += blockDim.x) {
+    uint32_t zp, rp;
+    spot_point(base + k, nr, nz, sc->n_solves, zp, rp);
+    const double er = (double)__bfloat162float(out[zp * nr + rp]) * scale;
+    const double ez = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale;
+    const double2 e = spot[base + k];
+    num += (er - e.x) * (er - e.x) + (ez - e.y) * (ez - e.y);
+    den += e.x * e.x + e.y * e.y;
+  }
+  rn[threadIdx.x] = num;
+  rd[threadIdx.x] = den;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      rn[threadIdx.x] += rn[threadIdx.x + off];
+      rd[threadIdx.x] += rd[threadIdx.x + off];
+    }
+    __syncthreads();
+  }
+  const double res = rd[0] > 0.0 ? sqrt(rn[0] / rd[0]) : (rn[0] > 0.0 ? 1.0 : 0.0);
+  const bool ok = res <= tol;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sd->residual = res;
+    if (ok) sd->n_accepted += 1;
+    else sd->n_rejected += 1;
+    sc->sur_accepted = ok;
+  }
+  if (!ok) return;
+  const uint32_t nrow = nr + 1;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (nz + 1) * nrow) return;
+  const uint32_t zp = p / nrow, rp = p % nrow;
+  double2 e;
+  if (zp < nz && rp < nr) {
+    e.x = (double)__bfloat162float(out[zp * nr + rp]) * scale;
+    e.y = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale;
+  } else {
+    e = spot[zp == nz ? rp : nr + 1 + zp];
+  }
+  ((double2 *)t.fld2)[p] = e;
+}
+
+}  // namespace
+
+SurNet::~SurNet() {
+  for (void *p : w) cudaFree(p);
+  for (float *p : b) cudaFree(p);
+  for (void *p : act) cudaFree(p);
+  if (x) cudaFree(x);
+  if (spot) cudaFree(spot);
+  if (d) cudaFree(d);
+}
+
+void sur_solve(const DevBeam &bm, ScState *sc, const ScTables &t, const ScKickArgs &a, const SurNet &n,
+               cudaStream_t st) {
+  SurDev *sd = (SurDev *)n.d;
+  k_sur_input<<<1, 1024, 0, st>>>(sc, t, sd, (__nv_bfloat16 *)n.x, n.nr, n.nz, n.out_scale, bm.n,
+                                  a.current * a.frac / bm.mass);
+  const void *cur = n.x;
+  for (size_t l = 0; l < n.arch.size(); ++l) {
+    const int32_t *dims = n.dims.data() + 7 * l;
+    const void *skip = n.skip[l] >= 0 ? n.act[n.skip[l]] : nullptr;
+    nn_conv_forward(dims, cur, n.w[l], n.b[l], n.arch[l][4], skip, n.act[l], st);
+    if ((int)l == n.gmean_after) nn_gmean_forward(n.act[l], dims[2], n.hw[l], st);
+    cur = n.act[l];
+  }
+  const uint32_t npts = n.nr + 1 + n.nz + n.n_samples;
+  k_sur_spot<<<npts, kSurBlock, 0, st>>>(sc, t, sd, (double2 *)n.spot, n.nr, n.nz);
+  const uint32_t nf = (n.nz + 1) * (n.nr + 1);
+  k_sur_apply<<<(nf + kSurBlock - 1) / kSurBlock, kSurBlock, 0, st>>>(
+      sc, t, sd, (const __nv_bfloat16 *)n.act.back(), (const double2 *)n.spot, n.nr, n.nz, n.n_samples, n.tol);
+  note_launch(3);
+}
+
+int sur_build(SurNet &n, int n_layers, const int32_t *arch, int gmean_after, const int32_t *skip,
+              const uint16_t *const *weights, const float *const *biases, uint32_t nr, uint32_t nz, double out_scale,
+              double tol, uint32_t n_samples, std::string &err) {
+  if (n_layers < 1 || n_layers > 64 || !arch || !skip || !weights || !biases) { err = "bad arguments"; return 1; }
+  if (nr < 2 || nz < 2 || nr > 256 || nz > 512 || n_samples < 1 || n_samples > 4096 || !(tol >= 0.0) ||
+      !(out_scale > 0.0)) {
+    err = "bad mesh, sample count, tolerance or output scale";
+    return 1;
+  }
+  n.nr = nr; n.nz = nz; n.out_scale = out_scale; n.tol = tol; n.n_samples = n_samples;
+  n.gmean_after = gmean_after;
+  uint32_t h = nz, wd = nr, c = 2;
+  std::vector<uint32_t> hs, ws, cs;
+  for (int l = 0; l < n_layers; ++l) {
+    const int32_t *a5 = arch + 5 * l;
+    const int ci = a5[0], co = a5[1], s = a5[2], u = a5[3];
+    if ((uint32_t)ci != c || co < 1 || (s != 1 && s != 2) || (u != 1 && u != 2) || ci > 512) {
+      err = "layer " + std::to_string(l) + ": channels or stride/upsampling do not chain";
+      return 1;
+    }
+    n.arch.push_back({a5[0], a5[1], a5[2], a5[3], a5[4]});
+    n.dims.insert(n.dims.end(), {1, ci, co, (int32_t)h, (int32_t)wd, s, u});
+    h = (h * u - 1) / s + 1;
+    wd = (wd * u - 1) / s + 1;
+    c = co;
+    hs.push_back(h); ws.push_back(wd); cs.push_back(c);
+    n.hw.push_back((int)(h * wd));
+    if (skip[l] >= 0 && (skip[l] >= l || hs[skip[l]] != h || ws[skip[l]] != wd || cs[skip[l]] != c)) {
+      err = "layer " + std::to_string(l) + ": skip source does not match";
+      return 1;
+    }
+    n.skip.push_back(skip[l]);
+  }
+  if (c != 2 || h != nz || wd != nr) { err = "the last layer must give 2 channels on the nz x nr mesh"; return 1; }
+  if (gmean_after >= n_layers) { err = "plane-mean layer out of range"; return 1; }
+  auto dm = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess; };
+  for (int l = 0; l < n_layers; ++l) {
+    const size_t nw = (size_t)n.arch[l][1] * n.arch[l][0] * 9, nb = n.arch[l][1];
+    void *wp = nullptr, *bp = nullptr, *ap = nullptr;
+    if (!dm(&wp, nw * 2) || !dm(&bp, nb * 4) || !dm(&ap, (size_t)cs[l] * hs[l] * ws[l] * 2)) {
+      if (wp) cudaFree(wp);
+      if (bp) cudaFree(bp);
+      err = "device allocation failed";
+      return 2;
+    }
+    n.w.push_back(wp);
+    n.b.push_back((float *)bp);
+    n.act.push_back(ap);
+    if (cudaMemcpy(wp, weights[l], nw * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(bp, biases[l], nb * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+      err = "weight upload failed";
+      return 2;
+    }
+  }
+  if (!dm(&n.x, (size_t)2 * nr * nz * 2) || !dm(&n.spot, (size_t)(nr + 1 + nz + n_samples) * 16) ||
+      !dm(&n.d, sizeof(SurDev)) || cudaMemset(n.d, 0, sizeof(SurDev)) != cudaSuccess) {
+    err = "device allocation failed";
+    return 2;
+  }
+  return 0;
+}
+
+int sur_read(const SurNet &n, double *accepted, double *rejected, double *residual) {
+  SurDev h;
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(&h, n.d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return 1;
+  if (accepted) *accepted = h.n_accepted;
+  if (rejected) *rejected = h.n_rejected;
+  if (residual) *residual = h.residual;
+  return 0;
+}
+
+}  // namespace hps

@@ -196,6 +196,10 @@ hps_status hps_scheff_destroy(hps_scheff_t s);
  * (the element map before the kick could not certify them) */
 hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
 hps_status hps_scheff_get(hps_scheff_t s, int param, double *value);
+/* the solver's tables after its last kick (no reference counterpart): charge
+ * (nr*nz), field ((nz+1)*(nr+1) pairs) of the FP32 (fp32 != 0) or FP64 tables,
+ * mesh = {nr, nz, dr, dz, beta, num_on_mesh, remesh} */
+hps_status hps_scheff_snapshot(hps_scheff_t s, int fp32, double *bins, double *field, double *mesh);
 /* SetMeshSize, space_charge.cpp:61-73 */
 hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz);
 /* The SCHEFF table stage on its own: Green's table (UpdateFldTbl1Kernel via
@@ -279,6 +283,53 @@ hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *
 hps_status hps_batch_destroy(hps_batch_t batch);
 hps_status hps_batch_simulate(hps_batch_t batch, int32_t start, int32_t end);
 hps_status hps_batch_last_time_ms(hps_batch_t batch, double *ms);
+
+/* ---- SCHEFF field surrogate: network layers (no reference counterpart).
+ * Device pointers; tensors [batch][channel][z][r]; x, w, y BF16, bias, dy,
+ * dz, dx, dw, db FP32.  dims = {batch, c_in, c_out, h_in, w_in, stride (1|2),
+ * up (1|2: nearest 2x upsampling of the input before the 3x3 convolution)};
+ * output h = (h_in*up - 1)/stride + 1; c_in <= 512.  stream: a cudaStream_t
+ * or NULL.  y = ReLU(conv + bias) (relu != 0) rounded to BF16, plus skip
+ * (same shape as y, BF16, rounded again) when skip != NULL. */
+hps_status hps_nn_conv_forward(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,
+                               const void *skip, void *y, void *stream);
+/* dz = dy masked by the ReLU of y; dw, db = weight and bias gradients; dx
+ * (may be NULL) = input gradient */
+hps_status hps_nn_conv_backward(const int32_t dims[7], const void *x, const void *w, const void *y, int relu,
+                                const float *dy, float *dz, float *dx, float *dw, float *db, void *stream);
+/* y[b][c] += mean of the plane (BF16, in place) and its backward on FP32 */
+hps_status hps_nn_gmean_forward(void *y, int32_t planes, int32_t hw, void *stream);
+hps_status hps_nn_gmean_backward(float *d, int32_t planes, int32_t hw, void *stream);
+/* squared error: per-block partial sums of wt (pred - target)^2 and dpred =
+ * 2 wt (pred - target) / n, wt = weight[i / per_sample] (weight may be NULL) */
+hps_status hps_nn_mse(const void *pred, const float *target, int64_t n, const float *weight, int64_t per_sample,
+                      float *dpred, float *partial, int32_t nblocks, void *stream);
+/* y = a + b (bf16 != 0: BF16 tensors, else FP32) */
+hps_status hps_nn_add(const void *a, const void *b, void *y, int64_t n, int bf16, void *stream);
+/* Adam on FP32 weights (step >= 1), refreshing their BF16 copy when w_bf16 != NULL */
+hps_status hps_nn_adam(float *w, void *w_bf16, const float *g, float *m, float *v, int64_t n, float lr, float b1,
+                       float b2, float eps, int32_t step, void *stream);
+/* FP32 <-> BF16 (to_bf16: 1 FP32 -> BF16, 0 BF16 -> FP32) */
+hps_status hps_nn_convert(const void *src, void *dst, int64_t n, int to_bf16, void *stream);
+
+/* Attach a trained field network to a solver (FP64 beams; FP32 beams keep
+ * the plain path).  Host arrays: arch[5*l..] = {c_in, c_out, stride, up,
+ * relu} per layer (first c_in = 2, last c_out = 2, output on nz x nr);
+ * gmean_after = the layer whose output gets its plane mean added (-1 none);
+ * skip[l] = the earlier layer whose output layer l adds (-1 none);
+ * weights[l] = BF16 bits [c_out][c_in][3][3], biases[l] = FP32 [c_out].
+ * Input channels: charge * nr*nz / total and log(dz*gamma/dr); the field is
+ * output * c1 * total / (out_scale * dr * dz*gamma).  Each kick that
+ * remeshes on an nr x nz mesh evaluates it, solves the plain sum at the last
+ * row and column and at n_samples interior points, and keeps the network's
+ * field when its relative residual there is <= tol, else the plain
+ * contraction runs.  Replaces an attached network. */
+hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int32_t *arch, int32_t gmean_after,
+                                    const int32_t *skip, const uint16_t *const *weights, const float *const *biases,
+                                    uint32_t nr, uint32_t nz, double out_scale, double tol, uint32_t n_samples);
+hps_status hps_scheff_clear_surrogate(hps_scheff_t s);
+/* kicks whose field was accepted / fell back, and the last residual */
+hps_status hps_scheff_surrogate_stats(hps_scheff_t s, double *accepted, double *rejected, double *residual);
 
 #ifdef __cplusplus
 }

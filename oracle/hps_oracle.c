@@ -1666,6 +1666,8 @@ static int visit(orc_sim *s, uint32_t i) {
 int orc_sim_simulate(orc_sim *s, int start, int end) {
   int start_index = start < 0 ? 0 : start;
   int end_index = end < 0 ? (int)s->nelem - 1 : end;
+  /* prev_end_element_index_ is an int (simulation_engine.h:66) holding
+   * UINT_MAX, i.e. -1: the first call does not reset */
   if (start_index < s->prev_end) orc_sim_reset(s);
   s->prev_end = end_index;
   for (int i = 0; i <= end_index; ++i) {

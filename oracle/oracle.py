@@ -220,19 +220,27 @@ class Sim:
 
 
 def run(elems, num, spch_args=None, spch_set=None, seed=12345, twiss=None, w0=0.75, phi0=0.0,
-        freq=201.25, start=-1, end=-1):
-    """Build a waterbag beam, run the lattice, return (monitor, coords)."""
+        freq=201.25, start=-1, end=-1, late=False):
+    """Build a waterbag beam, run the lattice, return (monitor, coords).
+    late: the beam is configured after the simulator is created."""
     from hpsim_gb300 import lattices as L
     types, params, _ = L.lattice_arrays(elems)
     b = Beam(num)
-    b.set_waterbag(twiss or L.waterbag_twiss(), phi0, w0, freq, seed)
-    b.set_ref_w(w0)
-    b.set_ref_phi(phi0)
+
+    def configure():
+        b.set_waterbag(twiss or L.waterbag_twiss(), phi0, w0, freq, seed)
+        b.set_ref_w(w0)
+        b.set_ref_phi(phi0)
+
+    if not late:
+        configure()
     sp = None
     if spch_args is not None:
         sp = Scheff(*spch_args)
         if spch_set:
             sp.set(**spch_set)
     sim = Sim(b, types, params, sp)
+    if late:
+        configure()
     mon = sim.simulate(start, end).copy()
     return mon, b.coords()

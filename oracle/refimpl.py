@@ -67,26 +67,32 @@ def _up(a):
 
 
 def run(elems, num, spch=None, seed=12345, twiss=None, w0=0.75, phi0=0.0, freq=201.25,
-        dist=None, mass=939.294, charge=-1.0, current=0.015):
+        dist=None, mass=939.294, charge=-1.0, current=0.015, late=False):
     """Run the reference on a waterbag (or given) beam; return (monitor, coords).
 
     spch: None or dict(nr, nz, interval, adj_bunch, remesh_threshold,
-    adj_bunch_cutoff_w, mesh_size_cutoff_w)."""
+    adj_bunch_cutoff_w, mesh_size_cutoff_w).  late: the beam's distribution
+    and reference energy / phase are set after the simulator is created."""
     from hpsim_gb300 import lattices as L
     lb = lib()
     b = lb.ref_beam_create(int(num), mass, charge, current)
-    if dist is None:
-        tw = np.ascontiguousarray(twiss or L.waterbag_twiss(), dtype=np.float64)
-        lb.ref_beam_set_waterbag(b, _dp(tw), phi0, w0, freq, int(seed))
-    else:
-        arrs = [np.ascontiguousarray(dist[k], dtype=np.float64) for k in ("x", "xp", "y", "yp", "phi", "w")]
-        lo = np.ascontiguousarray(dist["loss"], dtype=np.uint32) if "loss" in dist else None
-        ll = np.ascontiguousarray(dist["lloss"], dtype=np.uint32) if "lloss" in dist else None
-        lb.ref_beam_set_distribution(b, *[_dp(a) for a in arrs], _up(lo) if lo is not None else None,
-                                     _up(ll) if ll is not None else None)
-        lb.ref_beam_set_frequency(b, freq)
-    lb.ref_beam_set_ref_w(b, w0)
-    lb.ref_beam_set_ref_phi(b, phi0)
+
+    def configure():
+        if dist is None:
+            tw = np.ascontiguousarray(twiss or L.waterbag_twiss(), dtype=np.float64)
+            lb.ref_beam_set_waterbag(b, _dp(tw), phi0, w0, freq, int(seed))
+        else:
+            arrs = [np.ascontiguousarray(dist[k], dtype=np.float64) for k in ("x", "xp", "y", "yp", "phi", "w")]
+            lo = np.ascontiguousarray(dist["loss"], dtype=np.uint32) if "loss" in dist else None
+            ll = np.ascontiguousarray(dist["lloss"], dtype=np.uint32) if "lloss" in dist else None
+            lb.ref_beam_set_distribution(b, *[_dp(a) for a in arrs], _up(lo) if lo is not None else None,
+                                         _up(ll) if ll is not None else None)
+            lb.ref_beam_set_frequency(b, freq)
+        lb.ref_beam_set_ref_w(b, w0)
+        lb.ref_beam_set_ref_phi(b, phi0)
+
+    if not late:
+        configure()
     bl = lb.ref_beamline_create()
     for t, name, p in elems:
         pp = np.ascontiguousarray(p, dtype=np.float64)
@@ -100,6 +106,8 @@ def run(elems, num, spch=None, seed=12345, twiss=None, w0=0.75, phi0=0.0, freq=2
         sp = lb.ref_scheff_create(s["nr"], s["nz"], s["adj_bunch"], s["interval"],
                                   s["remesh_threshold"], s["adj_bunch_cutoff_w"], s["mesh_size_cutoff_w"])
     sim = lb.ref_sim_create(b, bl, sp)
+    if late:
+        configure()
     mon = np.zeros((len(elems), NMON))
     rc = lb.ref_sim_simulate(sim, b, -1, -1, _dp(mon))
     out = {k: np.zeros(num) for k in ("x", "xp", "y", "yp", "phi", "w")}

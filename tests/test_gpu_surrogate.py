@@ -1,0 +1,185 @@
+"""The SCHEFF field surrogate's kernels (csrc/nn.cu) against the numpy
+oracle (oracle/nn_oracle.py) layer by layer, Adam against its formula, and
+training on plain-SCHEFF snapshots reducing the field error."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import nn_oracle as N
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+@pytest.mark.parametrize("layer", range(10))
+def test_layer_forward_and_backward_match_oracle(layer):
+    from hpsim_gb300 import surrogate as S
+    from hpsim_gb300._capi import call
+    ci, co, stride, up, relu = S.ARCH[layer]
+    B, H, W = 2, 16, 8
+    rng = np.random.default_rng(layer)
+    dims = np.array([B, ci, co, H, W, stride, up], np.int32)
+    x = N.bf16_round(rng.normal(size=(B, ci, H, W)).astype(np.float32))
+    w = N.bf16_round((rng.normal(size=(co, ci, 3, 3)) / np.sqrt(9 * ci)).astype(np.float32))
+    b = rng.normal(size=co).astype(np.float32) * 0.1
+    ho, wo = (H * up - 1) // stride + 1, (W * up - 1) // stride + 1
+    X = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
+    Wt = torch.tensor(w, dtype=torch.bfloat16, device="cuda")
+    Bt = torch.tensor(b, device="cuda")
+    Y = torch.empty((B, co, ho, wo), dtype=torch.bfloat16, device="cuda")
+    dptr = dims.ctypes.data_as(C.POINTER(C.c_int))
+    call("hps_nn_conv_forward", dptr, p(X), p(Wt), p(Bt), relu, None, p(Y), None)
+    torch.cuda.synchronize()
+    y_gpu = Y.float().cpu().numpy()
+    _, y_ref = N.conv_forward(x, w, b, stride, up, relu)
+    # one BF16 rounding of an FP32 sum against the FP64 sum
+    assert np.all(np.abs(y_gpu - y_ref) <= 2.0 ** -7 * np.abs(y_ref) + 1e-6)
+    # the fused skip addition: the same BF16 activation plus skip, rounded again
+    sk = N.bf16_round(rng.normal(size=y_gpu.shape).astype(np.float32))
+    SK = torch.tensor(sk, dtype=torch.bfloat16, device="cuda")
+    Y2 = torch.empty_like(Y)
+    call("hps_nn_conv_forward", dptr, p(X), p(Wt), p(Bt), relu, p(SK), p(Y2), None)
+    torch.cuda.synchronize()
+    assert np.array_equal(Y2.float().cpu().numpy(), N.bf16_round(y_gpu + sk))
+    dy = rng.normal(size=y_gpu.shape).astype(np.float32)
+    DY = torch.tensor(dy, device="cuda")
+    DZ = torch.empty_like(DY)
+    DX = torch.empty((B, ci, H, W), device="cuda")
+    DW = torch.empty((co, ci, 3, 3), device="cuda")
+    DB = torch.empty(co, device="cuda")
+    call("hps_nn_conv_backward", dptr, p(X), p(Wt), p(Y), relu, p(DY), p(DZ), p(DX), p(DW), p(DB), None)
+    torch.cuda.synchronize()
+    dz, dx, dw, db = N.conv_backward(x, w, y_gpu, relu, dy, stride, up)  # with the kernel's own activations
+    assert np.array_equal(DZ.cpu().numpy(), dz.astype(np.float32))
+    for got, ref in ((DX, dx), (DW, dw), (DB, db)):
+        g = got.cpu().numpy()
+        assert np.allclose(g, ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
+
+
+def test_gmean_and_adam_match_formulas():
+    from hpsim_gb300._capi import call
+    rng = np.random.default_rng(9)
+    y = N.bf16_round(rng.normal(size=(2, 3, 4, 8)).astype(np.float32))
+    Y = torch.tensor(y, dtype=torch.bfloat16, device="cuda")
+    call("hps_nn_gmean_forward", p(Y), 6, 32, None)
+    d = rng.normal(size=(2, 3, 4, 8)).astype(np.float32)
+    D = torch.tensor(d, device="cuda")
+    call("hps_nn_gmean_backward", p(D), 6, 32, None)
+    torch.cuda.synchronize()
+    assert np.allclose(Y.float().cpu().numpy(), N.gmean_forward(y), rtol=2 ** -7, atol=1e-6)
+    assert np.allclose(D.cpu().numpy(), N.gmean_backward(d), rtol=1e-5, atol=1e-6)
+    n = 1000
+    w, g, m, v = (rng.normal(size=n).astype(np.float32) for _ in range(4))
+    v = np.abs(v)
+    T = [torch.tensor(a, device="cuda") for a in (w, g, m, v)]
+    call("hps_nn_adam", p(T[0]), None, p(T[1]), p(T[2]), p(T[3]), n, 1e-3, 0.9, 0.999, 1e-8, 3, None)
+    torch.cuda.synchronize()
+    m2 = 0.9 * m + 0.1 * g
+    v2 = 0.999 * v + 0.001 * g * g
+    w2 = w - 1e-3 * (m2 / (1 - 0.9 ** 3)) / (np.sqrt(v2 / (1 - 0.999 ** 3)) + 1e-8)
+    assert np.allclose(T[0].cpu().numpy(), w2, rtol=1e-5, atol=1e-7)
+
+
+def test_network_gradients_match_oracle():
+    """Network.forward / backward (skip additions, plane-mean broadcast)
+    against the FP64 oracle composition with the same BF16 weights: the
+    prediction within 3% in norm (BF16 activations), and, from the kernels'
+    own activations, every layer's gradients within 0.1% (FP32 sums)."""
+    from hpsim_gb300 import surrogate as S
+    net = S.Network(seed=3)
+    rng = np.random.default_rng(3)
+    x = N.bf16_round(rng.normal(size=(2, 2, 32, 16)).astype(np.float32))
+    fwd = net.forward(torch.tensor(x, dtype=torch.bfloat16, device="cuda"))
+    g = rng.normal(size=tuple(fwd[2][-1].shape)).astype(np.float32)
+    dws, dbs = net.backward(fwd, torch.tensor(g, device="cuda"))
+    torch.cuda.synchronize()
+    ws = [w.float().cpu().numpy().astype(np.float64) for w in net.wb]
+    bs = [b.cpu().numpy().astype(np.float64) for b in net.b]
+    rf = N.net_forward(x, ws, bs, S.ARCH, S.GMEAN_AFTER, S.SKIP)
+    pred = fwd[2][-1].float().cpu().numpy()
+    assert np.linalg.norm(pred - rf[2][-1]) <= 0.03 * np.linalg.norm(rf[2][-1])
+    own = tuple([t.float().cpu().numpy().astype(np.float64) for t in part] for part in fwd)
+    rdw, rdb = N.net_backward(own, ws, S.ARCH, S.GMEAN_AFTER, S.SKIP, g)
+    for l in range(len(S.ARCH)):
+        for got, ref in ((dws[l], rdw[l]), (dbs[l], rdb[l])):
+            err = np.linalg.norm(got.cpu().numpy() - ref)
+            assert err <= 1e-3 * np.linalg.norm(ref) + 1e-12, (l, err, np.linalg.norm(ref))
+
+
+def test_training_on_scheff_snapshots_reduces_the_field_error():
+    from hpsim_gb300 import surrogate as S
+    xs, ys = S.snapshots(n_runs=6, num=8192, seed=4)
+    assert len(xs) > 100
+    net = S.Network(seed=1)
+    before = np.median(S.relative_error(net, xs, ys))
+    hist = S.train(net, xs, ys, epochs=12, batch=16, lr=2e-3)
+    after = np.median(S.relative_error(net, xs, ys))
+    assert hist[-1] < 0.2 * hist[0]
+    assert after < 0.5 * before and after < 0.3, (before, after)
+
+
+def _zero_state():
+    from hpsim_gb300 import surrogate as S
+    st = {f"w{i}": np.zeros((co, ci, 3, 3), np.float32) for i, (ci, co, *_) in enumerate(S.ARCH)}
+    st.update({f"b{i}": np.zeros(co, np.float32) for i, (_, co, *_) in enumerate(S.ARCH)})
+    st["out_scale"] = 1.0
+    return st
+
+
+def _fodo_sim(n, state=None, tol=0.5, graph=True):
+    from hpsim_gb300 import HPSim, lattices as L
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=n, precision="fp64")
+    beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 4242)
+    beam.set_ref_w(0.75)
+    sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
+    sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()), sc)
+    sim.use_graph(graph)
+    if state is not None:
+        sc.set_surrogate(state, tol=tol)
+    return beam, sc, sim
+
+
+def test_rejected_surrogate_leaves_the_plain_results_bit_exact():
+    """A network whose field fails the spot check on every kick (all zeros)
+    falls back each time: monitors and coordinates equal the plain run's."""
+    runs = []
+    for state in (None, _zero_state()):
+        beam, sc, sim = _fodo_sim(16384, state)
+        sim.enable_monitor(True)
+        solves0 = sc.get_counter("solves")
+        sim.simulate()
+        runs.append((sim.monitor.copy(), [beam._coord(k) for k in ("x", "xp", "y", "yp", "phi", "w")],
+                     sc.get_counter("solves") - solves0, sc.surrogate_stats() if state is not None else None))
+    (m0, c0, n0, _), (m1, c1, n1, st) = runs
+    assert n0 == n1 > 0
+    assert st[0] == 0 and st[1] == n1 and st[2] == 1.0
+    assert np.array_equal(m0, m1)
+    for a, b in zip(c0, c1):
+        assert np.array_equal(a, b)
+
+
+def test_accepted_surrogate_field_has_the_exact_boundary():
+    """With every field accepted, the table holds the network's interior
+    (zero here) and the plain sum on the last row and column, equal to the
+    plain contraction's values there."""
+    from hpsim_gb300._capi import call
+    fields = []
+    for state in (None, _zero_state()):
+        beam, sc, sim = _fodo_sim(16384, state, tol=1e30, graph=False)
+        sim.simulate(0, 1)  # buncher, then the first drift's kick
+        bins, field, mesh = np.empty(32 * 128), np.empty(129 * 33 * 2), np.empty(7)
+        call("hps_scheff_snapshot", sc.handle, 0, bins.ctypes.data_as(C.POINTER(C.c_double)),
+             field.ctypes.data_as(C.POINTER(C.c_double)), mesh.ctypes.data_as(C.POINTER(C.c_double)))
+        assert mesh[6] == 1 and mesh[0] == 32 and mesh[1] == 128
+        fields.append(field.reshape(129, 33, 2))
+        if state is not None:
+            assert sc.surrogate_stats()[:2] == (1, 0)
+    plain, sur = fields
+    assert np.all(sur[:128, :32] == 0.0)
+    for got, ref in ((sur[128, :], plain[128, :]), (sur[:, 32], plain[:, 32])):
+        assert np.allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())

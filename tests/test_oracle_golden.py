@@ -112,3 +112,23 @@ def test_field_from_charge_table(oracle):
     _, fld1, fld2 = s.tables()
     assert np.allclose(fld1, z["fld1"], rtol=1e-12, atol=1e-13 * np.abs(z["fld1"]).max())
     assert np.allclose(fld2, z["fld2"], rtol=1e-11, atol=1e-13 * np.abs(z["fld2"]).max())
+
+
+def test_first_simulate_keeps_the_engine_state_of_its_creation(oracle):
+    """SimulationEngine's previous end index is an int holding UINT_MAX (-1),
+    so its first Simulate call does not reset: a beam configured after the
+    simulator was created keeps the creation-time design energy and
+    wavelength (zero frequency: the phase does not advance through the first
+    quad), and the reference build does the same.  (Its RF gaps then run
+    with a design energy of zero, where the reference's arithmetic gives
+    non-finite phases and loses every particle; that degenerate input is not
+    restated.)"""
+    from hpsim_gb300 import lattices as L
+    from oracle import refimpl as R
+    elems = L.dtl_like(n_gaps=2, seed=3)
+    m0, _ = oracle.run(elems, 500, seed=5)
+    m1, _ = oracle.run(elems, 500, seed=5, late=True)
+    assert m0[0, 18] != 0.0 and m1[0, 18] == 0.0  # particle 0's phase after the first quad
+    if R.available():
+        mr, _ = R.run(elems, 500, seed=5, late=True)
+        assert mr[0, 18] == 0.0 and np.allclose(mr[0], m1[0], rtol=1e-10, atol=0.0)
