@@ -32,6 +32,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-element steps/s"
 N_PART = 1 << 20
 GAPS = 165
+SURROGATE_NET = os.path.join(ROOT, "hpsim_gb300", "data", "scheff_surrogate_32x128.npz")
 
 
 def parse():
@@ -51,6 +52,10 @@ def parse():
                         "particles through 1024 CCL gaps, SCHEFF 64x256; batched: 256 beams of the "
                         "small-FODO topology in one graph launch")
     p.add_argument("--beams", type=int, default=256)
+    p.add_argument("--surrogate", nargs="?", const=SURROGATE_NET, default=None,
+                   help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
+                        "(a network file; default the shipped 32x128 network), and report both")
+    p.add_argument("--surrogate-tol", type=float, default=0.02)
     return p.parse_args()
 
 
@@ -404,11 +409,42 @@ def main():
         sim.simulate()
         return sim.last_time_ms()
 
+    def monitored():
+        sim.enable_monitor(True)
+        step()
+        mon = sim.monitor.copy()
+        sim.enable_monitor(False)
+        return mon
+
+    sur = None
+    if args.surrogate:
+        if args.workload != "small_fodo":
+            raise SystemExit("--surrogate: the field surrogate is trained for the small_fodo mesh (FP64 beams)")
+        # the plain path first, timed the same way, and its moments per element
+        for _ in range(args.warmup):
+            flush.zero_()
+            step()
+        barrier()
+        plain_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            plain_ms.append(step())
+        plain_value, _ = job_value(sum(plain_ms) / len(plain_ms) / 1000.0, ws, args.particles, n_elem,
+                                   device=f"cuda:{local}")
+        mon_plain = monitored()
+        net = np.load(args.surrogate)
+        sc.set_surrogate(net, tol=args.surrogate_tol)
+        sur = {"network": os.path.relpath(args.surrogate, ROOT), "tol": args.surrogate_tol,
+               "plain_value": plain_value, "plain_ms_per_step": sum(plain_ms) / len(plain_ms),
+               "network_val_field_err_median": float(net["meta_val_median"]) if "meta_val_median" in net else None}
+
     for _ in range(args.warmup):
         flush.zero_()
         step()
     launches0 = HPSim.kernel_launch_count()
     sweeps0 = sc.get_counter("stat_sweeps")
+    sur0 = sc.surrogate_stats() if sur else None
     barrier()
     dev_ms = []
     wall0 = time.perf_counter()
@@ -423,6 +459,15 @@ def main():
     stat_sweeps = (sc.get_counter("stat_sweeps") - sweeps0) / args.steps
     value, t_step = job_value(sum(dev_ms) / len(dev_ms) / 1000.0, ws, args.particles, n_elem,
                               device=f"cuda:{local}")
+    if sur:
+        acc, rej, _ = sc.surrogate_stats()
+        mon_sur = monitored()
+        rel = lambda i: float(np.max(np.abs(mon_sur[:, i] / mon_plain[:, i] - 1.0)))  # noqa: E731
+        sur.update({"gain": value / sur["plain_value"],
+                    "accepted_per_step": (acc - sur0[0]) / args.steps,
+                    "fallbacks_per_step": (rej - sur0[1]) / args.steps,
+                    "emittance_rel_err_max": {"x": rel(6), "y": rel(11), "z": rel(16)},
+                    "transmission_equal": bool(np.array_equal(mon_sur[:, 0], mon_plain[:, 0]))})
 
     # per-phase breakdown of one more (untimed) step: dominant kernel + roofline
     sim.profile(True)
@@ -506,6 +551,8 @@ def main():
         "gpu_launches": int(launches),
         "clocks": ck,
     }
+    if sur:
+        line["surrogate"] = sur
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -42,13 +42,6 @@ __device__ inline float in_at(const __nv_bfloat16 *p, int Y, int X, int Hi, int 
   return bf(p[(Y / up) * Wi + X / up]);
 }
 
-// in_at with the upsampling factor known at compile time
-template <int U>
-__device__ inline float in_at_u(const __nv_bfloat16 *p, int Y, int X, int Hi, int Wi) {
-  if (Y < 0 || X < 0 || Y >= Hi * U || X >= Wi * U) return 0.0f;
-  return bf(p[(Y / U) * Wi + X / U]);
-}
-
 // out[b][co][oy][ox] = bias[co] + sum_ci sum_ky,kx w[co][ci][ky][kx] in_up[b][ci][oy*S+ky-1][ox*S+kx-1],
 // then ReLU when relu != 0, then (skip != null) BF16-rounded and added to
 // skip[b][co][oy][ox].
@@ -77,37 +70,86 @@ __global__ void __launch_bounds__(kNnBlock) k_conv_fwd(ConvShape s, int split, i
   float *ws = conv_smem;                                // [cpr][9][kCoTile]
   float *part = conv_smem + (size_t)cpr * 9 * kCoTile;  // [split][kCoTile][P]
   float *csum = part + (size_t)split * kCoTile * P;     // [kCoTile][P]: this CTA's sums
+  const int slice = threadIdx.x / P, lp = threadIdx.x % P;
+  const int npix = s.Ho * s.Wo;
+  const int pix = (blockIdx.x / cl) * P + lp;
+  const bool live = pix < npix;
+  const int Y0 = (live ? pix / s.Wo : 0) * S - 1, X0 = (live ? pix % s.Wo : 0) * S - 1;
+  const int plane = s.Hi * s.Wi;
+  const __nv_bfloat16 *xb = x + ((size_t)b * s.Ci + ci_lo) * plane;
+  // the window's offsets in an input plane and which taps fall inside it
+  // (the same for every channel)
+  int off[9];
+  unsigned inside = 0;
+#pragma unroll
+  for (int t = 0; t < 9; ++t) {
+    const int Y = Y0 + t / 3, X = X0 + t % 3;
+    const bool in = live && Y >= 0 && X >= 0 && Y < s.Hi * U && X < s.Wi * U;
+    off[t] = in ? (Y / U) * s.Wi + X / U : 0;
+    inside |= (unsigned)in << t;
+  }
+  // this thread's input windows, kPre channels at a time; the first ones are
+  // loaded before the weights are staged, so both global reads overlap
+  constexpr int kPre = 2;
+  static_assert(kCoTile == 8, "the weights of one tap are read as two float4");
+  float v[kPre][9];
+  auto load = [&](int c0) {
+#pragma unroll
+    for (int j = 0; j < kPre; ++j) {
+      const int c = c0 + j * split;
+      const __nv_bfloat16 *p = xb + (size_t)max(0, min(c, nci - 1)) * plane;
+      const unsigned m = c < nci ? inside : 0u;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) v[j][t] = (m >> t) & 1u ? bf(p[off[t]]) : 0.0f;
+    }
+  };
+  load(slice);
   if (nco < kCoTile)
     for (int i = threadIdx.x; i < nci * 9 * kCoTile; i += blockDim.x) ws[i] = 0.0f;
   __syncthreads();
   const int run = nci * 9;  // each output channel's weights of this range are contiguous
-  for (int j = threadIdx.x; j < nco * run; j += blockDim.x) {
-    const int k = j / run, r = j - k * run;
-    ws[r * kCoTile + k] = bf(w[((size_t)(co0 + k) * s.Ci + ci_lo) * 9 + r]);
+  const __nv_bfloat16 *w0 = w + ((size_t)co0 * s.Ci + ci_lo) * 9;
+  if ((run & 7) == 0 && ((s.Ci * 9) & 7) == 0 && ((uintptr_t)w0 & 15) == 0) {
+    // 16-byte loads: thread j takes 8 weights of output channel j % nco
+    const int r8 = run / 8;
+    for (int j = threadIdx.x; j < nco * r8; j += blockDim.x) {
+      const int k = j % nco, q = j / nco;
+      const uint4 u = *(const uint4 *)(w0 + (size_t)k * s.Ci * 9 + q * 8);
+      const __nv_bfloat16 *h = (const __nv_bfloat16 *)&u;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) ws[(q * 8 + e) * kCoTile + k] = bf(h[e]);
+    }
+  } else {
+    for (int k = 0; k < nco; ++k) {
+      const __nv_bfloat16 *wk = w0 + (size_t)k * s.Ci * 9;
+      for (int r = threadIdx.x; r < run; r += blockDim.x) ws[r * kCoTile + k] = bf(wk[r]);
+    }
   }
   __syncthreads();
-  const int slice = threadIdx.x / P, lp = threadIdx.x % P;
-  const int npix = s.Ho * s.Wo;
-  const int pix = (blockIdx.x / cl) * P + lp;
   float acc[kCoTile];
 #pragma unroll
   for (int k = 0; k < kCoTile; ++k) acc[k] = 0.0f;
-  if (pix < npix) {
-    const int oy = pix / s.Wo, ox = pix % s.Wo;
-    const int Y0 = oy * S - 1, X0 = ox * S - 1;
-    const size_t plane = (size_t)s.Hi * s.Wi;
-    const __nv_bfloat16 *xb = x + ((size_t)b * s.Ci + ci_lo) * plane;
-#pragma unroll 2
-    for (int c = slice; c < nci; c += split) {
-      const __nv_bfloat16 *p = xb + c * plane;
-      const float *wc = ws + c * 9 * kCoTile;
-      float v[9];
+  if (live) {
+    for (int c0 = slice; c0 < nci; c0 += kPre * split) {
+      if (c0 != slice) load(c0);
 #pragma unroll
-      for (int t = 0; t < 9; ++t) v[t] = in_at_u<U>(p, Y0 + t / 3, X0 + t % 3, s.Hi, s.Wi);
+      for (int j = 0; j < kPre; ++j) {
+        const int c = c0 + j * split;
+        if (c >= nci) break;
+        const float4 *wc = (const float4 *)(ws + c * 9 * kCoTile);
 #pragma unroll
-      for (int t = 0; t < 9; ++t)
-#pragma unroll
-        for (int k = 0; k < kCoTile; ++k) acc[k] = fmaf(wc[t * kCoTile + k], v[t], acc[k]);
+        for (int t = 0; t < 9; ++t) {
+          const float4 w0 = wc[2 * t], w1 = wc[2 * t + 1];
+          acc[0] = fmaf(w0.x, v[j][t], acc[0]);
+          acc[1] = fmaf(w0.y, v[j][t], acc[1]);
+          acc[2] = fmaf(w0.z, v[j][t], acc[2]);
+          acc[3] = fmaf(w0.w, v[j][t], acc[3]);
+          acc[4] = fmaf(w1.x, v[j][t], acc[4]);
+          acc[5] = fmaf(w1.y, v[j][t], acc[5]);
+          acc[6] = fmaf(w1.z, v[j][t], acc[6]);
+          acc[7] = fmaf(w1.w, v[j][t], acc[7]);
+        }
+      }
     }
   }
   if (split > 1) {
@@ -350,11 +392,12 @@ int conv_split(int ci, int P) {
   return sp;
 }
 
-// CTAs per cluster: up to 8, until a layer has about four CTAs per SM,
-// keeping at least 8 input channels per CTA
+// CTAs per cluster: up to 8, while the layer has fewer CTAs than SMs,
+// keeping at least 8 input channels per CTA (a CTA's fixed costs -- weight
+// staging, barriers -- make more, thinner CTAs slower)
 int conv_cluster(long long blocks, int ci) {
   int cl = 1;
-  while (cl < 8 && blocks * cl < 4 * 152 && ci / (cl * 2) >= 8) cl *= 2;
+  while (cl < 8 && blocks * cl * 2 <= 152 && ci / (cl * 2) >= 8) cl *= 2;
   return cl;
 }
 

