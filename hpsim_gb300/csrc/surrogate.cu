@@ -10,12 +10,13 @@
 //                 times the Green's function, evaluated in FP32) at the
 //                 mesh's last row and column, which the network does not
 //                 predict, and at n_samples interior points drawn per solve;
-//   k_sur_apply   the network's E_r and E_z corrected by gains (constant
+//   k_sur_fit     the network's E_r and E_z corrected by gains (constant
 //                 plus linear across the mesh) fitted at the sample points,
-//                 and their relative residual there; within tolerance, the
-//                 field table gets the corrected interior and the
-//                 spot-solved boundary, and the solver state says so: the
-//                 FP64 Green's table and the contraction then return at once.
+//                 and their relative residual there against the tolerance;
+//   k_sur_write   when accepted, the field table gets the corrected interior
+//                 and the spot-solved boundary, and the solver state says
+//                 so: the FP64 Green's table and the contraction then return
+//                 at once.
 // Kicks that do not remesh, meshes other than the trained one and empty
 // meshes leave everything to the plain path.
 #include <cuda_bf16.h>
@@ -33,6 +34,7 @@ namespace hps {
 namespace {
 
 constexpr int kSurBlock = 256;
+constexpr int kFitBlock = 64;
 
 struct SurDev {
   int active;          // this kick is the surrogate's to try
@@ -40,6 +42,7 @@ struct SurDev {
   double scale;        // field = network output * scale
   double c1, dzg;      // Green's-table scale, bunch-frame cell length
   double residual;     // relative residual of the last check
+  double cf[6];        // field = output * (cf0 + cf1 z + cf2 r) for E_r, cf3.. for E_z
   uint32_t n_accepted, n_rejected;
 };
 
@@ -201,19 +204,18 @@ __device__ inline bool solve3(const double *m, const double *y, double *c) {
 __device__ inline float zhat(uint32_t zp, uint32_t nz) { return ((float)zp + 0.5f) / (float)nz - 0.5f; }
 __device__ inline float rhat(uint32_t rp, uint32_t nr) { return ((float)rp + 0.5f) / (float)nr; }
 
-// Every block forms the same acceptance test over the samples (same values,
-// same order).  Calibration: each component e of the network's field is
-// corrected to e (c0 + c1 z + c2 r) (z, r relative mesh coordinates) with
-// the least-squares coefficients that fit it to the spot-solved values (a
-// global amplitude error and gains varying linearly across the mesh are
-// removed; a singular fit keeps the amplitude factor alone).  The relative
-// residual of the corrected field at the samples decides; within tolerance,
-// each block writes its share of the field table.
-__global__ void __launch_bounds__(kSurBlock) k_sur_apply(ScState *sc, ScTables t, SurDev *sd,
-                                                         const __nv_bfloat16 *out, const double2 *spot, uint32_t nr,
-                                                         uint32_t nz, uint32_t n_samples, double tol) {
+// The acceptance test (one block).  Calibration: each component e of the
+// network's field is corrected to e (c0 + c1 z + c2 r) (z, r relative mesh
+// coordinates) with the least-squares coefficients that fit it to the
+// spot-solved values (a global amplitude error and gains varying linearly
+// across the mesh are removed; a singular fit keeps the amplitude factor
+// alone).  The relative residual of the corrected field at the samples
+// decides; the coefficients and the decision go to the solver state.
+__global__ void __launch_bounds__(kFitBlock) k_sur_fit(ScState *sc, SurDev *sd, const __nv_bfloat16 *out,
+                                                       const double2 *spot, uint32_t nr, uint32_t nz,
+                                                       uint32_t n_samples, double tol) {
   if (!sd->active) return;
-  __shared__ double red[18 * (kSurBlock / 32)];
+  __shared__ double red[18 * (kFitBlock / 32)];
   const double scale = sd->scale;
   const uint32_t nb = nr * nz, base = nr + 1 + nz;
   // per component: the normal matrix (6) and right-hand side (3)
@@ -260,24 +262,31 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_apply(ScState *sc, ScTables t
     r[1] += e.x * e.x + e.y * e.y;
   }
   block_sum(red, r);
+  if (threadIdx.x != 0) return;
   const double res = r[1] > 0.0 ? sqrt(r[0] / r[1]) : (r[0] > 0.0 ? 1.0 : 0.0);
   const bool ok = res <= tol;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    sd->residual = res;
-    if (ok) sd->n_accepted += 1;
-    else sd->n_rejected += 1;
-    sc->sur_accepted = ok;
-  }
-  if (!ok) return;
-  const uint32_t nrow = nr + 1;
+  sd->residual = res;
+  if (ok) sd->n_accepted += 1;
+  else sd->n_rejected += 1;
+  for (int j = 0; j < 6; ++j) sd->cf[j] = scale * cf[j / 3][j % 3];
+  sc->sur_accepted = ok;
+}
+
+// an accepted field into the field table: the corrected network field inside,
+// the spot-solved values on the last row and column
+__global__ void __launch_bounds__(kSurBlock) k_sur_write(const ScState *sc, ScTables t, const SurDev *sd,
+                                                         const __nv_bfloat16 *out, const double2 *spot, uint32_t nr,
+                                                         uint32_t nz) {
+  if (!sd->active || !sc->sur_accepted) return;
+  const uint32_t nrow = nr + 1, nb = nr * nz;
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= (nz + 1) * nrow) return;
   const uint32_t zp = p / nrow, rp = p % nrow;
   double2 e;
   if (zp < nz && rp < nr) {
     const double zh = zhat(zp, nz), rh = rhat(rp, nr);
-    e.x = (double)__bfloat162float(out[zp * nr + rp]) * scale * (cf[0][0] + cf[0][1] * zh + cf[0][2] * rh);
-    e.y = (double)__bfloat162float(out[nb + zp * nr + rp]) * scale * (cf[1][0] + cf[1][1] * zh + cf[1][2] * rh);
+    e.x = (double)__bfloat162float(out[zp * nr + rp]) * (sd->cf[0] + sd->cf[1] * zh + sd->cf[2] * rh);
+    e.y = (double)__bfloat162float(out[nb + zp * nr + rp]) * (sd->cf[3] + sd->cf[4] * zh + sd->cf[5] * rh);
   } else {
     e = spot[zp == nz ? rp : nr + 1 + zp];
   }
@@ -310,10 +319,12 @@ void sur_solve(const DevBeam &bm, ScState *sc, const ScTables &t, const ScKickAr
   }
   const uint32_t npts = n.nr + 1 + n.nz + n.n_samples;
   k_sur_spot<<<npts, kSurBlock, 0, st>>>(sc, t, sd, (double2 *)n.spot, n.nr, n.nz);
+  const __nv_bfloat16 *out = (const __nv_bfloat16 *)n.act.back();
+  k_sur_fit<<<1, kFitBlock, 0, st>>>(sc, sd, out, (const double2 *)n.spot, n.nr, n.nz, n.n_samples, n.tol);
   const uint32_t nf = (n.nz + 1) * (n.nr + 1);
-  k_sur_apply<<<(nf + kSurBlock - 1) / kSurBlock, kSurBlock, 0, st>>>(
-      sc, t, sd, (const __nv_bfloat16 *)n.act.back(), (const double2 *)n.spot, n.nr, n.nz, n.n_samples, n.tol);
-  note_launch(3);
+  k_sur_write<<<(nf + kSurBlock - 1) / kSurBlock, kSurBlock, 0, st>>>(sc, t, sd, out, (const double2 *)n.spot,
+                                                                      n.nr, n.nz);
+  note_launch(4);
 }
 
 int sur_build(SurNet &n, int n_layers, const int32_t *arch, int gmean_after, const int32_t *skip,
