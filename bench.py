@@ -46,12 +46,14 @@ def parse():
     p.add_argument("--gaps", type=int, default=GAPS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="dtl_like", choices=["dtl_like", "small_fodo", "ccl_large", "batched"],
+    p.add_argument("--workload", default="dtl_like",
+                   choices=["dtl_like", "small_fodo", "ccl_large", "batched", "ccl_batch"],
                    help="dtl_like: one 1M-particle beam through 165 DTL gaps (the headline); small_fodo: "
                         "65,536 particles in FP64 through buncher + 40 FODO elements; ccl_large: 16,777,216 "
                         "particles through 1024 CCL gaps, SCHEFF 64x256; batched: 256 beams of the "
-                        "small-FODO topology in one graph launch")
-    p.add_argument("--beams", type=int, default=256)
+                        "small-FODO topology in one graph launch; ccl_batch: 16 beams of 1,048,576 particles "
+                        "through the CCL lattice with perturbed set points in one graph launch")
+    p.add_argument("--beams", type=int, default=None, help="batched: 256, ccl_batch: 16")
     p.add_argument("--surrogate", nargs="?", const=SURROGATE_NET, default=None,
                    help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
                         "(a network file; default the shipped 32x128 network), and report both")
@@ -309,27 +311,42 @@ def run_reference(args):
 
 
 def run_batched(args):
-    """Independent beams of uneven sizes with perturbed RF and quad set points
-    (lattices.batched_scan) advanced by one graph launch per step; value =
-    all beams' particle-element steps / step time."""
+    """Independent beams advanced by one graph launch per step; value = all
+    beams' particle-element steps / step time.  batched: beams of uneven
+    sizes with perturbed RF and quad set points on the small-FODO topology
+    (lattices.batched_scan); ccl_batch: equal 1,048,576-particle beams
+    through the CCL-like lattice with perturbed set points
+    (lattices.ccl_batch)."""
     import torch
     from hpsim_gb300 import HPSim, build, lattices as L
     build.build()
     HPSim.set_gpu(0)
-    scan = L.batched_scan(args.beams)
+    ccl = args.workload == "ccl_batch"
+    if args.beams is None:
+        args.beams = 16 if ccl else 256
+    if ccl:
+        scan = L.ccl_batch(args.beams)
+        base = L.ccl_like()
+        spec = WORKLOADS["ccl_large"]
+        lattice = lambda sb: L.perturbed(base, sb)  # noqa: E731
+    else:
+        scan = L.batched_scan(args.beams)
+        spec = WORKLOADS["small_fodo"]
+        lattice = L.scan_lattice
+    w0, freq = spec["w0"], spec["freq"]
     objs = []
     for sb in scan:
         beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=sb.num, precision=args.precision)
-        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, sb.seed)
-        beam.set_ref_w(0.75)
+        beam.set_waterbag(*L.waterbag_twiss(w0=w0, freq=freq), 0.0, w0, freq, sb.seed)
+        beam.set_ref_w(w0)
         beam.set_ref_phi(0.0)
         beam.save_initial_beam()
-        bl = HPSim.BeamLine(elements=L.scan_lattice(sb))
-        sc = HPSim.SpaceCharge(32, 128, 0.1, 0)
+        bl = HPSim.BeamLine(elements=lattice(sb))
+        sc = HPSim.SpaceCharge(*spec["mesh"], spec["interval"], 0)
         sc.set_remesh_threshold(0.0)
         objs.append((beam, bl, sc, HPSim.Simulator(beam, bl, sc)))
     batch = HPSim.Batch([o[3] for o in objs])
-    n_elem = len(L.small_fodo())
+    n_elem = len(objs[0][1])
     total = sum(sb.num for sb in scan)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:0")
 
@@ -362,10 +379,14 @@ def run_batched(args):
     line = {"metric": METRIC, "value": total * n_elem / t, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
-            "config": {"workload": f"batched scan: {args.beams} beams, particles log-uniform in [16384, 524288] "
-                                   f"(total {total}), small-FODO topology ({n_elem} elements) with per-beam RF "
-                                   f"scale, phase offset and quad scale, SCHEFF 32x128 at every element, one "
-                                   f"graph launch per step", "beams": args.beams, "particles": total,
+            "config": {"workload": (f"CCL batch: {args.beams} beams of {scan[0].num} particles (total {total}), "
+                                    f"CCL-like lattice ({n_elem} elements) with per-beam RF amplitude scale, "
+                                    f"RF phase offset and quad scale, SCHEFF 64x256 at every element, one graph "
+                                    f"launch per step") if ccl else
+                                   (f"batched scan: {args.beams} beams, particles log-uniform in [16384, 524288] "
+                                    f"(total {total}), small-FODO topology ({n_elem} elements) with per-beam RF "
+                                    f"scale, phase offset and quad scale, SCHEFF 32x128 at every element, one "
+                                    f"graph launch per step"), "beams": args.beams, "particles": total,
                        "elements": n_elem, "precision": args.precision,
                        "l2": "flushed between steps (256 MB write)"},
             "sequential": {"ms_per_step": 1000 * t_seq, "value": total * n_elem / t_seq,
@@ -380,7 +401,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if args.workload == "batched":
+    if args.workload in ("batched", "ccl_batch"):
         run_batched(args)
         return
     ws, rank, local = dist_env()

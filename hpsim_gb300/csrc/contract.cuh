@@ -5,9 +5,10 @@
 // g(k) = G[rp][k - 1][rs] for sources below the point (k >= 1) and
 // G[rp][-k][rs] with E_z negated for sources at or above it (k <= 0).
 // For each source radius this is a convolution along z.  A block stages its
-// rp's g(k), k = -(nz - 1) .. nz, sign included, and the charges (2^-36
-// fixed point converted to T) in shared memory, a tile of source radii at a
-// time.  A warp computes kCP consecutive field points over half the source
+// rp's g(k) (mirrored with the sign included, or the table rows alone with
+// the E_z sign flipped on reading when the mirror does not fit) and the
+// charges (2^-36 fixed point converted to T) in shared memory, a tile of
+// source radii at a time.  A warp computes kCP consecutive field points over half the source
 // rows (two warps per point group, summed in a fixed order): the lanes run
 // over source radii, and as the warp walks the rows the kCP values of g it
 // needs slide by one, kept in a ring of kCP + 1 registers that takes one new
@@ -30,7 +31,9 @@ constexpr int kCH = 2;                     // warps sharing the source rows of a
 constexpr int kCG = 4;                     // point groups per block
 constexpr int kCZ = kCP * kCG;             // field points per block
 constexpr int kContractThreads = kCG * kCH * 32;
-constexpr int kContractSmem = 96 * 1024;   // largest table + charge tile
+// largest table + charge tile: 32 source radii of an FP32 256-row mesh or of
+// an FP64 128-row mesh (two CTAs per SM; lanes run over source radii)
+constexpr int kContractSmem = 96 * 1024;
 
 // the FP32 and FP64 tables: pair type, table layout, charge conversion
 template <class T> struct CTab;
@@ -64,17 +67,34 @@ template <> struct CTab<double> {
   static __device__ double *out(const ScTables &t) { return t.fld2; }
 };
 
-// source radii per staged tile: g(k) (2 nz pairs) and charges (nz values)
-// (5 values of T per row and radius)
-template <class T>
+// Two layouts of the staged table.  Mirrored (M): g(k) for k = -(nz - 1)
+// .. nz stored with its sign, 2 nz pairs per radius, read with no select;
+// single: the nz table rows, g(k) formed on reading (E_z negated for k <=
+// 0).  With the charges, 5 or 3 values of T per row and radius.  The
+// mirrored layout is used when a 32-radius tile of it fits.
+template <class T, bool M>
 __host__ __device__ inline uint32_t contract_tile(uint32_t nx, uint32_t nz) {
-  const uint32_t t = (uint32_t)(kContractSmem / (5 * sizeof(T) * nz));
+  const uint32_t t = (uint32_t)(kContractSmem / ((M ? 5 : 3) * sizeof(T) * nz));
   return t < nx ? t : nx;
+}
+template <class T>
+inline bool contract_mirrored(uint32_t nx_max, uint32_t nz_max) {
+  return (size_t)5 * sizeof(T) * nz_max * std::min<uint32_t>(32u, nx_max) <= (size_t)kContractSmem;
 }
 // (bounds the tile of every mesh up to nx_max x nz_max)
 template <class T>
 inline size_t contract_smem(uint32_t nx_max, uint32_t nz_max) {
-  return std::min<size_t>(kContractSmem, (size_t)5 * sizeof(T) * nx_max * nz_max);
+  const size_t per = contract_mirrored<T>(nx_max, nz_max) ? 5 : 3;
+  return std::min<size_t>(kContractSmem, per * sizeof(T) * nx_max * nz_max);
+}
+
+// g(k) of the staged tile (h: the tile's column of this lane's radius)
+template <bool M, class V>
+__device__ __forceinline__ V gk(const V *h, int k, int tr, int nz) {
+  if (M) return h[(nz - 1 + k) * tr];
+  const bool below = k >= 1;
+  const V v = h[(below ? k - 1 : -k) * tr];
+  return below ? v : V{v.x, -v.y};
 }
 
 // the bin limit of field row zp (the reference's partition of the table)
@@ -97,15 +117,15 @@ __device__ inline V cpair(T x, T y) { return V{x, y}; }
 // One block's work; TR > 0 is the tile width known at compile time (nr ==
 // TR, one tile: every shared-memory offset of the row walk is an immediate),
 // TR == 0 the general tiled form.
-template <class T, int TR>
+template <class T, int TR, bool M>
 __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables &t, T *sm,
                                                typename CTab<T>::V (*upper)[kCP]) {
   using V = typename CTab<T>::V;
   const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
   const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ;
-  const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile<T>(nx, nz);
-  V *gz = (V *)sm;                 // [k + nz - 1][tr], k = -(nz - 1) .. nz
-  T *qs = sm + 4 * nz * tr;        // [zs][tr]
+  const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile<T, M>(nx, nz);
+  V *gz = (V *)sm;                     // M: [k + nz - 1][tr]; else [dz][tr] holding g(dz + 1)
+  T *qs = sm + (M ? 4 : 2) * nz * tr;  // [zs][tr]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = warp / kCH, half = warp % kCH;
   const uint32_t zp0 = zb0 + grp * kCP;  // points zp0 .. zp0 + kCP - 1
@@ -145,8 +165,12 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
         const uint32_t e = e0 + u * blockDim.x;
         if (e < ntile) {
           const uint32_t z = CTab<T>::kZFast ? e % nz : e / ntr, r = CTab<T>::kZFast ? e / nz : e % ntr;
-          gz[(nz + z) * tr + r] = gv[u];                                // k = z + 1
-          gz[(nz - 1 - z) * tr + r] = cpair<T, V>(gv[u].x, -gv[u].y);   // k = -z
+          if (M) {
+            gz[(nz + z) * tr + r] = gv[u];                               // k = z + 1
+            gz[(nz - 1 - z) * tr + r] = cpair<T, V>(gv[u].x, -gv[u].y);  // k = -z
+          } else {
+            gz[z * tr + r] = gv[u];  // g(z + 1), and g(-z) with E_z negated
+          }
           qs[z * tr + r] = CTab<T>::charge(bv[u]);
         }
       }
@@ -160,16 +184,16 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
         // gp walks g(zp0 - zs - 1) down the rows, qp the charges up.
         constexpr int R = kCP + 1;
         V ring[R];
-        const V *g = gz + (nz - 1) * tr + r;  // g(k) at g[k * tr]
+        const V *h = gz + r;
 #pragma unroll
-        for (int j = 0; j < kCP; ++j) ring[j] = g[min((int)(zp0 + j) - (int)za, (int)nz) * (int)tr];
-        const V *gp = g + ((int)zp0 - (int)za - 1) * (int)tr;
+        for (int j = 0; j < kCP; ++j) ring[j] = gk<M>(h, min((int)(zp0 + j) - (int)za, (int)nz), (int)tr, (int)nz);
         const T *qp = qs + za * tr + r;
-        for (uint32_t zs0 = za; zs0 < zb; zs0 += R, gp -= R * tr, qp += R * tr) {
+        for (uint32_t zs0 = za; zs0 < zb; zs0 += R, qp += R * tr) {
 #pragma unroll
           for (int u = 0; u < R; ++u) {
             if (zs0 + u >= zb) break;
-            if (zs0 + u + 1 < zb) ring[(R - 1 - u) % R] = gp[-(int)(u * tr)];
+            // g(zp0 - zs - 1) for the next row
+            if (zs0 + u + 1 < zb) ring[(R - 1 - u) % R] = gk<M>(h, (int)zp0 - (int)(zs0 + u) - 1, (int)tr, (int)nz);
             const T qv = qp[u * tr];
 #pragma unroll
             for (int j = 0; j < kCP; ++j) {
@@ -182,14 +206,14 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
       } else {
         // small meshes: each point sums the source rows below its own limit
         const T *q = qs + r;
-        const V *g = gz + (nz - 1) * tr + r;
+        const V *h = gz + r;
         const uint32_t rs = rs0 + r;
         for (int j = 0; j < kCP; ++j) {
           if (zp0 + j > nz) continue;
           const uint32_t zend = lim[j] > rs ? min(zb, (lim[j] - rs + nx - 1) / nx) : 0u;
           for (uint32_t zs = za; zs < zend; ++zs) {
             const T qv = q[zs * tr];
-            const V gv = g[((int)(zp0 + j) - (int)zs) * (int)tr];
+            const V gv = gk<M>(h, (int)(zp0 + j) - (int)zs, (int)tr, (int)nz);
             ax[j] = fma(qv, gv.x, ax[j]);
             az[j] = fma(qv, gv.y, az[j]);
           }
@@ -219,17 +243,34 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
 }
 
 // grid (nr_max + 1, ceil((nz_max + 1) / kCZ)), kContractThreads threads,
-// contract_smem<T>(nr_max, nz_max) bytes
-template <class T>
-__global__ void __launch_bounds__(kContractThreads) k_contract_t(const ScState *sc, ScTables t) {
+// contract_smem<T>(nr_max, nz_max) bytes, M = contract_mirrored<T>(nr_max,
+// nz_max)
+template <class T, bool M>
+__global__ void __launch_bounds__(kContractThreads) k_contract_m(const ScState *sc, ScTables t) {
   if (!sc->remesh || sc->sur_accepted) return;
   const uint32_t nx = sc->nx, nz = sc->nz;
   if (blockIdx.x > nx || blockIdx.y * kCZ > nz) return;
   extern __shared__ __align__(16) unsigned char contract_raw[];
   __shared__ typename CTab<T>::V upper[kCG][kCP];  // second halves' sums
   T *sm = (T *)contract_raw;
-  if (nx == 32 && contract_tile<T>(nx, nz) == 32) contract_block<T, 32>(sc, t, sm, upper);
-  else contract_block<T, 0>(sc, t, sm, upper);
+  if (nx == 32 && contract_tile<T, M>(nx, nz) == 32) contract_block<T, 32, M>(sc, t, sm, upper);
+  else contract_block<T, 0, M>(sc, t, sm, upper);
+}
+
+// the launch: the layout for the largest mesh the solver takes
+template <class T>
+inline void contract_launch(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max,
+                            cudaStream_t st) {
+  const dim3 cg(nx_max + 1, (nz_max + 1 + kCZ - 1) / kCZ);
+  const size_t smem = contract_smem<T>(nx_max, nz_max);
+  if (contract_mirrored<T>(nx_max, nz_max)) k_contract_m<T, true><<<cg, kContractThreads, smem, st>>>(sc, t);
+  else k_contract_m<T, false><<<cg, kContractThreads, smem, st>>>(sc, t);
+}
+
+template <class T>
+inline void contract_configure() {
+  cudaFuncSetAttribute(k_contract_m<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
 }
 
 }  // namespace

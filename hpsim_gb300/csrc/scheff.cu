@@ -429,11 +429,8 @@ void sc_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs
 // sized for the largest mesh the solver takes
 void contract64(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max, cudaStream_t st) {
   static std::once_flag once;
-  std::call_once(once, [] {
-    cudaFuncSetAttribute(k_contract_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
-  });
-  dim3 cg(nx_max + 1, (nz_max + 1 + kCZ - 1) / kCZ);
-  k_contract_t<double><<<cg, kContractThreads, contract_smem<double>(nx_max, nz_max), st>>>(sc, t);
+  std::call_once(once, [] { contract_configure<double>(); });
+  contract_launch<double>(sc, t, nx_max, nz_max, st);
 }
 
 void sc_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,

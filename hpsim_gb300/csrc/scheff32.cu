@@ -529,9 +529,7 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   ngreen = (ngreen + kDepCluster - 1) / kDepCluster * kDepCluster;
   launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
   note_launch();
-  dim3 cg(a.nx_max + 1, (a.nz_max + 1 + kCZ - 1) / kCZ);
-  launch_k(k_contract_t<float>, cg, dim3(kContractThreads), contract_smem<float>(a.nx_max, a.nz_max), st,
-           (const ScState *)sc, u);
+  contract_launch<float>(sc, u, a.nx_max, a.nz_max, st);
   note_launch();
 }
 
@@ -551,7 +549,7 @@ void sc32_configure() {
   if (done) return;
   done = true;
   cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
-  cudaFuncSetAttribute(k_contract_t<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  contract_configure<float>();
 }
 
 namespace {
@@ -616,8 +614,7 @@ hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, co
     t.ffld2 = f2;
     t.c32 = c32;
     k32_green<<<4 * 152, kBlock>>>(sc, t);
-    dim3 cg(nr + 1, (nz + 1 + kCZ - 1) / kCZ);
-    k_contract_t<float><<<cg, kContractThreads, contract_smem<float>(nr, nz)>>>(sc, t);
+    contract_launch<float>(sc, t, nr, nz, 0);
     note_launch(4);
     e = cudaGetLastError();
   }

@@ -209,6 +209,35 @@ def scan_lattice(sb: ScanBeam, aperture=0.0):
     return out
 
 
+def ccl_batch(n_beams=16, num=1 << 20, seed=805):
+    """Beams of the CCL-like lattice with perturbed set points: RF amplitude
+    scale U(0.99, 1.01), RF phase offset U(-1, +1) deg and quad-gradient
+    scale U(0.97, 1.03) per beam, equal particle counts."""
+    rng = np.random.default_rng(seed)
+    return [ScanBeam(num=num, seed=int(rng.integers(1, 2 ** 31)), rf_scale=float(rng.uniform(0.99, 1.01)),
+                     phase_offset=math.radians(float(rng.uniform(-1.0, 1.0))),
+                     quad_scale=float(rng.uniform(0.97, 1.03))) for _ in range(n_beams)]
+
+
+def perturbed(elems, sb: ScanBeam):
+    """A lattice with one batch beam's set points: every RF gap's amplitude
+    scaled and phase shifted, the buncher's voltage and phase likewise, every
+    quad gradient scaled."""
+    out = []
+    for code, name, p in elems:
+        p = p.copy()
+        if code in (RFGAP_DTL, RFGAP_CCL):
+            p[param_index(code, "amplitude")] *= sb.rf_scale
+            p[param_index(code, "phase_shift")] += sb.phase_offset
+        elif code == BUNCHER:
+            p[param_index(BUNCHER, "voltage")] *= sb.rf_scale
+            p[param_index(BUNCHER, "phase")] += sb.phase_offset
+        elif code == QUAD:
+            p[param_index(QUAD, "gradient")] *= sb.quad_scale
+        out.append((code, name, p))
+    return out
+
+
 def _ttf_fit(rng, beta_g, t_nom=0.85, s_nom=0.10, spread=0.05):
     """Cubic T(beta), S(beta) in powers of beta.
 
