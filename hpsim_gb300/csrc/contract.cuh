@@ -114,33 +114,29 @@ __device__ inline uint32_t contract_lim(uint32_t zp, uint32_t rp, uint32_t nx, u
 template <class T, class V>
 __device__ inline V cpair(T x, T y) { return V{x, y}; }
 
-// One block's work; TR > 0 is the tile width known at compile time (nr ==
-// TR, one tile: every shared-memory offset of the row walk is an immediate),
-// TR == 0 the general tiled form.
-template <class T, int TR, bool M>
+// One block's work: S slabs of kCZ field rows of one field radius from
+// each staged tile (S > 1 stages the table once for more rows); TR > 0 is
+// the tile width known at compile time (nr == TR, one tile: every
+// shared-memory offset of the row walk is an immediate), TR == 0 the general
+// tiled form.
+template <class T, int TR, bool M, int S>
 __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables &t, T *sm,
-                                               typename CTab<T>::V (*upper)[kCP]) {
+                                               typename CTab<T>::V (*upper)[kCG][kCP]) {
   using V = typename CTab<T>::V;
   const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
-  const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ;
+  const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ * S;
   const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile<T, M>(nx, nz);
   V *gz = (V *)sm;                     // M: [k + nz - 1][tr]; else [dz][tr] holding g(dz + 1)
   T *qs = sm + (M ? 4 : 2) * nz * tr;  // [zs][tr]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = warp / kCH, half = warp % kCH;
-  const uint32_t zp0 = zb0 + grp * kCP;  // points zp0 .. zp0 + kCP - 1
   const uint32_t za = half * nz / kCH, zb = (half + 1) * nz / kCH;  // this warp's source rows
-  uint32_t lim[kCP];
-  bool cut = false;
-#pragma unroll
-  for (int j = 0; j < kCP; ++j) {
-    lim[j] = contract_lim(zp0 + j, rp, nx, nz);
-    cut |= zp0 + j <= nz && lim[j] < fld_sz;
-  }
   const V *G = CTab<T>::slice(t, rp, fld_sz);
-  T ax[kCP], az[kCP];
+  T axs[S][kCP], azs[S][kCP];
 #pragma unroll
-  for (int j = 0; j < kCP; ++j) ax[j] = az[j] = T(0);
+  for (int sl = 0; sl < S; ++sl)
+#pragma unroll
+    for (int j = 0; j < kCP; ++j) axs[sl][j] = azs[sl][j] = T(0);
   for (uint32_t rs0 = 0; rs0 < nx; rs0 += tr) {
     const uint32_t ntr = TR > 0 ? (uint32_t)TR : min(tr, nx - rs0), ntile = nz * ntr;
     __syncthreads();
@@ -176,7 +172,19 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
       }
     }
     __syncthreads();
+#pragma unroll
+    for (int sl = 0; sl < S; ++sl) {
+    const uint32_t zp0 = zb0 + sl * kCZ + grp * kCP;  // points zp0 .. zp0 + kCP - 1
     if (zp0 > nz) continue;
+    uint32_t lim[kCP];
+    bool cut = false;
+#pragma unroll
+    for (int j = 0; j < kCP; ++j) {
+      lim[j] = contract_lim(zp0 + j, rp, nx, nz);
+      cut |= zp0 + j <= nz && lim[j] < fld_sz;
+    }
+    T (&ax)[kCP] = axs[sl];
+    T (&az)[kCP] = azs[sl];
     for (uint32_t r = lane; r < ntr; r += 32) {
       if (!cut) {
         // ring slot (j - u) mod R holds g(zp0 + j - zs), u = zs - zs0; the
@@ -220,57 +228,78 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
         }
       }
     }
+    }  // slabs
   }
 #pragma unroll
-  for (int j = 0; j < kCP; ++j) {
+  for (int sl = 0; sl < S; ++sl)
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      ax[j] += __shfl_down_sync(0xffffffffu, ax[j], off);
-      az[j] += __shfl_down_sync(0xffffffffu, az[j], off);
+    for (int j = 0; j < kCP; ++j) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        axs[sl][j] += __shfl_down_sync(0xffffffffu, axs[sl][j], off);
+        azs[sl][j] += __shfl_down_sync(0xffffffffu, azs[sl][j], off);
+      }
     }
-  }
   if (half == 1 && lane == 0)
-    for (int j = 0; j < kCP; ++j) upper[grp][j] = cpair<T, V>(ax[j], az[j]);
+    for (int sl = 0; sl < S; ++sl)
+      for (int j = 0; j < kCP; ++j) upper[sl][grp][j] = cpair<T, V>(axs[sl][j], azs[sl][j]);
   __syncthreads();
-  if (half != 0 || lane != 0 || zp0 > nz) return;
+  if (half != 0 || lane != 0) return;
   T *out = CTab<T>::out(t);
-  for (int j = 0; j < kCP; ++j) {
-    if (zp0 + j > nz) break;
-    const size_t pt = (size_t)(zp0 + j) * nrow + rp;
-    out[2 * pt] = ax[j] + upper[grp][j].x;
-    out[2 * pt + 1] = az[j] + upper[grp][j].y;
+  for (int sl = 0; sl < S; ++sl) {
+    const uint32_t zp0 = zb0 + sl * kCZ + grp * kCP;
+    for (int j = 0; j < kCP; ++j) {
+      if (zp0 + j > nz) break;
+      const size_t pt = (size_t)(zp0 + j) * nrow + rp;
+      out[2 * pt] = axs[sl][j] + upper[sl][grp][j].x;
+      out[2 * pt + 1] = azs[sl][j] + upper[sl][grp][j].y;
+    }
   }
 }
 
-// grid (nr_max + 1, ceil((nz_max + 1) / kCZ)), kContractThreads threads,
+// grid (nr_max + 1, ceil((nz_max + 1) / (kCZ S))), kContractThreads threads,
 // contract_smem<T>(nr_max, nz_max) bytes, M = contract_mirrored<T>(nr_max,
-// nz_max)
-template <class T, bool M>
+// nz_max), S = contract_slabs<T>(nz_max)
+template <class T, bool M, int S>
 __global__ void __launch_bounds__(kContractThreads) k_contract_m(const ScState *sc, ScTables t) {
   if (!sc->remesh || sc->sur_accepted) return;
   const uint32_t nx = sc->nx, nz = sc->nz;
-  if (blockIdx.x > nx || blockIdx.y * kCZ > nz) return;
+  if (blockIdx.x > nx || blockIdx.y * kCZ * S > nz) return;
   extern __shared__ __align__(16) unsigned char contract_raw[];
-  __shared__ typename CTab<T>::V upper[kCG][kCP];  // second halves' sums
+  __shared__ typename CTab<T>::V upper[S][kCG][kCP];  // second halves' sums
   T *sm = (T *)contract_raw;
-  if (nx == 32 && contract_tile<T, M>(nx, nz) == 32) contract_block<T, 32, M>(sc, t, sm, upper);
-  else contract_block<T, 0, M>(sc, t, sm, upper);
+  if (nx == 32 && contract_tile<T, M>(nx, nz) == 32) contract_block<T, 32, M, S>(sc, t, sm, upper);
+  else contract_block<T, 0, M, S>(sc, t, sm, upper);
 }
 
-// the launch: the layout for the largest mesh the solver takes
+// slabs per block: FP32 meshes of 256 rows and more have blocks enough to
+// stage the table for 4 slabs at once (4x less table traffic from L2)
+template <class T>
+inline int contract_slabs(uint32_t nz_max) { return sizeof(T) == 4 && nz_max >= 256 ? 4 : 1; }
+
+// the launch: the layout and slab count for the largest mesh the solver takes
 template <class T>
 inline void contract_launch(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max,
                             cudaStream_t st) {
-  const dim3 cg(nx_max + 1, (nz_max + 1 + kCZ - 1) / kCZ);
+  const int S = contract_slabs<T>(nz_max);
+  const dim3 cg(nx_max + 1, (nz_max + 1 + kCZ * S - 1) / (kCZ * S));
   const size_t smem = contract_smem<T>(nx_max, nz_max);
-  if (contract_mirrored<T>(nx_max, nz_max)) k_contract_m<T, true><<<cg, kContractThreads, smem, st>>>(sc, t);
-  else k_contract_m<T, false><<<cg, kContractThreads, smem, st>>>(sc, t);
+  const bool mir = contract_mirrored<T>(nx_max, nz_max);
+  if (S == 4) {
+    if (mir) k_contract_m<T, true, 4><<<cg, kContractThreads, smem, st>>>(sc, t);
+    else k_contract_m<T, false, 4><<<cg, kContractThreads, smem, st>>>(sc, t);
+  } else {
+    if (mir) k_contract_m<T, true, 1><<<cg, kContractThreads, smem, st>>>(sc, t);
+    else k_contract_m<T, false, 1><<<cg, kContractThreads, smem, st>>>(sc, t);
+  }
 }
 
 template <class T>
 inline void contract_configure() {
-  cudaFuncSetAttribute(k_contract_m<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
-  cudaFuncSetAttribute(k_contract_m<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m<T, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m<T, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m<T, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m<T, false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
 }
 
 }  // namespace

@@ -76,3 +76,16 @@ def test_field_f32_32x128_against_fp64(adj):
     bins = np.round(q * 2 ** 20) / 2 ** 20
     mesh = np.array([4.0e-4, 2.0e-4, 0.05, 201.25, 65536, 1.6e-5, float(adj)])
     _close_per_component(field_f32(nr, nz, bins.ravel(), mesh), field(nr, nz, bins.ravel(), mesh), 2e-5)
+
+
+def test_field_f32_64x256_against_fp64():
+    """The 64 x 256 mesh of the CCL workloads (32-radius tiles of the
+    single-copy table, four row slabs per block): FP32 table stage within 2e-5
+    of the largest component of the FP64 one."""
+    nr, nz = 64, 256
+    r = (np.arange(nr) + 0.5) / nr
+    zz = (np.arange(nz) + 0.5) / nz - 0.5
+    q = np.exp(-(zz[:, None] / 0.12) ** 2 - (r[None, :] / 0.25) ** 2) * 2 * np.pi * r[None, :] * 5000
+    bins = np.round(q * 2 ** 20) / 2 ** 20
+    mesh = np.array([2.0e-4, 1.0e-4, 0.43, 805.0, 1048576, 1.6e-5, 0.0])
+    _close_per_component(field_f32(nr, nz, bins.ravel(), mesh), field(nr, nz, bins.ravel(), mesh), 2e-5)
