@@ -35,6 +35,7 @@ namespace {
 
 constexpr int kSurBlock = 256;
 constexpr int kFitBlock = 64;
+constexpr int kInBlocks = 16;
 
 struct SurDev {
   int active;          // this kick is the surrogate's to try
@@ -75,22 +76,27 @@ __device__ inline void spot_point(uint32_t k, uint32_t nr, uint32_t nz, uint32_t
   rp = (h >> 16) % nr;
 }
 
-__global__ void __launch_bounds__(1024) k_sur_input(ScState *sc, ScTables t, SurDev *sd, __nv_bfloat16 *x,
-                                                    uint32_t nr, uint32_t nz, double out_scale, uint32_t num_part,
-                                                    double cur_ov_mc2) {
-  __shared__ unsigned long long red[1024];
+// kInBlocks blocks: each sums the whole charge table (a few microseconds of
+// loads, not worth a second launch) and normalises its share; block 0
+// records the kick's scalars
+__global__ void __launch_bounds__(kSurBlock) k_sur_input(ScState *sc, ScTables t, SurDev *sd, __nv_bfloat16 *x,
+                                                         uint32_t nr, uint32_t nz, double out_scale,
+                                                         uint32_t num_part, double cur_ov_mc2) {
+  __shared__ unsigned long long red[kSurBlock];
   __shared__ int go;
+  __shared__ float qs;
+  __shared__ __nv_bfloat16 la;
   if (threadIdx.x == 0) {
-    sc->sur_accepted = 0;
     // the trained mesh, no adjacent bunches, every source row in the table
     const uint32_t by = (512 / nz < nr) ? 512 / nz : nr;
     go = sc->remesh && sc->nx == nr && sc->nz == nz && sc->adj == 0 && by && (nr / by) * by == nr;
   }
   __syncthreads();
-  if (!go) {
-    if (threadIdx.x == 0) sd->active = 0;
-    return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->sur_accepted = 0;
+    if (!go) sd->active = 0;
   }
+  if (!go) return;
   const uint32_t nb = nr * nz;
   unsigned long long a = 0;
   for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) a += t.bin_fx[k];
@@ -100,25 +106,24 @@ __global__ void __launch_bounds__(1024) k_sur_input(ScState *sc, ScTables t, Sur
     if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
     __syncthreads();
   }
-  // one thread forms the scalars (FP64 divides and logs run on the slow pipe)
-  __shared__ float qs;
-  __shared__ __nv_bfloat16 la;
   if (threadIdx.x == 0) {
-    const double total = (double)(long long)red[0] * kBinInvScale;
     const double dzg = sc->dz * rsqrt(1.0 - sc->beta * sc->beta);
-    const double c1 = 5721.67 * cur_ov_mc2 / (sc->freq * 1e6 * (double)num_part);
-    sd->active = total > 0.0;
-    sd->total = total;
-    sd->scale = c1 * total / (out_scale * sc->dr * dzg);
-    sd->c1 = c1;
-    sd->dzg = dzg;
+    if (blockIdx.x == 0) {
+      const double total = (double)(long long)red[0] * kBinInvScale;
+      const double c1 = 5721.67 * cur_ov_mc2 / (sc->freq * 1e6 * (double)num_part);
+      sd->active = total > 0.0;
+      sd->total = total;
+      sd->scale = c1 * total / (out_scale * sc->dr * dzg);
+      sd->c1 = c1;
+      sd->dzg = dzg;
+    }
     // charge / total * nb in bin units: the fixed-point integers times nb / sum
     qs = red[0] ? (float)((double)nb / (double)(long long)red[0]) : 0.0f;
     la = __float2bfloat16_rn((float)log(dzg / sc->dr));
   }
   __syncthreads();
   if (!red[0]) return;
-  for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += gridDim.x * blockDim.x) {
     x[k] = __float2bfloat16_rn(fixed_to_float(t.bin_fx[k]) * qs);
     x[nb + k] = la;
   }
@@ -194,9 +199,10 @@ __device__ inline bool solve3(const double *m, const double *y, double *c) {
   const double det = a * c00 + b * c01 + d * c02;
   if (!(fabs(det) > 1e-12 * fabs(a * e * g) && a > 0.0)) return false;
   const double c11 = a * g - d * d, c12 = b * d - a * f, c22 = a * e - b * b;
-  c[0] = (c00 * y[0] + c01 * y[1] + c02 * y[2]) / det;
-  c[1] = (c01 * y[0] + c11 * y[1] + c12 * y[2]) / det;
-  c[2] = (c02 * y[0] + c12 * y[1] + c22 * y[2]) / det;
+  const double inv = 1.0 / det;  // one FP64 divide (each costs about a microsecond)
+  c[0] = (c00 * y[0] + c01 * y[1] + c02 * y[2]) * inv;
+  c[1] = (c01 * y[0] + c11 * y[1] + c12 * y[2]) * inv;
+  c[2] = (c02 * y[0] + c12 * y[1] + c22 * y[2]) * inv;
   return true;
 }
 
@@ -263,7 +269,11 @@ __global__ void __launch_bounds__(kFitBlock) k_sur_fit(ScState *sc, SurDev *sd, 
   }
   block_sum(red, r);
   if (threadIdx.x != 0) return;
-  const double res = r[1] > 0.0 ? sqrt(r[0] / r[1]) : (r[0] > 0.0 ? 1.0 : 0.0);
+  // the ratio in FP32 (the test needs a few digits; FP64 divide and square
+  // root take microseconds on this GPU)
+  const bool f32 = r[1] > 1e-30 && r[1] < 1e30 && r[0] < 1e30;
+  const double res = r[1] > 0.0 ? (f32 ? (double)sqrtf((float)r[0] / (float)r[1]) : sqrt(r[0] / r[1]))
+                                 : (r[0] > 0.0 ? 1.0 : 0.0);
   const bool ok = res <= tol;
   sd->residual = res;
   if (ok) sd->n_accepted += 1;
@@ -307,8 +317,8 @@ SurNet::~SurNet() {
 void sur_solve(const DevBeam &bm, ScState *sc, const ScTables &t, const ScKickArgs &a, const SurNet &n,
                cudaStream_t st) {
   SurDev *sd = (SurDev *)n.d;
-  k_sur_input<<<1, 1024, 0, st>>>(sc, t, sd, (__nv_bfloat16 *)n.x, n.nr, n.nz, n.out_scale, bm.n,
-                                  a.current * a.frac / bm.mass);
+  k_sur_input<<<kInBlocks, kSurBlock, 0, st>>>(sc, t, sd, (__nv_bfloat16 *)n.x, n.nr, n.nz, n.out_scale, bm.n,
+                                               a.current * a.frac / bm.mass);
   const void *cur = n.x;
   for (size_t l = 0; l < n.arch.size(); ++l) {
     const int32_t *dims = n.dims.data() + 7 * l;

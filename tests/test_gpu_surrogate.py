@@ -192,7 +192,7 @@ def test_accepted_surrogate_field_has_the_plain_boundary():
         assert np.allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
 
 
-def test_shipped_network_against_the_plain_solver():
+def test_shipped_network_against_the_plain_solver(oracle):
     """The shipped network (hpsim_gb300/data) inside FP64 small-FODO tracking
     at 65,536 particles, against the plain solver on the same beam, at the
     residual tolerance 0.02 and with every field accepted: most kicks take
@@ -214,6 +214,7 @@ def test_shipped_network_against_the_plain_solver():
         beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=65536, precision="fp64")
         beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 777)
         beam.set_ref_w(0.75)
+        beam.set_ref_phi(0.0)  # as the oracle's run does
         beam.save_initial_beam()
         sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
         sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()), sc)
@@ -230,6 +231,12 @@ def test_shipped_network_against_the_plain_solver():
             times.append(sim.last_time_ms())
         res[tol] = (mon, float(np.median(times[1:])), sc.surrogate_stats() if tol is not None else None)
     plain, t_plain, _ = res[None]
+    # the FP64 oracle on the same beam: the plain path agrees to rounding, so
+    # the surrogate's errors below are its errors against the oracle too
+    mon_o, _ = oracle.run(L.small_fodo(), 65536, spch_args=(32, 128, 0.10, 0), seed=777)
+    assert np.array_equal(plain[:, 0], mon_o[:, 0])
+    for i in (6, 11, 16):
+        assert np.max(np.abs(plain[:, i] / mon_o[:, i] - 1.0)) <= 1e-6
     for tol in (0.02, 1e30):
         mon, t, st = res[tol]
         msg = f"tol {tol}: accepted/fell back {st[:2]}, {t:.2f} ms vs plain {t_plain:.2f} ms (gain {t_plain / t:.3f})"
