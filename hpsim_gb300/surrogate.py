@@ -239,7 +239,7 @@ def make_target(field, nr, nz, dr, dzg, c1, total):
 def snapshots(n_runs=48, num=32768, seed=1, precision="fp64", elems=None):
     """(inputs [S, 2, nz, nr], targets [S, 2, nz, nr]) from plain-SCHEFF kicks
     of small-FODO runs with currents U(5, 25) mA and emittance scales
-    U(0.5, 2) (the survey's recipe), one snapshot per element."""
+    U(0.5, 2), one snapshot per element."""
     from . import HPSim, lattices as L
     rng = np.random.default_rng(seed)
     elems = elems or L.small_fodo()

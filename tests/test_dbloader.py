@@ -11,8 +11,10 @@ import pytest
 
 from hpsim_gb300 import HPSim, dbloader, lattices as L
 
-REF_DB = "/root/reference/db"
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference tree's lattice databases, beside this repository (or named by
+# HPS_REFERENCE_DB); the tests that read them are skipped where it is absent
+REF_DB = os.environ.get("HPS_REFERENCE_DB", os.path.join(HERE, "..", "..", "reference", "db"))
 
 TABLES = {
     "linac": "view_index INTEGER, name TEXT, model_type TEXT, model_index INTEGER",
