@@ -209,6 +209,19 @@ def scan_lattice(sb: ScanBeam, aperture=0.0):
     return out
 
 
+def partition_beams(nums, ranks):
+    """Beam indices per rank, balanced by particle count: the largest beams
+    first, each to the rank with the fewest particles so far (ties to the
+    lower rank); every beam goes to exactly one rank."""
+    load = [0] * ranks
+    out = [[] for _ in range(ranks)]
+    for i in sorted(range(len(nums)), key=lambda k: (-nums[k], k)):
+        r = min(range(ranks), key=lambda q: (load[q], q))
+        out[r].append(i)
+        load[r] += nums[i]
+    return [sorted(o) for o in out]
+
+
 def ccl_batch(n_beams=16, num=1 << 20, seed=805):
     """Beams of the CCL-like lattice with perturbed set points: RF amplitude
     scale U(0.99, 1.01), RF phase offset U(-1, +1) deg and quad-gradient

@@ -72,3 +72,50 @@ def test_reference_arm_prints_once_under_torchrun():
     assert d["impl"] == "reference" and d["n_gpus"] == 2
     assert d["value"] > 0 and d["e2e"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_partition_beams_balances_and_covers():
+    from hpsim_gb300 import lattices as L
+    nums = [b.num for b in L.batched_scan(256)]
+    for ranks in (1, 2, 3, 4, 8):
+        parts = L.partition_beams(nums, ranks)
+        assert sorted(i for p in parts for i in p) == list(range(len(nums)))
+        loads = [sum(nums[i] for i in p) for p in parts]
+        assert max(loads) - min(loads) <= max(nums)  # greedy largest-first bound
+    assert L.partition_beams([5, 5, 5, 5], 2) == [[0, 2], [1, 3]]
+
+
+def _part_rank(rank, ws, port, q):
+    import torch
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    from hpsim_gb300 import lattices as L
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=ws)
+    try:
+        nums = [b.num for b in L.batched_scan(64)]
+        mine = L.partition_beams(nums, ws)[rank]
+        # every beam counted once over the ranks; particles add up to the batch
+        seen = torch.zeros(len(nums), dtype=torch.int64)
+        seen[mine] = 1
+        dist.all_reduce(seen)
+        tot = torch.tensor([sum(nums[i] for i in mine)], dtype=torch.int64)
+        dist.all_reduce(tot)
+        q.put((rank, seen.tolist(), int(tot.item()), sum(nums)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_batch_partition_across_gloo_ranks():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_part_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for _, seen, tot, want in out:
+        assert all(s == 1 for s in seen) and tot == want
