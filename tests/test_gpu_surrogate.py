@@ -246,3 +246,50 @@ def test_shipped_network_against_the_plain_solver(oracle):
             assert np.max(np.abs(mon[:, i] / plain[:, i] - 1.0)) <= bound, (i, msg)
         assert t <= 1.15 * t_plain, msg
         print(msg)
+
+
+def test_malformed_network_is_refused():
+    """A layer table whose channels do not chain, or whose last layer does
+    not give two channels on the mesh, is rejected with an error and leaves
+    no network attached."""
+    from hpsim_gb300 import HPSim, surrogate as S
+    from hpsim_gb300._capi import HPSimError, call
+    sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
+    ex = S.export(_zero_state())
+    n = len(ex["weights"])
+    wp = (C.c_void_p * n)(*[w.ctypes.data for w in ex["weights"]])
+    bp = (C.c_void_p * n)(*[b.ctypes.data for b in ex["biases"]])
+    skip = np.ascontiguousarray(ex["skip"], np.int32)
+    for bad in ("chain", "last"):
+        arch = np.array(ex["arch"], np.int32)
+        if bad == "chain":
+            arch[3, 0] = 64          # layer 3 does not read layer 2's 128 channels
+        else:
+            arch[-1, 1] = 3          # three output channels
+        with pytest.raises(HPSimError):
+            call("hps_scheff_set_surrogate", sc.handle, n, arch.reshape(-1).ctypes.data_as(C.POINTER(C.c_int)),
+                 int(ex["gmean_after"]), skip.ctypes.data_as(C.POINTER(C.c_int)), wp, bp, 32, 128,
+                 1.0, 0.02, 64)
+    with pytest.raises(HPSimError):
+        sc.surrogate_stats()         # nothing attached
+
+
+def test_fp32_beams_ignore_the_surrogate():
+    """FP32 beams keep the plain FP32 solve with a network attached: results
+    bit-identical to the run without it."""
+    from hpsim_gb300 import HPSim, lattices as L
+    mons = []
+    for state in (None, _zero_state()):
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=16384, precision="fp32")
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 4242)
+        beam.set_ref_w(0.75)
+        sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
+        sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()), sc)
+        if state is not None:
+            sc.set_surrogate(state, tol=1e30)
+        sim.enable_monitor(True)
+        sim.simulate()
+        mons.append(sim.monitor.copy())
+        if state is not None:
+            assert sc.surrogate_stats()[:2] == (0, 0)
+    assert np.array_equal(mons[0], mons[1])
