@@ -89,3 +89,22 @@ def test_field_f32_64x256_against_fp64():
     bins = np.round(q * 2 ** 20) / 2 ** 20
     mesh = np.array([2.0e-4, 1.0e-4, 0.43, 805.0, 1048576, 1.6e-5, 0.0])
     _close_per_component(field_f32(nr, nz, bins.ravel(), mesh), field(nr, nz, bins.ravel(), mesh), 2e-5)
+
+
+def test_field_table_64x256_against_oracle(oracle):
+    """The 64 x 256 mesh in FP64 (single-copy table tiles of 16 source
+    radii): random charges against the oracle's Green's table and
+    contraction."""
+    import ctypes as C
+    rng = np.random.default_rng(4)
+    nr, nz = 64, 256
+    bins = np.ascontiguousarray(rng.uniform(0.0, 5.0, nr * nz) * (rng.uniform(size=nr * nz) > 0.3))
+    mesh = np.array([2.0e-4, 1.0e-4, 0.43, 805.0, 1048576, 1.6e-5, 0.0])
+    f = field(nr, nz, bins, mesh)
+    s = oracle.Scheff(nr, nz, 0.01, 0)
+    s.s.dr, s.s.dz = mesh[0], mesh[1]
+    oracle.lib().orc_scheff_green_table(s.h, mesh[2], mesh[3], int(mesh[4]), mesh[5], int(mesh[6]))
+    C.memmove(s.s.bin, bins.ctypes.data, bins.nbytes)
+    oracle.lib().orc_scheff_contract(s.h)
+    _, _, ref = s.tables()
+    assert np.allclose(f, ref, rtol=1e-9, atol=1e-12 * np.abs(ref).max())
