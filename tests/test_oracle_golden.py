@@ -132,3 +132,21 @@ def test_first_simulate_keeps_the_engine_state_of_its_creation(oracle):
     if R.available():
         mr, _ = R.run(elems, 500, seed=5, late=True)
         assert mr[0, 18] == 0.0 and np.allclose(mr[0], m1[0], rtol=1e-10, atol=0.0)
+
+
+def test_oracle_against_reference_build_ccl_64x256(oracle):
+    """The large configuration's mesh and elements: CCL gaps at 805 MHz from
+    100 MeV, a doublet and a drift, SCHEFF 64 x 256 with a solve at every
+    element, 2048 particles -- the oracle against the reference's own code."""
+    from oracle import refimpl as R
+    if not R.available():
+        pytest.skip("reference build (oracle/_ref) not present on this machine")
+    from hpsim_gb300 import lattices as L
+    elems = L.ccl_like(modules=1, tanks=1, cells=2)
+    kw = dict(seed=9, w0=100.0, freq=805.0, twiss=L.waterbag_twiss(w0=100.0, freq=805.0))
+    mr, cr = R.run(elems, 2048, spch=dict(nr=64, nz=256, remesh_threshold=0.0), **kw)
+    mo, co = oracle.run(elems, 2048, spch_args=(64, 256, 0.01, 0), spch_set={"remesh_threshold": 0.0}, **kw)
+    assert np.array_equal(cr["loss"], co["loss"])
+    for k in G.COORDS:
+        assert np.allclose(cr[k], co[k], rtol=1e-10, atol=1e-12 * np.abs(co[k]).max()), k
+    assert G.monitor_close(mo, mr, 1e-7).all()
