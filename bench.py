@@ -173,9 +173,24 @@ def describe(args, n_elem):
     elif args.workload == "ccl_large":
         lat = f"ccl_large: 4 x 32 x 8 CCL gaps at 805 MHz from 100 MeV, doublets between tanks ({n_elem} elements)"
     else:
-        lat = f"dtl_like: {args.gaps} DTL gaps + {args.gaps + 1} quads"
+        lat = (f"dtl_like: {args.gaps} DTL gaps (E0 2.5 MV/m, phi_s -26 deg, T(beta) and S(beta) cubics in "
+               f"u = (beta - beta_g)/beta_g with coefficients drawn +-5% about (0.85, 0.40, -1.2, 0.5) and "
+               f"(0.10, -0.10, 0.3, -0.1)) + {args.gaps + 1} quads of 0.04 m at +-80 T/m (not +-45 T/m: at "
+               f"+-45 T/m the 15 mA beam is lost within the first tank)")
     return (f"{lat}, {args.particles} H- particles, waterbag {spec['w0']} MeV, SCHEFF {nr}x{nz} full solve at "
             f"every element")
+
+
+def beam_flags(beam):
+    """loss and lloss flags of every particle (host copies)."""
+    import numpy as np
+    from hpsim_gb300._capi import call, uptr
+    out = []
+    for k in (0, 1):
+        a = np.empty(beam.get_size(), dtype=np.uint32)
+        call("hps_beam_get_loss", beam.handle, k, uptr(a))
+        out.append(a)
+    return out
 
 
 def make_sim(args, elems, seed):
@@ -253,30 +268,39 @@ def load_traffic(phase, prec, n):
         return None
 
 
-def cpu_baseline(args, elems, budget_s=12.0, min_s=10.0, impl_kind="port"):
+def oracle_sim(args, elems, seed=12345):
+    """The FP64 oracle's beam and simulator for the workload (waterbag of the
+    same seed as the GPU beam of rank 0; set-up is not timed)."""
+    from hpsim_gb300 import lattices as L
+    from oracle import oracle as O
+    types, params, _ = L.lattice_arrays(elems)
+    spec = WORKLOADS[args.workload]
+    b = O.Beam(args.particles)
+    b.set_waterbag(L.waterbag_twiss(w0=spec["w0"], freq=spec["freq"]), 0.0, spec["w0"], spec["freq"], seed)
+    b.set_ref_w(spec["w0"])
+    b.set_ref_phi(0.0)
+    sp = O.Scheff(*spec["mesh"], spec["interval"], 0)
+    sp.set(remesh_threshold=0.0)
+    return b, O.Sim(b, types, params, sp)
+
+
+def cpu_baseline(args, elems, budget_s=12.0, min_s=10.0, impl_kind="port", keep_first=False):
     """The FP64 oracle (oracle/, OpenMP over all host cores) on a bounded
     sample of the same workload at the same particle count: passes of the
     lattice from a fresh beam, element by element, until at least min_s of
     oracle time (at most budget_s; a long lattice stops inside its first
-    pass).  Beam setup is not timed."""
-    import numpy as np  # noqa: F401
-    from hpsim_gb300 import lattices as L
+    pass).  Beam setup is not timed.  keep_first: the first pass's monitor
+    records and final loss flags are returned too (key "first"), when that
+    pass covered the whole lattice."""
     from oracle import oracle as O
     O.build()
     threads = os.cpu_count() or 1
     O.lib().orc_set_threads(threads)
-    types, params, _ = L.lattice_arrays(elems)
-    spec = WORKLOADS[args.workload]
     done = passes = 0
     dt = 0.0
-    while dt < min_s:
-        b = O.Beam(args.particles)
-        b.set_waterbag(L.waterbag_twiss(w0=spec["w0"], freq=spec["freq"]), 0.0, spec["w0"], spec["freq"], 12345)
-        b.set_ref_w(spec["w0"])
-        b.set_ref_phi(0.0)
-        sp = O.Scheff(*spec["mesh"], spec["interval"], 0)
-        sp.set(remesh_threshold=0.0)
-        sim = O.Sim(b, types, params, sp)
+    first = None
+    while True:  # at least one pass
+        b, sim = oracle_sim(args, elems)
         t0 = time.perf_counter()
         stopped = False
         for i in range(len(elems)):
@@ -287,37 +311,102 @@ def cpu_baseline(args, elems, budget_s=12.0, min_s=10.0, impl_kind="port"):
                 break
         dt += time.perf_counter() - t0
         passes += 1
-        if stopped or dt > budget_s:
+        if keep_first and passes == 1 and not stopped:
+            first = (sim.mon.copy(), b.arr("loss").copy(), b.arr("lloss").copy())
+        if stopped or dt > budget_s or dt >= min_s:
             break
     what = (f"{passes} passes of all {len(elems)} elements" if done == passes * len(elems)
             else f"the first {done} of {len(elems)} elements" if passes == 1
             else f"{done} element steps over {passes} passes of {len(elems)} elements")
-    return {"value": args.particles * done / dt, "unit": METRIC, "cores": threads, "kind": impl_kind,
-            "sample": f"{args.particles} particles x {what}, FP64 oracle, {dt:.1f} s"}
+    out = {"value": args.particles * done / dt, "unit": METRIC, "cores": threads, "kind": impl_kind,
+           "sample": f"{args.particles} particles x {what}, FP64 oracle, {dt:.1f} s",
+           "whole_passes": done == passes * len(elems)}
+    if keep_first:
+        out["first"] = first
+    return out
+
+
+# monitor columns (include/hps_layout.h): centroid -> its sigma, sigmas,
+# emittances, synchronous particle
+MON_CENTROIDS = {2: 3, 4: 5, 7: 8, 9: 10, 12: 13, 14: 15}
+MON_SIGMAS = (3, 5, 8, 10, 13, 15)
+MON_EMITS = {"eps_x": 6, "eps_y": 11, "eps_z": 16}
+EMIT_GATE = 1e-3
+
+
+def accuracy(mon, ref, loss, ref_loss, lloss, ref_lloss):
+    """Per-element agreement of a GPU pass with the FP64 oracle's pass of the
+    same beam: transmission (particles alive after every element), loss and
+    longitudinal-loss flags of every particle, and the largest relative
+    error over the elements of the emittances, the rms sizes, the centroids
+    (in units of their rms size) and particle 0's energy and phase.  The
+    gate: emittances within 1e-3 relative, transmission and flags exact."""
+    import numpy as np
+    m, r = np.asarray(mon, float), np.asarray(ref, float)
+
+    def rel(a, b):
+        ok = np.abs(b) > 0
+        if not ok.any():
+            return 0.0, -1
+        e = np.zeros(len(b))
+        e[ok] = np.abs(a[ok] - b[ok]) / np.abs(b[ok])
+        k = int(np.argmax(e))
+        return float(e[k]), k
+
+    err, at = {}, {}
+    for name, col in MON_EMITS.items():
+        err[name], at[name] = rel(np.nan_to_num(m[:, col]), np.nan_to_num(r[:, col]))
+    err["sigma"] = max(rel(m[:, c], r[:, c])[0] for c in MON_SIGMAS)
+    cen = 0.0
+    for a, sc in MON_CENTROIDS.items():
+        sig = np.abs(r[:, sc])
+        ok = sig > 0
+        if ok.any():
+            cen = max(cen, float(np.max(np.abs(m[ok, a] - r[ok, a]) / sig[ok])))
+    err["centroid_over_sigma"] = cen
+    err["w0"] = rel(m[:, 17], r[:, 17])[0]
+    err["phi0"] = rel(m[:, 18], r[:, 18])[0]
+    out = {"transmission_equal": bool(np.array_equal(m[:, 0], r[:, 0])),
+           "good_count_equal": bool(np.array_equal(m[:, 1], r[:, 1])),
+           "loss_flags_equal": bool(np.array_equal(loss, ref_loss)),
+           "lloss_equal": bool(np.array_equal(lloss, ref_lloss)),
+           "transmitted": int(m[-1, 0]), "elements": int(len(m)),
+           "max_rel_err": err, "worst_element": at}
+    out["gate"] = {"emittance_rel_max": EMIT_GATE,
+                   "pass": bool(out["transmission_equal"] and out["loss_flags_equal"] and out["lloss_equal"]
+                                and max(err[k] for k in MON_EMITS) <= EMIT_GATE)}
+    return out
 
 
 def run_reference(args):
+    """The reference's CPU path (the FP64 oracle, all host cores) on the same
+    workload: each step is one whole pass of the lattice over the full beam
+    when the warm-up pass shows it takes at most 8 s, else a prefix of the
+    lattice bounded to 8 s whose time is scaled to the whole lattice."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     elems = workload(args)
-    per_step = 4.0
+    per_step = 8.0
     for _ in range(args.warmup):
-        cpu_baseline(args, elems, budget_s=per_step / 4, min_s=per_step / 4)
-    vals, times = [], []
+        cpu_baseline(args, elems, budget_s=per_step, min_s=0.0)
+    vals, times, prefix = [], [], False
+    r = None
     for _ in range(args.steps):
-        r = cpu_baseline(args, elems, budget_s=per_step, min_s=per_step)
+        r = cpu_baseline(args, elems, budget_s=per_step, min_s=0.0)
         vals.append(r["value"])
         times.append(args.particles * len(elems) / r["value"])
+        prefix |= not r["whole_passes"]
     v = args.steps / sum(1.0 / x for x in vals)
+    note = " (time scaled from bounded prefixes of the lattice)" if prefix else ""
     line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": describe(args, len(elems)) + " (time extrapolated from bounded prefixes)",
-                       "particles": args.particles, "elements": len(elems)},
+            "config": {"workload": describe(args, len(elems)) + note,
+                       "particles": args.particles, "elements": len(elems), "precision": "fp64"},
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": r["cores"], "kind": "port",
-                             "sample": r["sample"]},
+                             "sample": f"{args.steps} steps, each {r['sample']}"},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -353,6 +442,8 @@ def run_batched(args):
     w0, freq = spec["w0"], spec["freq"]
     # with N ranks each GPU takes its share of the beams, balanced by particle
     # count; the beams are independent, so no collective touches the data
+    if ws > len(scan):
+        raise SystemExit(f"--beams {len(scan)} is fewer than the {ws} ranks: every rank needs at least one beam")
     mine = L.partition_beams([sb.num for sb in scan], ws)[rank]
     all_total = sum(sb.num for sb in scan)
     scan = [scan[i] for i in mine]
@@ -578,11 +669,23 @@ def main():
         e2e = {"value": te_value, "unit": METRIC, "h2d_bytes_per_step": n * (6 * 8 + 4 + 4),
                "d2h_bytes_per_step": n * (6 * 8 + 4)}
 
+    # one more (untimed) pass from the initial beam with per-element records,
+    # for the accuracy check against the FP64 oracle's pass of the same beam
+    mon_gpu = monitored()
+    loss_gpu, lloss_gpu = beam_flags(beam)
+
     if rank != 0:
         return
-    cpu = None
+    cpu = acc = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, elems)
+        cpu = cpu_baseline(args, elems, keep_first=True)
+        first = cpu.pop("first")
+        if first is not None:
+            acc = accuracy(mon_gpu, first[0], loss_gpu, first[1], lloss_gpu, first[2])
+            acc["oracle"] = "FP64 oracle, same waterbag seed and lattice, one whole pass"
+        else:
+            acc = {"skipped": "the oracle's first pass did not cover the whole lattice within its time bound"}
+        cpu.pop("whole_passes", None)
     ck = clocks.summary()
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
@@ -607,6 +710,8 @@ def main():
         "gpu_launches": int(launches),
         "clocks": ck,
     }
+    if acc is not None:
+        line["accuracy"] = acc
     if sur:
         line["surrogate"] = sur
     print(json.dumps(line), flush=True)

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <array>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,29 @@ namespace hps {
 void note_launch(int n = 1);
 // record the message returned by hps_last_error() and pass the status through
 int set_error(int status, const char *msg);
+
+// Kernel attributes (the dynamic shared-memory limit above 48 KB) belong to
+// the device that was current when they were set.  PerDevice runs a set-up
+// once on every device the process uses, with that device current; a
+// device index beyond the table runs it at every call.
+constexpr int kMaxDevices = 64;
+struct PerDevice {
+  std::mutex m;
+  bool done[kMaxDevices] = {};
+  template <class F>
+  void once(F &&f) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+      f();
+      return;
+    }
+    std::lock_guard<std::mutex> lock(m);
+    if (!done[dev]) {
+      f();
+      done[dev] = true;
+    }
+  }
+};
 
 // ---- beam reductions and small beam kernels (beam_ops.cu) -------------
 void beam_update_loss(const DevBeam &b, PassScratch s, cudaStream_t st);

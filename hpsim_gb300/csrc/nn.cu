@@ -409,8 +409,8 @@ size_t conv_smem(int cpr, int split) {
 template <int S, int U>
 void conv_launch(const ConvShape &s, const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *bias, int relu,
                  const __nv_bfloat16 *skip, __nv_bfloat16 *y, cudaStream_t st) {
-  static std::once_flag once;
-  std::call_once(once, [] {
+  static PerDevice configured;
+  configured.once([] {
     cudaFuncSetAttribute(k_conv_fwd<S, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
   });
   const int npix = s.Ho * s.Wo;

@@ -428,8 +428,8 @@ void sc_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs
 // tables: contract.cuh's ring-convolution kernel, grid and shared memory
 // sized for the largest mesh the solver takes
 void contract64(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max, cudaStream_t st) {
-  static std::once_flag once;
-  std::call_once(once, [] { contract_configure<double>(); });
+  static PerDevice configured;
+  configured.once([] { contract_configure<double>(); });
   contract_launch<double>(sc, t, nx_max, nz_max, st);
 }
 
@@ -471,10 +471,18 @@ void sc_green(const ScState *sc, const ScTables &t, uint32_t num_part, double cu
   note_launch();
 }
 
+// the limit only grows, per device (the attribute is per device)
 void sc_configure(size_t max_deposit_smem) {
-  static size_t configured = 0;
-  if (max_deposit_smem <= configured) return;
-  configured = max_deposit_smem;
+  static std::mutex m;
+  static size_t configured[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_deposit_smem);
+    return;
+  }
+  std::lock_guard<std::mutex> lock(m);
+  if (max_deposit_smem <= configured[dev]) return;
+  configured[dev] = max_deposit_smem;
   cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_deposit_smem);
 }
 
@@ -506,11 +514,13 @@ bool mesh_ok(uint32_t nr, uint32_t nz) {
 // Green's table + contraction for a given charge table (UpdateFldTbl1Kernel
 // and UpdateFldTbl2KernelDouble).  sc, fx, fld1 and fld2 are device buffers
 // sized for (nr, nz); fld2 is overwritten.
-void sc_field_solve(ScState *sc, unsigned long long *fx, double *fld1, double *fld2, uint32_t nr, uint32_t nz,
-                    const double *bins_dev, const double *mesh, cudaStream_t st) {
+// Returns the status of the field table's clearing or of the launches.
+cudaError_t sc_field_solve(ScState *sc, unsigned long long *fx, double *fld1, double *fld2, uint32_t nr, uint32_t nz,
+                           const double *bins_dev, const double *mesh, cudaStream_t st) {
   k_field_setup<<<1, 1, 0, st>>>(sc, nr, nz, mesh[0], mesh[1], mesh[2], mesh[3], (uint32_t)mesh[6]);
   k_bins_to_fixed<<<64, kBlock, 0, st>>>(bins_dev, fx, nr * nz);
-  cudaMemsetAsync(fld2, 0, (size_t)(nz + 1) * (nr + 1) * 2 * sizeof(double), st);
+  const cudaError_t me = cudaMemsetAsync(fld2, 0, (size_t)(nz + 1) * (nr + 1) * 2 * sizeof(double), st);
+  if (me != cudaSuccess) return me;
   ScTables t{};
   t.bin_fx = fx;
   t.fld1 = fld1;
@@ -518,6 +528,7 @@ void sc_field_solve(ScState *sc, unsigned long long *fx, double *fld1, double *f
   k_green<<<2 * 152, kBlock, 0, st>>>(sc, t, (uint32_t)mesh[4], mesh[5]);
   contract64(sc, t, nr, nz, st);
   note_launch(4);
+  return cudaGetLastError();
 }
 
 }  // namespace hps
@@ -542,10 +553,7 @@ hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const 
   if (e == cudaSuccess) e = cudaMalloc((void **)&f2, n2 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(sc, 0, sizeof(ScState));
   if (e == cudaSuccess) e = cudaMemcpy(b, bins, nb * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) {
-    sc_field_solve(sc, fx, f1, f2, nr, nz, b, mesh, 0);
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess) e = sc_field_solve(sc, fx, f1, f2, nr, nz, b, mesh, 0);
   if (e == cudaSuccess) e = cudaMemcpy(field, f2, n2 * sizeof(double), cudaMemcpyDeviceToHost);
   cudaFree(sc); cudaFree(fx); cudaFree(b); cudaFree(f1); cudaFree(f2);
   if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
@@ -577,13 +585,14 @@ static_assert(sizeof(ScState) <= kNoAllocStateBytes, "ScState outgrew its slot i
 // state block | fixed-point charge table | Green's table
 static __device__ __align__(256) unsigned char g_field_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void *g_scratch_addr[kMaxDevices];  // device address of g_field_scratch, per device
 
 // Device address of the scratch array on the current device.  The symbol's
 // name is only a host-side handle: the address has to be asked for once per
-// device, with that device current.
+// device, with that device current.  The cached address belongs to the
+// device's current context: after cudaDeviceReset the library has to be
+// reloaded before this entry point is used on that device again.
 int scratch_address(void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -623,6 +632,11 @@ hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins
     return (hps_status)set_error(HPS_ERR_INVALID,
                                  "scheff_field_noalloc: mesh too large for the static scratch "
                                  "(limit nr*nz <= 4096 and (nr+1)*nr*nz <= 135168, e.g. 32 x 128)");
+  // an error left pending by earlier work is the caller's, not this call's
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess)
+    return (hps_status)set_error(HPS_ERR_CUDA, (std::string("scheff_field_noalloc: an earlier CUDA error is "
+                                                            "pending: ") + cudaGetErrorString(pending)).c_str());
   void *base = nullptr;
   int st = scratch_address(&base);
   if (st != HPS_OK) return (hps_status)st;
@@ -630,8 +644,7 @@ hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins
   ScState *sc = (ScState *)p;
   unsigned long long *fx = (unsigned long long *)(p + kNoAllocStateBytes);
   double *fld1 = (double *)(p + kNoAllocStateBytes + kNoAllocMaxBins * sizeof(unsigned long long));
-  sc_field_solve(sc, fx, fld1, field_dev, nr, nz, bins_dev, mesh, (cudaStream_t)stream);
-  cudaError_t e = cudaGetLastError();
+  const cudaError_t e = sc_field_solve(sc, fx, fld1, field_dev, nr, nz, bins_dev, mesh, (cudaStream_t)stream);
   if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
   return HPS_OK;
 }

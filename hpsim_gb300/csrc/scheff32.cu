@@ -545,11 +545,11 @@ void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
 }
 
 void sc32_configure() {
-  static bool done = false;
-  if (done) return;
-  done = true;
-  cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
-  contract_configure<float>();
+  static PerDevice configured;
+  configured.once([] {
+    cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
+    contract_configure<float>();
+  });
 }
 
 namespace {

@@ -222,7 +222,10 @@ hps_status hps_scheff_field(uint32_t nr, uint32_t nz, const double *bins, const 
  * call before any stream capture.  Limit: nr*nz <= 4096 and
  * (nr+1)*nr*nz <= 135168 (e.g. 32 x 128); larger meshes return
  * HPS_ERR_INVALID.  Calls share the array: calls that overlap on the GPU
- * race. */
+ * race.  A CUDA error already pending when the call starts is returned as
+ * HPS_ERR_CUDA before any work is issued.  The looked-up address belongs to
+ * the device's context: after cudaDeviceReset reload the library before
+ * calling this again on that device. */
 hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins_dev, const double *mesh,
                                     double *field_dev, void *stream);
 /* hps_scheff_field through the kernels FP32 beams use (FP32 Green's table

@@ -52,4 +52,7 @@ def main(db_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/db")
+    # the reference's databases: the argument, else $HPS_REFERENCE_DB, else
+    # the "reference" checkout beside this repository
+    default = os.environ.get("HPS_REFERENCE_DB", os.path.join(HERE, "..", "..", "..", "reference", "db"))
+    main(sys.argv[1] if len(sys.argv) > 1 else default)

@@ -192,17 +192,13 @@ def test_accepted_surrogate_field_has_the_plain_boundary():
         assert np.allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
 
 
-def test_shipped_network_against_the_plain_solver(oracle):
+@pytest.fixture(scope="module")
+def shipped_runs():
     """The shipped network (hpsim_gb300/data) inside FP64 small-FODO tracking
-    at 65,536 particles, against the plain solver on the same beam, at the
-    residual tolerance 0.02 and with every field accepted: most kicks take
-    the network's field, the transmission is exact, the transverse rms
-    emittances stay within 1.5e-3 of the plain run's at every element and the
-    longitudinal one within 1.5e-2 (measured: 1.0e-3 and 9.6e-3).  The time
-    of both paths is measured and the ratio carried in the messages: the
-    surrogate's kernels cost about what the FP64 Green's table and
-    contraction they replace cost (measured 0.94-0.97x of the plain path's
-    speed), so the test bounds the loss at 15%."""
+    at 65,536 particles, against the plain solver on the same beam: the
+    per-element monitor records, the median time of a pass and the
+    surrogate's counters for the plain path (key None), the residual
+    tolerance 0.02 and every field accepted (1e30)."""
     import os
     from hpsim_gb300 import HPSim, lattices as L
     path = os.path.join(os.path.dirname(HPSim.__file__), "data", "scheff_surrogate_32x128.npz")
@@ -230,6 +226,22 @@ def test_shipped_network_against_the_plain_solver(oracle):
             sim.simulate()
             times.append(sim.last_time_ms())
         res[tol] = (mon, float(np.median(times[1:])), sc.surrogate_stats() if tol is not None else None)
+    return res
+
+
+def test_shipped_network_against_the_plain_solver(oracle, shipped_runs):
+    """Regression bounds of the shipped network (not its accuracy gate, see
+    the next test): at the residual tolerance 0.02 and with every field
+    accepted, most kicks take the network's field, the transmission is
+    exact, the transverse rms emittances stay within 1.5e-3 of the plain
+    run's at every element and the longitudinal one within 1.5e-2
+    (measured: 1.0e-3 and 9.6e-3).  The time of both paths is measured and
+    the ratio carried in the messages: the surrogate's kernels cost about
+    what the FP64 Green's table and contraction they replace cost (measured
+    0.94-0.97x of the plain path's speed), so the test bounds the loss at
+    15%."""
+    from hpsim_gb300 import lattices as L
+    res = shipped_runs
     plain, t_plain, _ = res[None]
     # the FP64 oracle on the same beam: the plain path agrees to rounding, so
     # the surrogate's errors below are its errors against the oracle too
@@ -246,6 +258,20 @@ def test_shipped_network_against_the_plain_solver(oracle):
             assert np.max(np.abs(mon[:, i] / plain[:, i] - 1.0)) <= bound, (i, msg)
         assert t <= 1.15 * t_plain, msg
         print(msg)
+
+
+@pytest.mark.xfail(reason="the shipped 32x128 network's longitudinal emittance error is 9.6e-3 at tolerance "
+                          "0.02, above the 1e-3 gate; tightening the tolerance until it holds makes most "
+                          "kicks fall back", strict=False)
+def test_shipped_network_meets_the_emittance_gate(shipped_runs):
+    """The surrogate's own accuracy target: at the residual tolerance 0.02,
+    every rms emittance within 1e-3 relative of the plain solver's at every
+    element, with exact transmission."""
+    plain = shipped_runs[None][0]
+    mon = shipped_runs[0.02][0]
+    assert np.array_equal(mon[:, 0], plain[:, 0])
+    for i in (6, 11, 16):
+        assert np.max(np.abs(mon[:, i] / plain[:, i] - 1.0)) <= 1e-3, i
 
 
 def test_malformed_network_is_refused():

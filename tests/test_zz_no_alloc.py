@@ -77,6 +77,7 @@ def test_noalloc_source_allocates_nothing():
     src = open(os.path.join(ROOT, "hpsim_gb300", "csrc", "scheff.cu")).read()
     start = src.index("hps_status hps_scheff_field_noalloc(")
     body = src[start:src.index("}  // extern \"C\"", start)]
-    solve = src[src.index("void sc_field_solve("):src.index("}  // namespace hps", src.index("void sc_field_solve("))]
+    solve = src[src.index("cudaError_t sc_field_solve("):src.index("}  // namespace hps",
+                                                                  src.index("cudaError_t sc_field_solve("))]
     for text in (body, solve):
         assert not re.search(r"cudaMalloc|cudaFree|\bmalloc\(|\bnew\b|torch", text)
