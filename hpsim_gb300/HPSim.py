@@ -529,12 +529,21 @@ class SpaceCharge:
         self._set("remesh_threshold", v)
 
     def get_counter(self, name):
-        """Counters kept on the device (not in the reference's API): 'solves'
-        (field solves since creation) or 'stat_sweeps' (kicks of an FP32 beam
-        whose statistics took the separate loss-test and moments sweeps)."""
+        """Counters and flags kept on the device (not in the reference's API):
+        'solves' (field solves since creation), 'stat_sweeps' (kicks of an
+        FP32 beam whose statistics took the separate loss-test and moments
+        sweeps), 'tensor_cores' (1: FP32 beams' contractions run on the
+        tensor cores), 'tc_error' (1: a bounded wait of that kernel gave up)."""
         out = C.c_double()
-        call("hps_scheff_get", self._h, {"solves": 8, "stat_sweeps": 9}[name], C.byref(out))
+        call("hps_scheff_get", self._h, {"solves": 8, "stat_sweeps": 9, "tensor_cores": 11, "tc_error": 12}[name],
+             C.byref(out))
         return int(out.value)
+
+    def set_contraction(self, kernel):
+        """Contraction kernel of FP32 beams (not in the reference's API):
+        'tensor' (the default: split-BF16 tcgen05 products where the mesh
+        allows) or 'cuda' (the FP32 ring convolution on CUDA cores)."""
+        call("hps_scheff_set", self._h, 10, {"tensor": 0.0, "cuda": 1.0}[kernel])
 
     def set_surrogate(self, net, tol=0.02, n_samples=64):
         """Attach a trained field surrogate (not in the reference's API):

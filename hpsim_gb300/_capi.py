@@ -90,6 +90,7 @@ def lib():
         "hps_scheff_field": (st, [u32, u32, dp, dp, dp]),
         "hps_scheff_field_noalloc": (st, [u32, u32, vp, dp, vp, vp]),
         "hps_scheff_field_f32": (st, [u32, u32, dp, dp, dp]),
+        "hps_scheff_field_f32_kernel": (st, [u32, u32, dp, dp, dp, i32]),
         "hps_sim_create": (st, [vp, vp, vp, pvp]),
         "hps_sim_destroy": (st, [vp]),
         "hps_sim_simulate": (st, [vp, i32, i32]),

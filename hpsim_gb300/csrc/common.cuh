@@ -72,6 +72,8 @@ struct ScState {
   uint32_t n_stat_sweeps;
   // FP64 beams with a field surrogate: this kick's field came from it
   int sur_accepted;
+  // the tensor-core contraction gave up a bounded wait (stays set)
+  uint32_t tc_error;
 };
 
 // Constants of one FP32 SCHEFF kick, formed once per kick in FP32 by the
@@ -108,6 +110,12 @@ struct ScTables {
   double *fld2;                // (nz+1)*(nx+1) (x,y interleaved)
   float *ffld1, *ffld2;        // FP32 variants (FP32 beams)
   Sc32Consts *c32;             // FP32 beams: constants of the current kick
+  // FP32 beams on a tensor-core mesh (contract_tc.cuh): the folded Green's
+  // table as split-BF16 MMA tiles, the per-(tile, source radius) partial
+  // fields, and the mesh they are sized for (tcg null: no tensor-core path)
+  void *tcg;
+  float *tcp;
+  uint32_t tc_nr, tc_nz;
 };
 
 // Kinematics of the reference particle in FP32, for offset arithmetic.

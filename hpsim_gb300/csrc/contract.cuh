@@ -263,6 +263,8 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
 template <class T, bool M, int S>
 __global__ void __launch_bounds__(kContractThreads) k_contract_m(const ScState *sc, ScTables t) {
   if (!sc->remesh || sc->sur_accepted) return;
+  // FP32 tables of a tensor-core mesh: contract_tc.cuh's kernels take the solve
+  if (sizeof(T) == 4 && t.tcg && sc->nx == t.tc_nr && sc->nz == t.tc_nz) return;
   const uint32_t nx = sc->nx, nz = sc->nz;
   if (blockIdx.x > nx || blockIdx.y * kCZ * S > nz) return;
   extern __shared__ __align__(16) unsigned char contract_raw[];

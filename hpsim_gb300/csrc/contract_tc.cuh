@@ -1,0 +1,441 @@
+// contract_tc.cuh -- the SCHEFF ring-to-mesh field sum of FP32 beams on the
+// tensor cores (UpdateFldTbl2KernelDouble, src/simulation/inc/
+// space_charge_kernel.cu:472-568, launched by UpdateFinalFldTblKernelCall,
+// src/simulation/src/space_charge.cu:189-218).
+//
+// The sum E[zp][rp] = sum over bins (zs, rs) of q(zs, rs) g(rp, rs, zp - zs)
+// (g the sign-folded Green's table of contract.cuh) is, for the interior
+// points zp < nz, rp < nr, a matrix product
+//   D[zp][n] = sum over (rs, k) of A[zp][(rs, k)] B[(rs, k)][n],
+//   A[zp][(rs, k)] = q(zp - k, rs)   (zero outside the mesh),
+//   B[(rs, k)][n]  = g(rp, rs, k)    (n = 2 rp + component),
+// with k = zp - zs running over the folded range -(nz - 1) .. nz.  Each CTA
+// takes one 128-row tile of zp (the MMA's M) and one source radius rs: K =
+// the 127 + nz offsets that tile needs, in chunks of 64, N = 2 nr.
+//
+// Precision: split BF16.  Both operands are written as hi = bf16(x), lo =
+// bf16(x - hi); the three products hi*hi + hi*lo + lo*hi are accumulated in
+// FP32 in tensor memory (relative error of a product ~2^-17; measured on the
+// test meshes ~4e-6 of the largest field component against FP64).
+//
+// Data movement: the Green's kernel writes B directly as the MMA's shared-
+// memory image (K-major, 128-byte swizzle, tiles of N rows x 64 offsets,
+// hi and lo), so a 1D bulk copy (cp.async.bulk, completion on an mbarrier)
+// stages each tile.  A is a Toeplitz expansion of one charge column: row zp
+// of a chunk is a window of 64 consecutive values of the reversed,
+// zero-padded column, which the producer warps copy with 16-byte shared-
+// memory loads from 8 shifted copies of it and store swizzled.
+//
+// Warp roles (160 threads): warps 0-3 build the A tiles and issue the bulk
+// copies, then read the accumulator back (warp w owns TMEM lanes 32w..);
+// warp 4 allocates the tensor memory and one of its threads issues the MMAs
+// and commits them to the stage's "empty" barrier.  Every wait is bounded
+// (about a second); a wait that gives up sets the solver's error word, and
+// the CTA drains its copies and MMAs before it frees the tensor memory.
+//
+// The per-radius partial tiles are summed in a fixed order by
+// k_tc_reduce, whose other blocks compute the last row (zp = nz) and
+// column (rp = nr) with CUDA cores from the FP32 table: results are
+// deterministic.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace hps {
+namespace {
+
+constexpr int kTcM = 128;           // field rows per tile (MMA M)
+constexpr int kTcKC = 64;           // offsets per chunk (one 128-byte swizzle row of BF16)
+constexpr int kTcThreads = 160;     // 4 producer / epilogue warps + 1 MMA warp
+constexpr int kTcProducers = 128;
+constexpr size_t kTcSmemMax = 227 * 1024;
+
+// meshes the tensor-core path takes: nz a multiple of the tile height, N =
+// 2 nr at most 256 (one MMA) and at least 32 (the smallest tensor-memory
+// allocation), powers of two as every SCHEFF mesh
+__host__ __device__ inline bool tc_mesh_ok(uint32_t nr, uint32_t nz) {
+  return nz >= 128 && nz <= 512 && (nz & (nz - 1)) == 0 && nr >= 16 && nr <= 128 && (nr & (nr - 1)) == 0;
+}
+
+// launch shape of one mesh
+struct TcDims {
+  uint32_t nr, nz;
+  uint32_t N;        // 2 nr
+  uint32_t NC;       // chunks of the folded range (2 nz / 64)
+  uint32_t CPT;      // chunks a tile needs (nz / 64 + 2)
+  uint32_t BT;       // bytes of one B tile (N rows x 128 B)
+  uint32_t S;        // pipeline stages
+  uint32_t L;        // elements of one shifted copy of the padded charge column
+  uint32_t tiles;    // nz / 128
+  uint32_t red_blocks, edge_blocks;
+  size_t smem;       // dynamic shared memory of k_contract_tc
+};
+
+__host__ __device__ inline size_t tc_stage_bytes(uint32_t BT) { return 2 * 16384 + 2 * (size_t)BT; }
+
+inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
+  TcDims d{};
+  d.nr = nr; d.nz = nz; d.N = 2 * nr; d.NC = 2 * nz / kTcKC; d.CPT = nz / kTcKC + 2;
+  d.BT = d.N * 128; d.L = nz + 264; d.tiles = nz / kTcM;
+  const size_t fixed = 1024 + (size_t)16 * d.L * 2 + (size_t)nz * 4;
+  d.S = fixed + 3 * tc_stage_bytes(d.BT) <= kTcSmemMax ? 3 : 2;
+  d.smem = fixed + d.S * tc_stage_bytes(d.BT);
+  d.red_blocks = (nz * nr + 255) / 256;
+  d.edge_blocks = (nz + nr + 1 + 7) / 8;  // 8 warps per block, one edge point each
+  return d;
+}
+
+// bytes of the folded split-BF16 table and of the partial tiles
+inline size_t tc_table_bytes(uint32_t nr, uint32_t nz) { return (size_t)nr * (2 * nz / kTcKC) * 2 * (2 * nr) * 128; }
+inline size_t tc_partial_bytes(uint32_t nr, uint32_t nz) { return (size_t)(nz / kTcM) * nr * (2 * nr) * kTcM * 4; }
+
+// the tensor-core path runs this kick: FP32 tables sized for this mesh
+__device__ inline bool tc_go(const ScState *sc, const ScTables &t) {
+  return t.tcg != nullptr && sc->remesh && !sc->sur_accepted && sc->nx == t.tc_nr && sc->nz == t.tc_nz;
+}
+
+// byte offset of element (row r, column j) in a K-major tile with the
+// 128-byte swizzle: rows of 128 bytes, 16-byte chunks permuted by r mod 8
+__host__ __device__ inline uint32_t tc_swz(uint32_t r, uint32_t j) {
+  return (r >> 3) * 1024 + (r & 7) * 128 + ((((j >> 3) ^ (r & 7)) & 7) << 4) + ((j & 7) << 1);
+}
+
+// the Green's kernel's share: entry (rp < nr, rs, dz) of component comp
+// (value v, E_z already carrying its sign for k >= 1) at both folded
+// offsets k = dz + 1 and k = -dz (E_z negated there), hi and lo
+__device__ inline void tc_put_green(const ScTables &t, uint32_t nr, uint32_t nz, uint32_t rp, uint32_t rs,
+                                    uint32_t dz, float er, float ez) {
+  unsigned char *base = (unsigned char *)t.tcg;
+  const uint32_t NC = 2 * nz / kTcKC, BT = 2 * nr * 128;
+  const uint32_t kid[2] = {dz + nz, nz - 1 - dz};
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const uint32_t c = kid[side] / kTcKC, j = kid[side] % kTcKC;
+    unsigned char *tile = base + ((size_t)(rs * NC + c) * 2) * BT;
+#pragma unroll
+    for (int comp = 0; comp < 2; ++comp) {
+      const float v = comp == 0 ? er : (side == 0 ? ez : -ez);
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+      const uint32_t off = tc_swz(2 * rp + comp, j);
+      *(__nv_bfloat16 *)(tile + off) = hi;
+      *(__nv_bfloat16 *)(tile + BT + off) = lo;
+    }
+  }
+}
+
+// ---- PTX wrappers -----------------------------------------------------------
+__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_now() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(tc_smem(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(tc_smem(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(tc_smem(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+constexpr uint64_t kTcWaitNs = 1000000000ull;  // a wait gives up after one second
+
+// wait for the phase of the given parity; false when it gave up (or another
+// thread of the CTA already gave up: *abort set)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
+  if (mbar_test(bar, parity)) return true;
+  const uint64_t t0 = tc_now();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if ((it & 63) == 63) {
+      if (*abort) return false;
+      if (tc_now() - t0 > kTcWaitNs) {
+        *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   tc_smem(dst)),
+               "l"(src), "r"(bytes), "r"(tc_smem(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand with the 128-byte swizzle: start address, leading offset
+// (unused with this swizzle), 1024 bytes between 8-row groups, descriptor
+// version 1, swizzle mode 2
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// kind::f16 instruction: FP32 accumulator, BF16 A and B, both K-major,
+// N columns, M = 128
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// 2^-36 fixed-point charge as FP32 (two 32-bit conversions)
+__device__ __forceinline__ float tc_charge(unsigned long long v) {
+  const long long s = (long long)v;
+  return fmaf((float)(int)(s >> 32), 4294967296.0f, (float)(unsigned)(v & 0xffffffffull)) *
+         1.4551915228366852e-11f;
+}
+
+// ---- the product ------------------------------------------------------------
+// grid (tiles, nr): tile blockIdx.x of field rows, source radius blockIdx.y
+__global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc, ScTables t, TcDims d) {
+  if (!tc_go(sc, t)) return;
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ uint64_t full[3], empty[3], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t tile = blockIdx.x, rs = blockIdx.y;
+  const uint32_t N = d.N, nz = d.nz, nr = d.nr, S = d.S, BT = d.BT, L = d.L;
+  // 1024-byte aligned stage buffers, then the shifted charge copies and the column
+  unsigned char *sm = (unsigned char *)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
+  const size_t stage = tc_stage_bytes(BT);
+  __nv_bfloat16 *cp = (__nv_bfloat16 *)(sm + S * stage);  // [h][s][L]
+  float *qc = (float *)(sm + S * stage + (size_t)16 * L * 2);
+  volatile int *abort = &abort_flag;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < S; ++s) {
+      mbar_init(&full[s], kTcProducers + 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 4) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_slot)),
+                 "r"(N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc_fence_before();
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t c0 = 2 * tile, nch = d.CPT;  // this tile's chunks of the folded range
+  bool issued_mma = false;
+
+  if (warp < 4) {
+    // ---- producers: the charge column's shifted copies, then per chunk the
+    // B tiles' bulk copies and the A tiles ----
+    const uint32_t nb = nr * nz;
+    for (uint32_t zs = tid; zs < nz; zs += kTcProducers) qc[zs] = tc_charge(t.bin_fx[zs * nr + rs]);
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    // copy s, element x holds R(x + s - 128), R(v) = q(nz - 1 - v) inside the mesh
+    for (uint32_t e = tid; e < 8 * L; e += kTcProducers) {
+      const uint32_t s = e / L, x = e % L;
+      const int v = (int)x + (int)s - 128;
+      const float q = (v >= 0 && v < (int)nz) ? qc[nz - 1 - v] : 0.0f;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(q);
+      cp[s * L + x] = hi;
+      cp[(8 + s) * L + x] = __float2bfloat16_rn(q - __bfloat162float(hi));
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    (void)nb;
+    const unsigned char *gsrc = (const unsigned char *)t.tcg + (size_t)rs * d.NC * 2 * BT;
+    const uint32_t m = tid;  // the A row this thread writes
+    for (uint32_t i = 0; i < nch && !*abort; ++i) {
+      const uint32_t s = i % S, use = i / S;
+      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort)) break;
+      unsigned char *st = sm + s * stage;
+      if (tid == 0) {
+        mbar_arrive_tx(&full[s], 2 * BT);
+        const unsigned char *src = gsrc + (size_t)(c0 + i) * 2 * BT;
+        bulk_g2s(st + 2 * 16384, src, BT, &full[s]);
+        bulk_g2s(st + 2 * 16384 + BT, src + BT, BT, &full[s]);
+      }
+      // row m of the chunk: R(W .. W + 63), W = 64 i - m (+128 into the copies)
+      const int wp = 64 * (int)i - (int)m + 128;
+      const int sh = wp & 7, base = wp - sh;
+      const uint4 *hi = (const uint4 *)(cp + sh * L + base);
+      const uint4 *lo = (const uint4 *)(cp + (8 + sh) * L + base);
+      unsigned char *ah = st + (m >> 3) * 1024 + (m & 7) * 128;
+      unsigned char *al = ah + 16384;
+#pragma unroll
+      for (uint32_t jj = 0; jj < 8; ++jj) {
+        const uint32_t off = ((jj ^ (m & 7)) & 7) << 4;
+        *(uint4 *)(ah + off) = hi[jj];
+        *(uint4 *)(al + off) = lo[jj];
+      }
+      fence_async_smem();
+      mbar_arrive(&full[s]);
+    }
+  } else if (lane == 0) {
+    // ---- the MMA thread ----
+    const uint32_t idesc = tc_idesc(N);
+    for (uint32_t i = 0; i < nch; ++i) {
+      const uint32_t s = i % S, use = i / S;
+      if (!mbar_wait(&full[s], use & 1, abort)) break;
+      tc_fence_after();
+      const uint32_t a0 = tc_smem(sm + s * stage), b0 = a0 + 2 * 16384;
+      const uint64_t ah = tc_desc(a0), al = tc_desc(a0 + 16384), bh = tc_desc(b0), bl = tc_desc(b0 + BT);
+#pragma unroll
+      for (uint32_t ks = 0; ks < kTcKC / 16; ++ks) {
+        const uint64_t adv = 2 * ks;  // 32 bytes along K, in 16-byte units
+        tc_mma(tmem, ah + adv, bh + adv, idesc, (i | ks) != 0);
+        tc_mma(tmem, ah + adv, bl + adv, idesc, 1);
+        tc_mma(tmem, al + adv, bh + adv, idesc, 1);
+      }
+      issued_mma = true;
+      tc_commit(&empty[s]);
+    }
+    if (issued_mma) tc_commit(&done);
+  }
+
+  // ---- epilogue: the accumulator to this (tile, radius) partial ----
+  if (warp < 4) {
+    const bool ok = !*abort && mbar_wait(&done, 0, abort);
+    if (ok) {
+      tc_fence_after();
+      float *out = t.tcp + ((size_t)(tile * nr + rs) * N) * kTcM + 32 * warp + lane;
+      const uint32_t tl = tmem + ((32 * warp) << 16);
+      for (uint32_t c = 0; c < N; c += 16) {
+        float v[16];
+        tc_ld16(tl + c, v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) out[(size_t)(c + k) * kTcM] = v[k];
+      }
+    }
+    tc_fence_before();
+  }
+  __syncthreads();
+  if (*abort) {
+    // a wait gave up: record it, let the bulk copies and MMAs already issued
+    // land (both finish on their own within microseconds), then free the
+    // tensor memory
+    if (tid == 0) atomicOr((unsigned int *)&((ScState *)sc)->tc_error, 1u);
+    if (warp == 4 && lane == 0 && issued_mma) {
+      tc_commit(&done);
+      int dummy = 0;
+      (void)mbar_wait(&done, 0, &dummy);
+    }
+    const uint64_t t0 = tc_now();
+    while (tc_now() - t0 < 100000ull) {
+    }
+    __syncthreads();
+  }
+  if (warp == 4) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N) : "memory");
+  }
+}
+
+// The partial tiles summed over the source radii in order (blocks [0,
+// red_blocks): one thread per interior point), and the last row and column
+// of the field table from the FP32 Green's table (the other blocks: one warp
+// per point, lanes over the bins, a fixed shuffle tree).
+__global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t, TcDims d) {
+  if (!tc_go(sc, t)) return;
+  const uint32_t nr = d.nr, nz = d.nz, N = d.N, nrow = nr + 1;
+  float *out = t.ffld2;
+  if (blockIdx.x < d.red_blocks) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nz * nr) return;
+    const uint32_t rp = id / nz, zp = id % nz, tile = zp / kTcM, m = zp % kTcM;
+    const float *p = t.tcp + ((size_t)tile * nr * N + 2 * rp) * kTcM + m;
+    float ex = 0.0f, ez = 0.0f;
+    for (uint32_t g = 0; g < nr; ++g) {
+      ex += p[(size_t)g * N * kTcM];
+      ez += p[(size_t)g * N * kTcM + kTcM];
+    }
+    const size_t pt = (size_t)zp * nrow + rp;
+    out[2 * pt] = ex;
+    out[2 * pt + 1] = ez;
+    return;
+  }
+  const uint32_t e = (blockIdx.x - d.red_blocks) * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (e >= nz + nr + 1) return;
+  const uint32_t zp = e <= nr ? nz : e - (nr + 1), rp = e <= nr ? e : nr;
+  const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * nr * nz;  // [dz][rs]
+  float ax = 0.0f, az = 0.0f;
+  for (uint32_t k = lane; k < nr * nz; k += 32) {
+    const uint32_t zs = k / nr, rs = k % nr;
+    const float q = tc_charge(t.bin_fx[k]);
+    if (q == 0.0f) continue;
+    const int kk = (int)zp - (int)zs;
+    const bool below = kk >= 1;
+    const float2 g = G[(size_t)(below ? kk - 1 : -kk) * nr + rs];
+    ax = fmaf(q, g.x, ax);
+    az = fmaf(q, below ? g.y : -g.y, az);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    ax += __shfl_down_sync(0xffffffffu, ax, off);
+    az += __shfl_down_sync(0xffffffffu, az, off);
+  }
+  if (lane == 0) {
+    const size_t pt = (size_t)zp * nrow + rp;
+    out[2 * pt] = ax;
+    out[2 * pt + 1] = az;
+  }
+}
+
+inline void contract_tc_configure() {
+  cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemMax);
+}
+
+// both launches of a tensor-core solve on a mesh of nr x nz
+inline void contract_tc_launch(const ScState *sc, const ScTables &t, uint32_t nr, uint32_t nz, cudaStream_t st) {
+  const TcDims d = tc_dims(nr, nz);
+  k_contract_tc<<<dim3(d.tiles, nr), kTcThreads, d.smem, st>>>(sc, t, d);
+  k_tc_reduce<<<d.red_blocks + d.edge_blocks, 256, 0, st>>>(sc, t, d);
+}
+
+}  // namespace
+}  // namespace hps

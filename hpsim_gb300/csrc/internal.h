@@ -94,6 +94,7 @@ struct ScKickArgs {
   size_t deposit_smem;  // bytes of the per-block histogram (largest mesh)
   uint32_t nx_max, nz_max;  // largest mesh the solver's tables hold
   int adj_possible;         // adjacent bunches configured (else r_max never sizes the mesh)
+  bool mesh_fixed;          // the kick's mesh is the largest one (no mesh-size cut-off energy)
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);
@@ -194,6 +195,12 @@ void beam32_to_double(const DevBeam &b, int coord, double *out, cudaStream_t st)
 void beam32_update_stat_for_sc(const DevBeam &b, PassScratch s, cudaStream_t st);
 
 void sc32_configure();
+// the tensor-core contraction (contract_tc.cuh): meshes it takes, and the
+// bytes of its folded split-BF16 Green's table and of its partial fields
+bool sc32_tc_mesh(uint32_t nr, uint32_t nz);
+size_t sc32_tc_bytes(uint32_t nr, uint32_t nz, size_t *partial_bytes);
+void contract32(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max, bool mesh_fixed,
+                cudaStream_t st);
 void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                 cudaStream_t st);
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,

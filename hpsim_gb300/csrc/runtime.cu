@@ -90,6 +90,7 @@ struct hps_scheff_s {
   ScTables t{};
   uint64_t version = 0;
   SurNet *sur = nullptr;  // field surrogate (FP64 beams), owned
+  int contraction = 0;    // FP32 beams: 0 tensor cores where the mesh allows, 1 CUDA cores
 };
 
 struct GraphEntry {
@@ -744,14 +745,38 @@ static hps_status scheff_upload(hps_scheff_t s) {
   return HPS_OK;
 }
 
-static hps_status scheff_alloc_tables(hps_scheff_t s) {
-  if (s->t.bin_fx) cudaFree(s->t.bin_fx);
-  if (s->t.fld1) cudaFree(s->t.fld1);
-  if (s->t.fld2) cudaFree(s->t.fld2);
-  if (s->t.ffld1) cudaFree(s->t.ffld1);
-  if (s->t.ffld2) cudaFree(s->t.ffld2);
-  if (s->t.c32) cudaFree(s->t.c32);
+static void scheff_free_tables(hps_scheff_t s) {
+  void *p[] = {s->t.bin_fx, s->t.fld1, s->t.fld2, s->t.ffld1, s->t.ffld2, s->t.c32, s->t.tcg, s->t.tcp};
+  for (void *q : p)
+    if (q) cudaFree(q);
   s->t = ScTables{};
+}
+
+// the tensor-core contraction's buffers for the largest mesh (FP32 beams),
+// when that mesh allows it and the solver does not ask for CUDA cores
+static hps_status scheff_alloc_tc(hps_scheff_t s) {
+  if (s->t.tcg) cudaFree(s->t.tcg);
+  if (s->t.tcp) cudaFree(s->t.tcp);
+  s->t.tcg = nullptr;
+  s->t.tcp = nullptr;
+  s->t.tc_nr = s->t.tc_nz = 0;
+  if (s->contraction != 0 || !sc32_tc_mesh(s->nx_max, s->nz_max)) return HPS_OK;
+  size_t pb = 0;
+  const size_t gb = sc32_tc_bytes(s->nx_max, s->nz_max, &pb);
+  unsigned char *g = nullptr;
+  float *p = nullptr;
+  hps_status st;
+  if ((st = dmalloc(&g, gb))) return st;
+  if ((st = dmalloc(&p, pb / sizeof(float)))) { cudaFree(g); return st; }
+  s->t.tcg = g;
+  s->t.tcp = p;
+  s->t.tc_nr = s->nx_max;
+  s->t.tc_nz = s->nz_max;
+  return HPS_OK;
+}
+
+static hps_status scheff_alloc_tables(hps_scheff_t s) {
+  scheff_free_tables(s);
   hps_status st;
   size_t nx = s->nx_max, nz = s->nz_max;
   if ((st = dmalloc(&s->t.bin_fx, nx * nz))) return st;
@@ -760,6 +785,7 @@ static hps_status scheff_alloc_tables(hps_scheff_t s) {
   if ((st = dmalloc(&s->t.ffld1, (nx + 1) * nx * nz * 2))) return st;
   if ((st = dmalloc(&s->t.ffld2, (nz + 1) * (nx + 1) * 2))) return st;
   if ((st = dmalloc(&s->t.c32, 1))) return st;
+  if ((st = scheff_alloc_tc(s))) return st;
   sc_configure(nx * nz * sizeof(unsigned long long));
   return HPS_OK;
 }
@@ -785,12 +811,7 @@ hps_status hps_scheff_destroy(hps_scheff_t s) {
   if (!s) return HPS_OK;
   cudaDeviceSynchronize();
   if (s->d) cudaFree(s->d);
-  if (s->t.bin_fx) cudaFree(s->t.bin_fx);
-  if (s->t.fld1) cudaFree(s->t.fld1);
-  if (s->t.fld2) cudaFree(s->t.fld2);
-  if (s->t.ffld1) cudaFree(s->t.ffld1);
-  if (s->t.ffld2) cudaFree(s->t.ffld2);
-  if (s->t.c32) cudaFree(s->t.c32);
+  scheff_free_tables(s);
   delete s->sur;
   delete s;
   return HPS_OK;
@@ -806,6 +827,15 @@ hps_status hps_scheff_set(hps_scheff_t s, int param, double v) {
     case 3: s->mesh_w = v; break;
     case 4: s->remesh_val = v; break;
     case 5: s->fraction = v; break;
+    case 10: {
+      if (v != 0.0 && v != 1.0) return fail(HPS_ERR_INVALID, "scheff_set: contraction kernel is 0 or 1");
+      if ((int)v == s->contraction) return HPS_OK;
+      CK(cudaDeviceSynchronize());
+      s->contraction = (int)v;
+      hps_status st = scheff_alloc_tc(s);
+      if (st) return st;
+      break;
+    }
     default: return fail(HPS_ERR_INVALID, "scheff_set: unknown or read-only parameter");
   }
   return scheff_upload(s);
@@ -822,13 +852,16 @@ hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
     case 6: *v = s->nx; break;
     case 7: *v = s->nz; break;
     case 8:
-    case 9: {  // counters kept by the kernels
+    case 9:
+    case 12: {  // counters and flags kept by the kernels
       ScState h;
       if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(&h, s->d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
         return fail(HPS_ERR_CUDA, "scheff_get: reading the solver state failed");
-      *v = param == 8 ? (double)h.n_solves : (double)h.n_stat_sweeps;
+      *v = param == 8 ? (double)h.n_solves : param == 9 ? (double)h.n_stat_sweeps : (double)h.tc_error;
       break;
     }
+    case 10: *v = s->contraction; break;
+    case 11: *v = s->t.tcg != nullptr; break;
     default: return fail(HPS_ERR_INVALID, "scheff_get: unknown parameter");
   }
   return HPS_OK;
@@ -965,6 +998,7 @@ ScKickArgs kick_args(Ctx &c, double length) {
   a.nx_max = c.sc->nx_max;
   a.nz_max = c.sc->nz_max;
   a.adj_possible = c.sc->adj_bunch != 0;
+  a.mesh_fixed = c.sc->mesh_w == 0.0 && c.sc->nx == c.sc->nx_max && c.sc->nz == c.sc->nz_max;
   return a;
 }
 

@@ -44,6 +44,7 @@
 #include "reduce.cuh"
 #include "sc32_kick.cuh"
 #include "contract.cuh"
+#include "contract_tc.cuh"
 #include "green32.cuh"
 #include "sc32_stats.cuh"
 #include "scheff_common.cuh"
@@ -278,6 +279,8 @@ __device__ void green_blocks(const ScState *sc, const ScTables &t, uint32_t bid,
   const float dr = k.dr0, dzg = k.dzg0, pl = k.pl, c1 = k.green_c1;
   const uint32_t adj = sc->adj;
   float2 *out = (float2 *)t.ffld1;
+  // a tensor-core mesh also gets the folded split-BF16 MMA tiles (rp < nr)
+  const bool tc = t.tcg != nullptr && nr == t.tc_nr && nz == t.tc_nz;
   for (uint32_t e = bid * blockDim.x + threadIdx.x; e < total; e += nblk * blockDim.x) {
     uint32_t tz = e % nz;
     uint32_t kk = (e / nz) % nrs;
@@ -292,7 +295,9 @@ __device__ void green_blocks(const ScState *sc, const ScTables &t, uint32_t bid,
       g.ez += g1.ez + g2.ez;
     }
     // stored [rp][dz][rs] (rs fastest) for the contraction's lanes
-    out[((size_t)rpi * nz + tz) * nr + kk] = make_float2(c1 * g.er, c1 * g.ez);
+    const float2 v = make_float2(c1 * g.er, c1 * g.ez);
+    out[((size_t)rpi * nz + tz) * nr + kk] = v;
+    if (tc && rpi < nr) tc_put_green(t, nr, nz, rpi, kk, tz, v.x, v.y);
   }
 }
 
@@ -529,8 +534,7 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   ngreen = (ngreen + kDepCluster - 1) / kDepCluster * kDepCluster;
   launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
   note_launch();
-  contract_launch<float>(sc, u, a.nx_max, a.nz_max, st);
-  note_launch();
+  contract32(sc, u, a.nx_max, a.nz_max, a.mesh_fixed, st);
 }
 
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st) {
@@ -549,7 +553,32 @@ void sc32_configure() {
   configured.once([] {
     cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
     contract_configure<float>();
+    contract_tc_configure();
   });
+}
+
+bool sc32_tc_mesh(uint32_t nr, uint32_t nz) { return tc_mesh_ok(nr, nz); }
+size_t sc32_tc_bytes(uint32_t nr, uint32_t nz, size_t *partial_bytes) {
+  *partial_bytes = tc_partial_bytes(nr, nz);
+  return tc_table_bytes(nr, nz);
+}
+
+// UpdateFldTbl2KernelDouble for FP32 tables: the tensor-core kernels when
+// the solver holds their buffers for the largest mesh it takes, the FP32
+// ring convolution otherwise.  Each returns at once when the other one is
+// the one for the kick's mesh; mesh_fixed (the kick's mesh is the largest
+// one, decided on the host) leaves out the one that cannot run.
+void contract32(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max, bool mesh_fixed,
+                cudaStream_t st) {
+  const bool tc = t.tcg != nullptr && t.tc_nr == nx_max && t.tc_nz == nz_max;
+  if (tc) {
+    contract_tc_launch(sc, t, nx_max, nz_max, st);
+    note_launch(2);
+  }
+  if (!tc || !mesh_fixed) {
+    contract_launch<float>(sc, t, nx_max, nz_max, st);
+    note_launch();
+  }
 }
 
 namespace {
@@ -579,20 +608,29 @@ __global__ void k32_bins_to_fixed(const double *bins, unsigned long long *fx, ui
 extern "C" {
 
 // UpdateTblsKernelCall (Green's table) + UpdateFinalFldTblKernelCall with the
-// FP32 kernels, on a caller-given charge table
-hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field) {
+// FP32 kernels, on a caller-given charge table; kernel: 0 the one FP32 beams
+// use for the mesh, 1 the FP32 ring convolution, 2 the tensor cores
+hps_status hps_scheff_field_f32_kernel(uint32_t nr, uint32_t nz, const double *bins, const double *mesh,
+                                       double *field, int kernel) {
   using namespace hps;
   if (!bins || !mesh || !field) return (hps_status)set_error(HPS_ERR_INVALID, "scheff_field_f32: null pointer");
   if (!nr || !nz || (nr & (nr - 1)) || (nz & (nz - 1)) || nz > 512 || nr > 256)
     return (hps_status)set_error(HPS_ERR_INVALID,
                                  "scheff_field_f32: nr and nz must be powers of two, nz <= 512, nr <= 256");
+  if (kernel < 0 || kernel > 2) return (hps_status)set_error(HPS_ERR_INVALID, "scheff_field_f32: unknown kernel");
+  if (kernel == 2 && !tc_mesh_ok(nr, nz))
+    return (hps_status)set_error(HPS_ERR_UNSUPPORTED,
+                                 "scheff_field_f32: the tensor-core contraction takes nz in 128..512 and nr in "
+                                 "16..128 (powers of two)");
+  const bool tc = kernel == 2 || (kernel == 0 && tc_mesh_ok(nr, nz));
   sc32_configure();
   size_t nb = (size_t)nr * nz, n1 = (size_t)(nr + 1) * nr * nz * 2, n2 = (size_t)(nz + 1) * (nr + 1) * 2;
   ScState *sc = nullptr;
   Sc32Consts *c32 = nullptr;
   unsigned long long *fx = nullptr;
   double *b = nullptr;
-  float *f1 = nullptr, *f2 = nullptr;
+  float *f1 = nullptr, *f2 = nullptr, *tcp = nullptr;
+  void *tcg = nullptr;
   std::vector<float> host(n2);
   cudaError_t e = cudaMalloc((void **)&sc, sizeof(ScState));
   if (e == cudaSuccess) e = cudaMalloc((void **)&c32, sizeof(Sc32Consts));
@@ -600,10 +638,13 @@ hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, co
   if (e == cudaSuccess) e = cudaMalloc((void **)&b, nb * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc((void **)&f1, n1 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void **)&f2, n2 * sizeof(float));
+  if (e == cudaSuccess && tc) e = cudaMalloc(&tcg, tc_table_bytes(nr, nz));
+  if (e == cudaSuccess && tc) e = cudaMalloc((void **)&tcp, tc_partial_bytes(nr, nz));
   if (e == cudaSuccess) e = cudaMemset(sc, 0, sizeof(ScState));
   if (e == cudaSuccess) e = cudaMemset(c32, 0, sizeof(Sc32Consts));
   if (e == cudaSuccess) e = cudaMemset(f2, 0, n2 * sizeof(float));
   if (e == cudaSuccess) e = cudaMemcpy(b, bins, nb * sizeof(double), cudaMemcpyHostToDevice);
+  uint32_t tc_error = 0;
   if (e == cudaSuccess) {
     k32_field_setup<<<1, 1>>>(sc, c32, nr, nz, mesh[0], mesh[1], mesh[2], mesh[3], mesh[4], mesh[5],
                               (uint32_t)mesh[6]);
@@ -613,16 +654,30 @@ hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, co
     t.ffld1 = f1;
     t.ffld2 = f2;
     t.c32 = c32;
+    if (tc) {
+      t.tcg = tcg;
+      t.tcp = tcp;
+      t.tc_nr = nr;
+      t.tc_nz = nz;
+    }
     k32_green<<<4 * 152, kBlock>>>(sc, t);
-    contract_launch<float>(sc, t, nr, nz, 0);
-    note_launch(4);
+    note_launch(3);
+    contract32(sc, t, nr, nz, true, 0);
     e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&tc_error, &sc->tc_error, 4, cudaMemcpyDeviceToHost);
   }
   if (e == cudaSuccess) e = cudaMemcpy(host.data(), f2, n2 * sizeof(float), cudaMemcpyDeviceToHost);
   cudaFree(sc); cudaFree(c32); cudaFree(fx); cudaFree(b); cudaFree(f1); cudaFree(f2);
+  if (tcg) cudaFree(tcg);
+  if (tcp) cudaFree(tcp);
   if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
+  if (tc_error) return (hps_status)set_error(HPS_ERR_TIMEOUT, "scheff_field_f32: a tensor-core wait gave up");
   for (size_t k = 0; k < n2; ++k) field[k] = host[k];
   return HPS_OK;
+}
+
+hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field) {
+  return hps_scheff_field_f32_kernel(nr, nz, bins, mesh, field, 0);
 }
 
 }  // extern "C"

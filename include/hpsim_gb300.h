@@ -193,7 +193,12 @@ hps_status hps_scheff_destroy(hps_scheff_t s);
  *            4 remesh_threshold, 5 fraction, 6 nr, 7 nz (6/7 read-only);
  * read-only counters since creation: 8 field solves (remeshes), 9 kicks of an
  * FP32 beam whose statistics took the separate loss-test and moments sweeps
- * (the element map before the kick could not certify them) */
+ * (the element map before the kick could not certify them).
+ * No reference counterpart: 10 the contraction kernel of FP32 beams (0, the
+ * default: split-BF16 tensor cores where the mesh allows -- nz a power of
+ * two in 128..512, nr in 16..128 -- else the FP32 ring convolution; 1: the
+ * ring convolution always); read-only: 11 the solver holds the tensor-core
+ * buffers, 12 a bounded wait of the tensor-core kernel gave up (1). */
 hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
 hps_status hps_scheff_get(hps_scheff_t s, int param, double *value);
 /* the solver's tables after its last kick (no reference counterpart): charge
@@ -233,6 +238,15 @@ hps_status hps_scheff_field_noalloc(uint32_t nr, uint32_t nz, const double *bins
  * counterpart in the reference: it exposes the FP32 solver's table stage so
  * that its error against the FP64 table can be stated. */
 hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, const double *mesh, double *field);
+/* hps_scheff_field_f32 with the contraction kernel chosen: 0 the one FP32
+ * beams use for the mesh (the tensor cores where the mesh allows), 1 the
+ * FP32 ring convolution on CUDA cores, 2 the split-BF16 tensor-core product
+ * (tcgen05; nz a power of two in 128..512, nr in 16..128, else
+ * HPS_ERR_UNSUPPORTED).  Same computation as UpdateFinalFldTblKernelCall,
+ * src/simulation/src/space_charge.cu:189-218; the kernel choice has no
+ * counterpart in the reference. */
+hps_status hps_scheff_field_f32_kernel(uint32_t nr, uint32_t nz, const double *bins, const double *mesh,
+                                       double *field, int kernel);
 
 /* ---- Simulator (src/simulation/inc/simulation_engine.h) ----------------- */
 /* SimulationEngine::InitEngine, simulation_engine.cpp:408-427 (scheff may be NULL) */

@@ -112,6 +112,46 @@ def test_fp32_ccl_matches_oracle(oracle):
     assert_fp32_close(mon, mo, "ccl")
 
 
+def test_fp32_ccl_64x256_tensor_cores_match_oracle(oracle):
+    """The large configuration's shape: FP32 push, CCL gaps at 805 MHz from
+    100 MeV, SCHEFF 64 x 256 at every element with the contraction on the
+    tensor cores, against the FP64 oracle: loss flags exact, statistics at
+    every element within the stated tolerances; the solver ran its
+    tensor-core kernels and no bounded wait gave up."""
+    from hpsim_gb300 import lattices as L
+    elems = L.ccl_like(modules=1, tanks=2)
+    mon, c, objs = run_gpu(elems, 16384, spch=dict(nr=64, nz=256), w0=100.0, freq=805.0, precision="fp32")
+    sc = objs[2]
+    assert sc.get_counter("tensor_cores") == 1 and sc.get_counter("tc_error") == 0
+    mo, co = oracle.run(elems, 16384, spch_args=(64, 256, 0.01, 0), w0=100.0, freq=805.0)
+    assert np.array_equal(c["loss"], co["loss"])
+    assert np.array_equal(c["lloss"], co["lloss"])
+    assert_fp32_close(mon, mo, "ccl 64x256")
+
+
+def test_fp32_contraction_kernels_agree():
+    """The same FP32 DTL run with the contraction on the tensor cores and on
+    CUDA cores: identical loss flags, statistics within the FP32 tolerances
+    of each other."""
+    from hpsim_gb300 import HPSim, lattices as L
+    mons, losses = [], []
+    for kernel in ("tensor", "cuda"):
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=16384, precision="fp32")
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 31)
+        beam.set_ref_w(0.75)
+        beam.set_ref_phi(0.0)
+        sc = HPSim.SpaceCharge(32, 128)
+        sc.set_contraction(kernel)
+        assert sc.get_counter("tensor_cores") == (kernel == "tensor")
+        sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.dtl_like(n_gaps=40)), sc)
+        sim.enable_monitor(True)
+        sim.simulate()
+        mons.append(sim.monitor.copy())
+        losses.append(beam._loss(0))
+    assert np.array_equal(losses[0], losses[1])
+    assert_fp32_close(mons[0], mons[1], "tensor vs cuda cores")
+
+
 def test_fp32_graph_replay_is_bit_identical():
     from hpsim_gb300 import lattices as L
     elems = L.small_fodo()

@@ -108,3 +108,53 @@ def test_field_table_64x256_against_oracle(oracle):
     oracle.lib().orc_scheff_contract(s.h)
     _, _, ref = s.tables()
     assert np.allclose(f, ref, rtol=1e-9, atol=1e-12 * np.abs(ref).max())
+
+
+def field_f32_kernel(nr, nz, bins, mesh, kernel):
+    from hpsim_gb300._capi import call, dptr
+    out = np.zeros((nz + 1) * (nr + 1) * 2)
+    call("hps_scheff_field_f32_kernel", nr, nz, dptr(np.ascontiguousarray(bins)), dptr(np.ascontiguousarray(mesh)),
+         dptr(out), kernel)
+    return out
+
+
+def _bunched(nr, nz, sz=0.12, sr=0.25):
+    r = (np.arange(nr) + 0.5) / nr
+    zz = (np.arange(nz) + 0.5) / nz - 0.5
+    q = np.exp(-(zz[:, None] / sz) ** 2 - (r[None, :] / sr) ** 2) * 2 * np.pi * r[None, :] * 5000
+    return (np.round(q * 2 ** 20) / 2 ** 20).ravel()
+
+
+@pytest.mark.parametrize("nr,nz", [(16, 128), (32, 128), (32, 256), (64, 256), (128, 512)])
+def test_tensor_core_contraction_against_fp64(nr, nz):
+    """The split-BF16 tcgen05 contraction (kernel 2) on bunched and random
+    charge tables: within 2e-5 of the largest field component of the FP64
+    table stage, and within 2e-5 of the FP32 CUDA-core contraction (kernel
+    1), on every mesh shape the tensor-core path takes."""
+    mesh = np.array([2.0e-4, 1.0e-4, 0.43, 805.0, 1048576, 1.6e-5, 0.0])
+    rng = np.random.default_rng(nr + nz)
+    for bins in (_bunched(nr, nz), rng.uniform(0.0, 5.0, nr * nz) * (rng.uniform(size=nr * nz) > 0.3)):
+        tc = field_f32_kernel(nr, nz, bins, mesh, 2)
+        cuda = field_f32_kernel(nr, nz, bins, mesh, 1)
+        _close_per_component(tc, field(nr, nz, bins, mesh), 2e-5)
+        _close_per_component(tc, cuda, 2e-5)
+        assert np.array_equal(tc, field_f32_kernel(nr, nz, bins, mesh, 2))  # deterministic
+
+
+def test_tensor_core_contraction_adjacent_bunches():
+    """32 x 128 with adjacent-bunch images in the Green's table."""
+    nr, nz = 32, 128
+    mesh = np.array([4.0e-4, 2.0e-4, 0.05, 201.25, 65536, 1.6e-5, 2.0])
+    bins = _bunched(nr, nz, 0.15, 0.3)
+    _close_per_component(field_f32_kernel(nr, nz, bins, mesh, 2), field(nr, nz, bins, mesh), 2e-5)
+
+
+def test_tensor_core_contraction_rejects_other_meshes():
+    from hpsim_gb300._capi import HPSimError
+    mesh = np.array([2.0e-4, 1.0e-4, 0.43, 805.0, 1048576, 1.6e-5, 0.0])
+    for nr, nz in ((8, 64), (8, 128), (32, 64)):
+        with pytest.raises(HPSimError):
+            field_f32_kernel(nr, nz, np.ones(nr * nz), mesh, 2)
+        # the default kernel takes the FP32 ring convolution there
+        _close_per_component(field_f32_kernel(nr, nz, np.ones(nr * nz), mesh, 0),
+                             field(nr, nz, np.ones(nr * nz), mesh), 2e-5)
