@@ -547,10 +547,11 @@ class SpaceCharge:
 
     def set_surrogate(self, net, tol=0.02, n_samples=64):
         """Attach a trained field surrogate (not in the reference's API):
-        `net` is a surrogate.Network or its saved state (dict / npz).  FP64
-        beams' kicks on the network's mesh then take the network's field when
-        its relative residual against the plain sum at n_samples spot points
-        is <= tol, and the plain contraction otherwise."""
+        `net` is a surrogate.Network or its saved state (dict / npz).  Kicks
+        on the network's mesh (FP64 and FP32 beams) then take the network's
+        field when its relative residual against the plain sum at n_samples
+        spot points is <= tol, and the plain Green's table and contraction
+        otherwise."""
         from . import surrogate
         ex = surrogate.export(net.state() if hasattr(net, "state") else net)
         n = len(ex["weights"])

@@ -41,6 +41,8 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace hps {
@@ -79,7 +81,8 @@ inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
   TcDims d{};
   d.nr = nr; d.nz = nz; d.N = 2 * nr; d.NC = 2 * nz / kTcKC; d.CPT = nz / kTcKC + 2;
   d.BT = d.N * 128; d.L = nz + 264; d.tiles = nz / kTcM;
-  const size_t fixed = 1024 + (size_t)16 * d.L * 2 + (size_t)nz * 4;
+  // 256 bytes are left for the kernel's static shared memory (barriers)
+  const size_t fixed = 1024 + (size_t)16 * d.L * 2 + (size_t)nz * 4 + 256;
   d.S = fixed + 3 * tc_stage_bytes(d.BT) <= kTcSmemMax ? 3 : 2;
   d.smem = fixed + d.S * tc_stage_bytes(d.BT);
   d.red_blocks = (nz * nr + 255) / 256;
@@ -426,8 +429,13 @@ __global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t
   }
 }
 
-inline void contract_tc_configure() {
-  cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemMax);
+// the dynamic shared-memory limit of the largest mesh the path takes (static
+// and dynamic shared memory together stay within the 227 KB a CTA may have)
+inline cudaError_t contract_tc_configure() {
+  size_t most = 0;
+  for (uint32_t nr = 16; nr <= 128; nr *= 2)
+    for (uint32_t nz = 128; nz <= 512; nz *= 2) most = std::max(most, tc_dims(nr, nz).smem);
+  return cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
 }
 
 // both launches of a tensor-core solve on a mesh of nr x nz

@@ -137,10 +137,11 @@ struct SurNet {
 int sur_build(SurNet &n, int n_layers, const int32_t *arch, int gmean_after, const int32_t *skip,
               const uint16_t *const *weights, const float *const *biases, uint32_t nr, uint32_t nz, double out_scale,
               double tol, uint32_t n_samples, std::string &err);
-// after the deposit of an FP64 kick: the network's field, checked at spot
-// points, accepted into the field table or left to the contraction
+// after the deposit of a kick: the network's field, checked at spot points,
+// accepted into the field table (the FP32 one with fp32 != 0) or left to the
+// contraction
 void sur_solve(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, const SurNet &n,
-               cudaStream_t st);
+               cudaStream_t st, int fp32 = 0);
 int sur_read(const SurNet &n, double *accepted, double *rejected, double *residual);
 
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
@@ -204,7 +205,7 @@ void contract32(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t 
 void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                 cudaStream_t st);
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
-               cudaStream_t st);
+               cudaStream_t st, const SurNet *sur = nullptr);
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
 // the statistics after a PUSH_SCSTATS map that could not certify its own:
 // the longitudinal-loss test and the SCHEFF moments in one sweep, repeated

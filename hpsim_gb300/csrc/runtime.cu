@@ -1052,11 +1052,11 @@ void sc_apply(Ctx &c, double length, bool fused = false) {
     sc32_configure();
     if (fused) {
       PHASE(HPS_PROF_SC_STATS, sc32_stats_after_push(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
-      PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+      PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur));
       return;
     }
     PHASE(HPS_PROF_SC_STATS, sc32_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
-    PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
+    PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur));
     PHASE(HPS_PROF_SC_KICK, sc32_kick(b->d, c.sc->d, c.sc->t, a, b->stream));
     return;
   }

@@ -302,7 +302,7 @@ __device__ void green_blocks(const ScState *sc, const ScTables &t, uint32_t bid,
 }
 
 __global__ void k32_green(const ScState *sc, ScTables t) {
-  if (!sc->remesh) return;
+  if (!sc->remesh || sc->sur_accepted) return;
   green_blocks(sc, t, blockIdx.x, gridDim.x);
 }
 
@@ -510,7 +510,7 @@ void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, con
 }
 
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
-               cudaStream_t st) {
+               cudaStream_t st, const SurNet *sur) {
   ScTables u = tables32(t);
   if (a.adj_possible) {  // the mesh is sized from r_max only with adjacent bunches
     launch_pass_f(Op32AdjMesh{b, sc, u.c32, sc32_host(b, a)}, b.n, s, st);
@@ -532,8 +532,21 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   uint32_t ngreen = std::min<uint32_t>(
       (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 152u);
   ngreen = (ngreen + kDepCluster - 1) / kDepCluster * kDepCluster;
-  launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
-  note_launch();
+  if (sur) {
+    // field surrogate: the deposit alone, the network and its check, then
+    // the Green's table and the contraction, which return at once when the
+    // network's field was accepted
+    if (ndep) {
+      launch_k(k32_green_deposit, dim3(ndep), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, 0u);
+      note_launch();
+    }
+    sur_solve(b, sc, u, a, *sur, st, 1);
+    k32_green<<<ngreen, kBlock, 0, st>>>(sc, u);
+    note_launch();
+  } else {
+    launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
+    note_launch();
+  }
   contract32(sc, u, a.nx_max, a.nz_max, a.mesh_fixed, st);
 }
 
@@ -553,7 +566,8 @@ void sc32_configure() {
   configured.once([] {
     cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
     contract_configure<float>();
-    contract_tc_configure();
+    const cudaError_t e = contract_tc_configure();
+    if (e != cudaSuccess) set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
   });
 }
 

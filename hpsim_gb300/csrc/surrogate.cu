@@ -1,7 +1,7 @@
-// surrogate.cu -- the learned SCHEFF field surrogate inside an FP64 beam's
-// space-charge kick, with a spot-solve residual check and fallback to the
-// plain contraction.  Launch sequence of a kick that remeshes (after the
-// deposit, before the FP64 Green's table and the contraction):
+// surrogate.cu -- the learned SCHEFF field surrogate inside a beam's
+// space-charge kick (FP64 or FP32 tables), with a spot-solve residual check
+// and fallback to the plain contraction.  Launch sequence of a kick that
+// remeshes (after the deposit, before the Green's table and the contraction):
 //   k_sur_input   charge / total and log cell aspect as the network input
 //                 (BF16), the field scale, the acceptance flag cleared;
 //   the network   its 3x3 convolution layers (nn.cu) with the skip additions
@@ -41,7 +41,7 @@ struct SurDev {
   int active;          // this kick is the surrogate's to try
   double total;        // charge on the mesh (bin units)
   double scale;        // field = network output * scale
-  double c1, dzg;      // Green's-table scale, bunch-frame cell length
+  double c1, dzg, dr;  // Green's-table scale, bunch-frame cell length, radial cell size
   double residual;     // relative residual of the last check
   double cf[6];        // field = output * (cf0 + cf1 z + cf2 r) for E_r, cf3.. for E_z
   uint32_t n_accepted, n_rejected;
@@ -79,9 +79,11 @@ __device__ inline void spot_point(uint32_t k, uint32_t nr, uint32_t nz, uint32_t
 // kInBlocks blocks: each sums the whole charge table (a few microseconds of
 // loads, not worth a second launch) and normalises its share; block 0
 // records the kick's scalars
+// fp32: the kick of an FP32 beam (mesh and Green's-table scale from the FP32
+// kick constants, as the FP32 Green's table takes them)
 __global__ void __launch_bounds__(kSurBlock) k_sur_input(ScState *sc, ScTables t, SurDev *sd, __nv_bfloat16 *x,
                                                          uint32_t nr, uint32_t nz, double out_scale,
-                                                         uint32_t num_part, double cur_ov_mc2) {
+                                                         uint32_t num_part, double cur_ov_mc2, int fp32) {
   __shared__ unsigned long long red[kSurBlock];
   __shared__ int go;
   __shared__ float qs;
@@ -107,19 +109,37 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_input(ScState *sc, ScTables t
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double dzg = sc->dz * rsqrt(1.0 - sc->beta * sc->beta);
-    if (blockIdx.x == 0) {
-      const double total = (double)(long long)red[0] * kBinInvScale;
-      const double c1 = 5721.67 * cur_ov_mc2 / (sc->freq * 1e6 * (double)num_part);
-      sd->active = total > 0.0;
-      sd->total = total;
-      sd->scale = c1 * total / (out_scale * sc->dr * dzg);
-      sd->c1 = c1;
-      sd->dzg = dzg;
+    if (fp32) {
+      // FP32 arithmetic throughout (an FP64 divide costs about a microsecond)
+      const Sc32Consts &k = *t.c32;
+      const float dr = k.dr0, dzg = k.dzg0, c1 = k.green_c1;
+      if (blockIdx.x == 0) {
+        const float total = (float)(long long)red[0] * 1.4551915228366852e-11f;  // 2^-36
+        sd->active = total > 0.0f;
+        sd->total = total;
+        sd->scale = c1 * total / ((float)out_scale * dr * dzg);
+        sd->c1 = c1;
+        sd->dzg = dzg;
+        sd->dr = dr;
+      }
+      qs = red[0] ? (float)nb / (float)(long long)red[0] : 0.0f;
+      la = __float2bfloat16_rn(logf(dzg / dr));
+    } else {
+      const double dzg = sc->dz * rsqrt(1.0 - sc->beta * sc->beta);
+      if (blockIdx.x == 0) {
+        const double total = (double)(long long)red[0] * kBinInvScale;
+        const double c1 = 5721.67 * cur_ov_mc2 / (sc->freq * 1e6 * (double)num_part);
+        sd->active = total > 0.0;
+        sd->total = total;
+        sd->scale = c1 * total / (out_scale * sc->dr * dzg);
+        sd->c1 = c1;
+        sd->dzg = dzg;
+        sd->dr = sc->dr;
+      }
+      // charge / total * nb in bin units: the fixed-point integers times nb / sum
+      qs = red[0] ? (float)((double)nb / (double)(long long)red[0]) : 0.0f;
+      la = __float2bfloat16_rn((float)log(dzg / sc->dr));
     }
-    // charge / total * nb in bin units: the fixed-point integers times nb / sum
-    qs = red[0] ? (float)((double)nb / (double)(long long)red[0]) : 0.0f;
-    la = __float2bfloat16_rn((float)log(dzg / sc->dr));
   }
   __syncthreads();
   if (!red[0]) return;
@@ -141,7 +161,7 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_spot(const ScState *sc, const
   uint32_t zp, rp;
   spot_point(blockIdx.x, nr, nz, sc->n_solves, zp, rp);
   const uint32_t nb = nr * nz;
-  const float dr = (float)sc->dr, dzg = (float)sd->dzg;
+  const float dr = (float)sd->dr, dzg = (float)sd->dzg;
   const float rpf = (float)rp * dr;
   float ax = 0.0f, az = 0.0f;
   for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) {
@@ -282,11 +302,12 @@ __global__ void __launch_bounds__(kFitBlock) k_sur_fit(ScState *sc, SurDev *sd, 
   sc->sur_accepted = ok;
 }
 
-// an accepted field into the field table: the corrected network field inside,
-// the spot-solved values on the last row and column
+// an accepted field into the field table (the FP32 table of an FP32 beam):
+// the corrected network field inside, the spot-solved values on the last row
+// and column
 __global__ void __launch_bounds__(kSurBlock) k_sur_write(const ScState *sc, ScTables t, const SurDev *sd,
                                                          const __nv_bfloat16 *out, const double2 *spot, uint32_t nr,
-                                                         uint32_t nz) {
+                                                         uint32_t nz, int fp32) {
   if (!sd->active || !sc->sur_accepted) return;
   const uint32_t nrow = nr + 1, nb = nr * nz;
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,7 +321,8 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_write(const ScState *sc, ScTa
   } else {
     e = spot[zp == nz ? rp : nr + 1 + zp];
   }
-  ((double2 *)t.fld2)[p] = e;
+  if (fp32) ((float2 *)t.ffld2)[p] = make_float2((float)e.x, (float)e.y);
+  else ((double2 *)t.fld2)[p] = e;
 }
 
 }  // namespace
@@ -315,10 +337,10 @@ SurNet::~SurNet() {
 }
 
 void sur_solve(const DevBeam &bm, ScState *sc, const ScTables &t, const ScKickArgs &a, const SurNet &n,
-               cudaStream_t st) {
+               cudaStream_t st, int fp32) {
   SurDev *sd = (SurDev *)n.d;
   k_sur_input<<<kInBlocks, kSurBlock, 0, st>>>(sc, t, sd, (__nv_bfloat16 *)n.x, n.nr, n.nz, n.out_scale, bm.n,
-                                               a.current * a.frac / bm.mass);
+                                               a.current * a.frac / bm.mass, fp32);
   const void *cur = n.x;
   for (size_t l = 0; l < n.arch.size(); ++l) {
     const int32_t *dims = n.dims.data() + 7 * l;
@@ -333,7 +355,7 @@ void sur_solve(const DevBeam &bm, ScState *sc, const ScTables &t, const ScKickAr
   k_sur_fit<<<1, kFitBlock, 0, st>>>(sc, sd, out, (const double2 *)n.spot, n.nr, n.nz, n.n_samples, n.tol);
   const uint32_t nf = (n.nz + 1) * (n.nr + 1);
   k_sur_write<<<(nf + kSurBlock - 1) / kSurBlock, kSurBlock, 0, st>>>(sc, t, sd, out, (const double2 *)n.spot,
-                                                                      n.nr, n.nz);
+                                                                      n.nr, n.nz, fp32);
   note_launch(4);
 }
 

@@ -329,8 +329,11 @@ hps_status hps_nn_adam(float *w, void *w_bf16, const float *g, float *m, float *
 /* FP32 <-> BF16 (to_bf16: 1 FP32 -> BF16, 0 BF16 -> FP32) */
 hps_status hps_nn_convert(const void *src, void *dst, int64_t n, int to_bf16, void *stream);
 
-/* Attach a trained field network to a solver (FP64 beams; FP32 beams keep
- * the plain path).  Host arrays: arch[5*l..] = {c_in, c_out, stride, up,
+/* Attach a trained field network to a solver (FP64 and FP32 beams; the
+ * network's field goes into the table of the beam's precision).  No
+ * counterpart in the reference: it stands in for UpdateTblsKernelCall +
+ * UpdateFinalFldTblKernelCall inside Scheff::Start,
+ * src/simulation/src/space_charge.cpp:130-133.  Host arrays: arch[5*l..] = {c_in, c_out, stride, up,
  * relu} per layer (first c_in = 2, last c_out = 2, output on nz x nr);
  * gmean_after = the layer whose output gets its plane mean added (-1 none);
  * skip[l] = the earlier layer whose output layer l adds (-1 none);
@@ -340,8 +343,8 @@ hps_status hps_nn_convert(const void *src, void *dst, int64_t n, int to_bf16, vo
  * remeshes on an nr x nz mesh without adjacent bunches evaluates it, solves
  * the plain sum (Green's function in FP32) at the last row and column and at
  * n_samples interior points, and keeps the network's field when its
- * relative residual there is <= tol; else the FP64 Green's table and the
- * plain contraction run.  Replaces an attached network. */
+ * relative residual there is <= tol; else the Green's table and the plain
+ * contraction of the beam's precision run.  Replaces an attached network. */
 hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int32_t *arch, int32_t gmean_after,
                                     const int32_t *skip, const uint16_t *const *weights, const float *const *biases,
                                     uint32_t nr, uint32_t nz, double out_scale, double tol, uint32_t n_samples);

@@ -137,9 +137,9 @@ def _zero_state():
     return st
 
 
-def _fodo_sim(n, state=None, tol=0.5, graph=True):
+def _fodo_sim(n, state=None, tol=0.5, graph=True, precision="fp64"):
     from hpsim_gb300 import HPSim, lattices as L
-    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=n, precision="fp64")
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=n, precision=precision)
     beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 4242)
     beam.set_ref_w(0.75)
     sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
@@ -300,11 +300,13 @@ def test_malformed_network_is_refused():
         sc.surrogate_stats()         # nothing attached
 
 
-def test_fp32_beams_ignore_the_surrogate():
-    """FP32 beams keep the plain FP32 solve with a network attached: results
-    bit-identical to the run without it."""
+def test_fp32_rejected_network_leaves_the_plain_path():
+    """FP32 beams with a network attached whose every field is rejected
+    (tolerance 0): every kick falls back, and the results are bit-identical
+    to the run without a network (the deposit, Green's table and
+    contraction are the same kernels, launched apart)."""
     from hpsim_gb300 import HPSim, lattices as L
-    mons = []
+    mons, coords = [], []
     for state in (None, _zero_state()):
         beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=16384, precision="fp32")
         beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 4242)
@@ -312,10 +314,35 @@ def test_fp32_beams_ignore_the_surrogate():
         sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
         sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()), sc)
         if state is not None:
-            sc.set_surrogate(state, tol=1e30)
+            sc.set_surrogate(state, tol=0.0)
         sim.enable_monitor(True)
         sim.simulate()
         mons.append(sim.monitor.copy())
+        coords.append(beam._coord("xp"))
         if state is not None:
-            assert sc.surrogate_stats()[:2] == (0, 0)
+            acc, rej, _ = sc.surrogate_stats()
+            assert acc == 0 and rej > 0
     assert np.array_equal(mons[0], mons[1])
+    assert np.array_equal(coords[0], coords[1])
+
+
+def test_fp32_accepted_surrogate_field_has_the_plain_boundary():
+    """FP32 beams, every field accepted: the FP32 field table holds the
+    network's interior (zero here) and the spot-solved plain sum on the last
+    row and column, equal to the plain FP32 solve's values there."""
+    from hpsim_gb300._capi import call
+    fields = []
+    for state in (None, _zero_state()):
+        beam, sc, sim = _fodo_sim(16384, state, tol=1e30, graph=False, precision="fp32")
+        sim.simulate(0, 1)
+        bins, field, mesh = np.empty(32 * 128), np.empty(129 * 33 * 2), np.empty(7)
+        call("hps_scheff_snapshot", sc.handle, 1, bins.ctypes.data_as(C.POINTER(C.c_double)),
+             field.ctypes.data_as(C.POINTER(C.c_double)), mesh.ctypes.data_as(C.POINTER(C.c_double)))
+        assert mesh[6] == 1
+        fields.append(field.reshape(129, 33, 2))
+        if state is not None:
+            assert sc.surrogate_stats()[:2] == (1, 0)
+    plain, sur = fields
+    assert np.all(sur[:128, :32] == 0.0)
+    for got, ref in ((sur[128, :], plain[128, :]), (sur[:, 32], plain[:, 32])):
+        assert np.allclose(got, ref, rtol=1e-4, atol=1e-5 * np.abs(ref).max())
