@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--precision", default=None, choices=["fp32", "fp64"])
     p.add_argument("--particles", type=int, default=None)
     p.add_argument("--gaps", type=int, default=GAPS)
+    p.add_argument("--elements", type=int, default=None,
+                   help="single-beam workloads: keep only the lattice's first N elements (short profiling runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--workload", default="dtl_like",
@@ -58,6 +60,10 @@ def parse():
                    help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
                         "(a network file; default the shipped 32x128 network), and report both")
     p.add_argument("--surrogate-tol", type=float, default=0.02)
+    p.add_argument("--surrogate-batch", type=int, default=8,
+                   help="dtl_like on one GPU: also time this many set-point-perturbed beams of the same size in one "
+                        "batch launch, without and with the learned field surrogate, and report the ratio to the "
+                        "plain single-beam path (0: skip)")
     return p.parse_args()
 
 
@@ -159,10 +165,12 @@ def resolve(args):
 def workload(args):
     from hpsim_gb300 import lattices as L
     if args.workload == "small_fodo":
-        return L.small_fodo()
-    if args.workload == "ccl_large":
-        return L.ccl_like()
-    return L.dtl_like(n_gaps=args.gaps)
+        elems = L.small_fodo()
+    elif args.workload == "ccl_large":
+        elems = L.ccl_like()
+    else:
+        elems = L.dtl_like(n_gaps=args.gaps)
+    return elems[:args.elements] if args.elements else elems
 
 
 def describe(args, n_elem):
@@ -409,6 +417,111 @@ def run_reference(args):
                              "sample": f"{args.steps} steps, each {r['sample']}"},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def surrogate_batched(args, plain_value, local, flush, net_path, tol):
+    """Surrogate + batched against plain SCHEFF on the DTL-like workload: B
+    beams of the same particle count with per-beam perturbed set points
+    (lattices.dtl_batch) in one batch graph launch, timed without and then
+    with the learned field surrogate attached to every solver (the same
+    timing as the headline: L2 flushed, CUDA events around the launch).
+    Beam 0 of the surrogate run is then checked against the FP64 oracle on
+    the same lattice and seed (transmission, flags, emittances).  Returns
+    the record of the bench line's "surrogate_batched" key."""
+    import numpy as np
+    import torch
+    from hpsim_gb300 import HPSim, lattices as L
+    base = L.dtl_like(n_gaps=args.gaps)
+    scan = L.dtl_batch(args.surrogate_batch, num=args.particles)
+    spec = WORKLOADS["dtl_like"]
+    objs = []
+    for sb in scan:
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=sb.num, precision="fp32")
+        beam.set_waterbag(*L.waterbag_twiss(w0=spec["w0"], freq=spec["freq"]), 0.0, spec["w0"], spec["freq"],
+                          sb.seed)
+        beam.set_ref_w(spec["w0"])
+        beam.set_ref_phi(0.0)
+        beam.save_initial_beam()
+        bl = HPSim.BeamLine(elements=L.perturbed(base, sb))
+        sc = HPSim.SpaceCharge(*spec["mesh"], spec["interval"], 0)
+        sc.set_remesh_threshold(0.0)
+        objs.append((beam, bl, sc, HPSim.Simulator(beam, bl, sc)))
+    batch = HPSim.Batch([o[3] for o in objs])
+    n_elem = len(base)
+    total = sum(sb.num for sb in scan)
+
+    def step():
+        for o in objs:
+            o[0].restore_initial_beam()
+        batch.simulate()
+        return batch.last_time_ms()
+
+    def timed():
+        for _ in range(args.warmup):
+            flush.zero_()
+            step()
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms.append(step())
+        return total * n_elem / (sum(ms) / len(ms) / 1000.0), sum(ms) / len(ms)
+
+    def beam0_monitor():
+        sim0 = objs[0][3]
+        sim0.enable_monitor(True)
+        step()
+        mon = sim0.monitor.copy()
+        sim0.enable_monitor(False)
+        return mon
+
+    plain_b, plain_ms = timed()
+    mon_plain = beam0_monitor()
+    net = np.load(net_path)
+    for o in objs:
+        o[2].set_surrogate(net, tol=tol)
+    stats0 = [o[2].surrogate_stats() for o in objs]
+    sur_b, sur_ms = timed()
+    stats1 = [o[2].surrogate_stats() for o in objs]
+    acc_n = sum(b[0] - a[0] for a, b in zip(stats0, stats1)) / args.steps / len(objs)
+    rej_n = sum(b[1] - a[1] for a, b in zip(stats0, stats1)) / args.steps / len(objs)
+    mon_sur = beam0_monitor()
+    loss_sur, lloss_sur = beam_flags(objs[0][0])
+    rel = lambda i: float(np.max(np.abs(np.nan_to_num(mon_sur[:, i]) / np.nan_to_num(mon_plain[:, i]) - 1.0)))  # noqa: E731
+    out = {"beams": len(objs), "particles_per_beam": args.particles, "elements": n_elem,
+           "lattice": "dtl_like with per-beam RF amplitude x U(0.99, 1.01), RF phase offset U(-1, +1) deg, "
+                      "quad gradients x U(0.97, 1.03)",
+           "network": os.path.relpath(net_path, ROOT), "tol": tol,
+           "plain_single_value": plain_value, "plain_batched_value": plain_b, "plain_batched_ms_per_step": plain_ms,
+           "surrogate_batched_value": sur_b, "surrogate_batched_ms_per_step": sur_ms,
+           "surrogate_batched_over_plain": sur_b / plain_value, "plain_batched_over_plain": plain_b / plain_value,
+           "kicks_per_beam_step": n_elem, "accepted_per_beam_step": acc_n, "fallbacks_per_beam_step": rej_n,
+           "fallback_rate": rej_n / max(acc_n + rej_n, 1e-30),
+           "surrogate_vs_plain_beam0": {"transmission_equal": bool(np.array_equal(mon_sur[:, 0], mon_plain[:, 0])),
+                                        "emittance_rel_err_max": {"x": rel(6), "y": rel(11), "z": rel(16)}},
+           "target": ">= 5x the plain path at <= 1e-3 relative rms-emittance error and exact transmission"}
+    return out, (scan[0], L.perturbed(base, scan[0]), mon_sur, loss_sur, lloss_sur)
+
+
+def surrogate_accuracy(args, check):
+    """Beam 0 of the surrogate batch against the FP64 oracle's pass of the
+    same beam through the same lattice."""
+    from hpsim_gb300 import lattices as L
+    from oracle import oracle as O
+    sb, elems, mon, loss, lloss = check
+    spec = WORKLOADS["dtl_like"]
+    O.build()
+    O.lib().orc_set_threads(os.cpu_count() or 1)
+    types, params, _ = L.lattice_arrays(elems)
+    b = O.Beam(sb.num)
+    b.set_waterbag(L.waterbag_twiss(w0=spec["w0"], freq=spec["freq"]), 0.0, spec["w0"], spec["freq"], sb.seed)
+    b.set_ref_w(spec["w0"])
+    b.set_ref_phi(0.0)
+    sp = O.Scheff(*spec["mesh"], spec["interval"], 0)
+    sp.set(remesh_threshold=0.0)
+    sim = O.Sim(b, types, params, sp)
+    sim.simulate()
+    return accuracy(mon, sim.mon.copy(), loss, b.arr("loss").copy(), lloss, b.arr("lloss").copy())
 
 
 def run_batched(args):
@@ -674,6 +787,11 @@ def main():
     mon_gpu = monitored()
     loss_gpu, lloss_gpu = beam_flags(beam)
 
+    # the headline comparison: surrogate + batched against the plain path
+    sb_rec = sb_check = None
+    if args.workload == "dtl_like" and args.surrogate_batch > 0 and ws == 1 and not args.surrogate:
+        sb_rec, sb_check = surrogate_batched(args, value, local, flush, SURROGATE_NET, args.surrogate_tol)
+
     if rank != 0:
         return
     cpu = acc = None
@@ -712,6 +830,12 @@ def main():
     }
     if acc is not None:
         line["accuracy"] = acc
+    if sb_rec is not None:
+        if not args.no_cpu_baseline:
+            sb_rec["accuracy_vs_oracle_beam0"] = surrogate_accuracy(args, sb_check)
+            a = sb_rec["accuracy_vs_oracle_beam0"]
+            sb_rec["target_met"] = bool(sb_rec["surrogate_batched_over_plain"] >= 5.0 and a["gate"]["pass"])
+        line["surrogate_batched"] = sb_rec
     if sur:
         line["surrogate"] = sur
     print(json.dumps(line), flush=True)

@@ -86,7 +86,7 @@ inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
   d.S = fixed + 3 * tc_stage_bytes(d.BT) <= kTcSmemMax ? 3 : 2;
   d.smem = fixed + d.S * tc_stage_bytes(d.BT);
   d.red_blocks = (nz * nr + 255) / 256;
-  d.edge_blocks = (nz + nr + 1 + 7) / 8;  // 8 warps per block, one edge point each
+  d.edge_blocks = nz + nr + 1;  // one block per edge point
   return d;
 }
 
@@ -275,9 +275,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
   bool issued_mma = false;
 
   if (warp < 4) {
-    // ---- producers: the charge column's shifted copies, then per chunk the
-    // B tiles' bulk copies and the A tiles ----
-    const uint32_t nb = nr * nz;
+    // ---- producers: the B tiles of the first stages in flight, the charge
+    // column's shifted copies, then per chunk the A tile (and the B tile of
+    // the chunks after the first S) ----
+    const unsigned char *gsrc = (const unsigned char *)t.tcg + (size_t)rs * d.NC * 2 * BT;
+    if (tid == 0) {
+      for (uint32_t i = 0; i < S && i < nch; ++i) {
+        unsigned char *st = sm + i * stage;
+        mbar_arrive_tx(&full[i], 2 * BT);
+        const unsigned char *src = gsrc + (size_t)(c0 + i) * 2 * BT;
+        bulk_g2s(st + 2 * 16384, src, BT, &full[i]);
+        bulk_g2s(st + 2 * 16384 + BT, src + BT, BT, &full[i]);
+      }
+    }
     for (uint32_t zs = tid; zs < nz; zs += kTcProducers) qc[zs] = tc_charge(t.bin_fx[zs * nr + rs]);
     asm volatile("bar.sync 1, 128;" ::: "memory");
     // copy s, element x holds R(x + s - 128), R(v) = q(nz - 1 - v) inside the mesh
@@ -290,14 +300,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
       cp[(8 + s) * L + x] = __float2bfloat16_rn(q - __bfloat162float(hi));
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
-    (void)nb;
-    const unsigned char *gsrc = (const unsigned char *)t.tcg + (size_t)rs * d.NC * 2 * BT;
     const uint32_t m = tid;  // the A row this thread writes
     for (uint32_t i = 0; i < nch && !*abort; ++i) {
       const uint32_t s = i % S, use = i / S;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort)) break;
       unsigned char *st = sm + s * stage;
-      if (tid == 0) {
+      if (tid == 0 && use > 0) {
         mbar_arrive_tx(&full[s], 2 * BT);
         const unsigned char *src = gsrc + (size_t)(c0 + i) * 2 * BT;
         bulk_g2s(st + 2 * 16384, src, BT, &full[s]);
@@ -393,29 +401,57 @@ __global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t
     const uint32_t rp = id / nz, zp = id % nz, tile = zp / kTcM, m = zp % kTcM;
     const float *p = t.tcp + ((size_t)tile * nr * N + 2 * rp) * kTcM + m;
     float ex = 0.0f, ez = 0.0f;
-    for (uint32_t g = 0; g < nr; ++g) {
-      ex += p[(size_t)g * N * kTcM];
-      ez += p[(size_t)g * N * kTcM + kTcM];
+    // nr is a multiple of 8: eight radii's loads in flight, summed in order
+    for (uint32_t g0 = 0; g0 < nr; g0 += 8) {
+      float vx[8], vz[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        vx[u] = __ldcg(p + (size_t)(g0 + u) * N * kTcM);
+        vz[u] = __ldcg(p + (size_t)(g0 + u) * N * kTcM + kTcM);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        ex += vx[u];
+        ez += vz[u];
+      }
     }
     const size_t pt = (size_t)zp * nrow + rp;
     out[2 * pt] = ex;
     out[2 * pt + 1] = ez;
     return;
   }
-  const uint32_t e = (blockIdx.x - d.red_blocks) * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (e >= nz + nr + 1) return;
+  // one block per edge point: the threads stride over the bins four at a
+  // time (loads in flight together), then a fixed shuffle tree and the
+  // warps in order
+  __shared__ float red[2][8];
+  const uint32_t e = blockIdx.x - d.red_blocks, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t zp = e <= nr ? nz : e - (nr + 1), rp = e <= nr ? e : nr;
   const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * nr * nz;  // [dz][rs]
+  const uint32_t nb = nr * nz;
   float ax = 0.0f, az = 0.0f;
-  for (uint32_t k = lane; k < nr * nz; k += 32) {
-    const uint32_t zs = k / nr, rs = k % nr;
-    const float q = tc_charge(t.bin_fx[k]);
-    if (q == 0.0f) continue;
-    const int kk = (int)zp - (int)zs;
-    const bool below = kk >= 1;
-    const float2 g = G[(size_t)(below ? kk - 1 : -kk) * nr + rs];
-    ax = fmaf(q, g.x, ax);
-    az = fmaf(q, below ? g.y : -g.y, az);
+  for (uint32_t k0 = threadIdx.x; k0 < nb; k0 += 4 * blockDim.x) {
+    float q[4];
+    float2 g[4];
+    bool below[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t k = k0 + u * blockDim.x;
+      q[u] = 0.0f;
+      g[u] = make_float2(0.0f, 0.0f);
+      below[u] = true;
+      if (k < nb) {
+        const uint32_t zs = k / nr, rs = k % nr;
+        const int kk = (int)zp - (int)zs;
+        below[u] = kk >= 1;
+        q[u] = tc_charge(__ldg(t.bin_fx + k));
+        g[u] = __ldg(G + (size_t)(below[u] ? kk - 1 : -kk) * nr + rs);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      ax = fmaf(q[u], g[u].x, ax);
+      az = fmaf(q[u], below[u] ? g[u].y : -g[u].y, az);
+    }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -423,14 +459,22 @@ __global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t
     az += __shfl_down_sync(0xffffffffu, az, off);
   }
   if (lane == 0) {
+    red[0][warp] = ax;
+    red[1][warp] = az;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float sx = 0.0f, sz = 0.0f;
+    for (uint32_t w = 0; w < blockDim.x / 32; ++w) {
+      sx += red[0][w];
+      sz += red[1][w];
+    }
     const size_t pt = (size_t)zp * nrow + rp;
-    out[2 * pt] = ax;
-    out[2 * pt + 1] = az;
+    out[2 * pt] = sx;
+    out[2 * pt + 1] = sz;
   }
 }
 
-// the dynamic shared-memory limit of the largest mesh the path takes (static
-// and dynamic shared memory together stay within the 227 KB a CTA may have)
 inline cudaError_t contract_tc_configure() {
   size_t most = 0;
   for (uint32_t nr = 16; nr <= 128; nr *= 2)

@@ -14,8 +14,9 @@
 //    takes every statistics sweep in its own sweep (push32.cu,
 //    OpPushScStats) and certifies that the loss test flags no particle
 //    and that no relative phase wraps; only when it cannot, the loss test
-//    and the moments run here (Op32LlossScStats, then Op32ScStats when the
-//    good set changed).  The kick runs inside the element half after it;
+//    and the moments run here in one small launch (Op32LlossScStats, whose
+//    last block sweeps the moments again when the good set changed).  The
+//    kick runs inside the element half after it;
 //  * relative phases are not stored: the deposit and the kick form
 //    wrap(phi - <phi>_good) from the phase offset and Sc32Consts::pag;
 //  * the deposit keeps a 32-bit fixed-point histogram per block in shared
@@ -204,6 +205,8 @@ struct Op32LlossScStats {
   }
   __device__ void finalize(const double *s, int tid, int nth) const {
     __shared__ int redo;
+    __shared__ float red[kBlock / 32][8];
+    __shared__ double mom[8];
     if (tid == 0) {
       sc->n_stat_sweeps += 1;
       BeamStats &st = *b.st;
@@ -213,14 +216,53 @@ struct Op32LlossScStats {
       redo = s[11] != 0.0;
       if (redo) {
         st.st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)s[10] / (float)ng) + b.phi_ref : -99999;
-        st.sc_redo = 1u;
       } else {
         sc_moments_finish(b, s, sc, t, freq, frac, h);
         st.sc_redo = 0u;
       }
     }
     __syncthreads();
-    if (!redo) zero_mesh_tables(sc, t, tid, nth);
+    if (redo) {
+      // the loss test changed the good set: the moments again about the new
+      // <phi>_good (Op32ScStats), swept by this last block alone -- a rare
+      // path, kept out of a launch of its own; thread order, then a fixed
+      // shuffle tree and the warps in order
+      const float pag = (float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref);
+      float a[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) a[k] = 0.0f;
+      for (uint32_t i = tid; i < b.n; i += nth) {
+        const float pr = rel_phase_f(b.fphi[i] - pag);
+        b.fphi_r[i] = pr;
+        float a12[12];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a12[k] = a[k];
+        sc_moments_add(a12, pr, b.loss[i], b.lloss[i], b.fx[i], b.fy[i], b.fw[i]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = a12[k];
+      }
+      const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        float v = a[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][k] = v;
+      }
+      __syncthreads();
+      if (tid < 8) {
+        double v = 0.0;
+        for (int w = 0; w < nth / 32; ++w) v += (double)red[w][tid];
+        mom[tid] = v;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        sc_moments_finish(b, mom, sc, t, freq, frac, h);
+        b.st->sc_redo = 0u;
+      }
+      __syncthreads();
+    }
+    zero_mesh_tables(sc, t, tid, nth);
   }
 };
 
@@ -500,13 +542,16 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
   }
 }
 
+// one launch of one block per SM: it returns at once when the element map
+// before the kick certified its statistics (every kick of the bench
+// workloads), so its cost there is the launch alone
 void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
                            PassScratch s, cudaStream_t st) {
   ScTables u = tables32(t);
   const Sc32Host h = sc32_host(b, a);
-  launch_pass_f(Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st);
-  launch_pass_f(Op32ScStats{b, sc, u, a.freq, a.frac, h, 1}, b.n, s, st);
-  note_launch(2);
+  launch_k(pass_kernel_f<Op32LlossScStats>, dim3(pass_blocks_f(b.n, 1)), dim3(kBlock), 0, st,
+           Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s);
+  note_launch();
 }
 
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,

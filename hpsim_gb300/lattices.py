@@ -222,14 +222,24 @@ def partition_beams(nums, ranks):
     return [sorted(o) for o in out]
 
 
-def ccl_batch(n_beams=16, num=1 << 20, seed=805):
-    """Beams of the CCL-like lattice with perturbed set points: RF amplitude
-    scale U(0.99, 1.01), RF phase offset U(-1, +1) deg and quad-gradient
-    scale U(0.97, 1.03) per beam, equal particle counts."""
+def perturbed_beams(n_beams, num, seed):
+    """Equal beams with perturbed set points: RF amplitude scale U(0.99,
+    1.01), RF phase offset U(-1, +1) deg and quad-gradient scale U(0.97,
+    1.03) per beam."""
     rng = np.random.default_rng(seed)
     return [ScanBeam(num=num, seed=int(rng.integers(1, 2 ** 31)), rf_scale=float(rng.uniform(0.99, 1.01)),
                      phase_offset=math.radians(float(rng.uniform(-1.0, 1.0))),
                      quad_scale=float(rng.uniform(0.97, 1.03))) for _ in range(n_beams)]
+
+
+def ccl_batch(n_beams=16, num=1 << 20, seed=805):
+    """Beams of the CCL-like lattice with perturbed set points (perturbed_beams)."""
+    return perturbed_beams(n_beams, num, seed)
+
+
+def dtl_batch(n_beams=8, num=1 << 20, seed=2025):
+    """Beams of the DTL-like lattice with perturbed set points (perturbed_beams)."""
+    return perturbed_beams(n_beams, num, seed)
 
 
 def perturbed(elems, sb: ScanBeam):

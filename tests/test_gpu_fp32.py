@@ -152,6 +152,49 @@ def test_fp32_contraction_kernels_agree():
     assert_fp32_close(mons[0], mons[1], "tensor vs cuda cores")
 
 
+def test_fp32_uncertified_statistics_match_oracle(oracle):
+    """Kicks whose statistics the element map before them cannot certify:
+    particles more than 3 pi behind the bunch are flagged by the
+    longitudinal-loss test at the first kick (the good set changes, so the
+    moments are swept again about the new <phi>_good) and particles sit
+    near the relative-phase wrap.  The fallback sweep runs (the solver's
+    counter says so) and flags, counts and statistics still match the FP64
+    oracle on the same distribution."""
+    import numpy as np
+    from hpsim_gb300 import HPSim, lattices as L
+    n = 4096
+    rng = np.random.default_rng(8)
+    b0 = oracle.Beam(n)
+    b0.set_waterbag(L.waterbag_twiss(), 0.0, 0.75, 201.25, 77)
+    x, xp, y, yp, phi, w = (b0.arr(k).copy() for k in ("x", "xp", "y", "yp", "phi", "w"))
+    late = rng.choice(np.arange(1, n), 24, replace=False)
+    phi[late[:12]] += 4.0 * np.pi          # beyond <phi> + 3 pi: longitudinal loss
+    phi[late[12:]] += np.pi * 0.999        # next to the wrap of the relative phase
+    elems = L.small_fodo()[:7]
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=n, precision="fp32")
+    beam.set_distribution(x, xp, y, yp, phi, w)
+    beam.set_ref_w(0.75)
+    beam.set_frequency(201.25)
+    sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
+    sc.set_remesh_threshold(0.0)
+    sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=elems), sc)
+    sim.enable_monitor(True)
+    sim.simulate()
+    assert sc.get_counter("stat_sweeps") > 0
+    ob = oracle.Beam(n)
+    ob.set_distribution(x, xp, y, yp, phi, w)
+    ob.set_ref_w(0.75)
+    ob.set_frequency(201.25)
+    types, params, _ = L.lattice_arrays(elems)
+    sp = oracle.Scheff(32, 128, 0.10, 0)
+    sp.set(remesh_threshold=0.0)
+    mo = oracle.Sim(ob, types, params, sp).simulate().copy()
+    assert np.array_equal(beam._loss(0), ob.arr("loss"))
+    assert np.array_equal(beam._loss(1), ob.arr("lloss"))
+    assert int(ob.arr("lloss").sum()) >= 12
+    assert_fp32_close(sim.monitor, mo, "uncertified")
+
+
 def test_fp32_graph_replay_is_bit_identical():
     from hpsim_gb300 import lattices as L
     elems = L.small_fodo()
