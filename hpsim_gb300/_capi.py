@@ -114,6 +114,10 @@ def lib():
         "hps_batch_destroy": (st, [vp]),
         "hps_batch_simulate": (st, [vp, i32, i32]),
         "hps_batch_last_time_ms": (st, [vp, dp]),
+        "hps_sim_autotune": (st, [vp, i32, i32, i32, ip, dp, u32, C.POINTER(u32)]),
+        "hps_batch_autotune": (st, [vp, i32, i32, i32, ip, dp, u32, C.POINTER(u32)]),
+        "hps_sim_get_shape": (st, [vp, ip]),
+        "hps_sim_set_shape": (st, [vp, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

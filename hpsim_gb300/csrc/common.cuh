@@ -49,6 +49,9 @@ struct DevBeam {
   // particle the offsets fphi, fw are taken from.  Tracked on the host in
   // FP64 through the same element formulas (on axis) and passed by value.
   double phi_ref, w_ref;
+  // launch shape of the FP32 particle sweeps and statistics passes: at most
+  // this many blocks per SM (0: as many as the SM holds at once)
+  uint32_t sweep_cap;
 };
 
 // SCHEFF solver state in device memory (configuration, the adaptive-remesh

@@ -95,6 +95,7 @@ struct ScKickArgs {
   uint32_t nx_max, nz_max;  // largest mesh the solver's tables hold
   int adj_possible;         // adjacent bunches configured (else r_max never sizes the mesh)
   bool mesh_fixed;          // the kick's mesh is the largest one (no mesh-size cut-off energy)
+  uint32_t dep_per_sm;      // FP32 deposit: blocks per SM (launch shape)
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);

@@ -16,6 +16,7 @@
 // synchronous particle's step through the element.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <unordered_map>
 
 #include "internal.h"
@@ -60,12 +61,20 @@ __device__ inline uint32_t step(Part &p, const Map &m, const Shift &s) {
 // on the first, so each SM keeps enough loads in flight to cover latency.
 constexpr int kSweepBatch = 2;
 
-int sweep_grid(const void *kernel, uint32_t n) {
+// cap: at most this many blocks per SM (0: as many as the SM holds)
+int sweep_grid(const void *kernel, uint32_t n, uint32_t cap) {
+  static std::mutex m;
   static std::unordered_map<const void *, int> resident;
   static int sms = 0;
-  if (!sms && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) sms = 152;
-  int &r = resident[kernel];
-  if (!r && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kernel, kBlock, 0) != cudaSuccess || r < 1)) r = 1;
+  int r;
+  {
+    std::lock_guard<std::mutex> lock(m);
+    if (!sms && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) sms = 152;
+    int &rr = resident[kernel];
+    if (!rr && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rr, kernel, kBlock, 0) != cudaSuccess || rr < 1)) rr = 1;
+    r = rr;
+  }
+  if (cap && (uint32_t)r > cap) r = (int)cap;
   const uint64_t need = ((uint64_t)n + (uint64_t)kSweepBatch * kBlock - 1) / ((uint64_t)kSweepBatch * kBlock);
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)r * sms));
 }
@@ -225,13 +234,14 @@ void launch_map(const DevBeam &b, const Map &m, const RefK &rk, double phi0, dou
                 const PushFuse *pf) {
   const Shift sh{(float)(b.phi_ref - phi0), (float)(b.w_ref - w0)};
   if (!pf) {
-    launch_k(k32_push<Map>, dim3(sweep_grid((const void *)k32_push<Map>, b.n)), dim3(kBlock), 0, st, b, m, sh);
+    launch_k(k32_push<Map>, dim3(sweep_grid((const void *)k32_push<Map>, b.n, b.sweep_cap)), dim3(kBlock), 0, st, b,
+             m, sh);
   } else if (pf->mode == PUSH_SCSTATS) {
     launch_pass_f(OpPushScStats<Map>{b, m, sh, pf->s_last, pf->sc, pf->t, pf->freq, pf->frac, pf->h}, b.n, pf->scr,
-                  st);
+                  st, b.sweep_cap);
   } else {
-    launch_k(k32_kick_push<Map>, dim3(sweep_grid((const void *)k32_kick_push<Map>, b.n)), dim3(kBlock), 0, st, b,
-             (const ScState *)pf->sc, pf->t, rk, pf->skip_mask, m, sh);
+    launch_k(k32_kick_push<Map>, dim3(sweep_grid((const void *)k32_kick_push<Map>, b.n, b.sweep_cap)), dim3(kBlock),
+             0, st, b, (const ScState *)pf->sc, pf->t, rk, pf->skip_mask, m, sh);
   }
   note_launch();
 }

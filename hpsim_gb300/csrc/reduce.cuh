@@ -274,9 +274,11 @@ inline int pass_resident() {
   return r;
 }
 
+// cap: at most this many blocks per SM (0: no cap)
 template <class Op>
-inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s) {
-  const int per_sm = op_fast<Op>::value ? pass_resident<Op>() : 2;
+inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s, uint32_t cap = 0) {
+  int per_sm = op_fast<Op>::value ? pass_resident<Op>() : 2;
+  if (cap && (uint32_t)per_sm > cap) per_sm = (int)cap;
   launch_k(pass_kernel_f<Op>, dim3(pass_blocks_f(n, per_sm)), dim3(kBlock), 0, s, op, n, scr);
 }
 

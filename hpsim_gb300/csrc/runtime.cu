@@ -16,6 +16,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -131,6 +133,9 @@ struct hps_sim_s {
   uint64_t prof_cnt[HPS_NPROF] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  // launch shapes of the FP32 kernels (hps_sim_autotune picks them)
+  uint32_t sweep_cap = 0;   // particle sweeps: blocks per SM (0: all the SM holds)
+  uint32_t dep_per_sm = 3;  // deposit: blocks per SM
 };
 
 // Many simulators run as one graph launch: each simulator's captured range
@@ -999,6 +1004,7 @@ ScKickArgs kick_args(Ctx &c, double length) {
   a.nz_max = c.sc->nz_max;
   a.adj_possible = c.sc->adj_bunch != 0;
   a.mesh_fixed = c.sc->mesh_w == 0.0 && c.sc->nx == c.sc->nx_max && c.sc->nz == c.sc->nz_max;
+  a.dep_per_sm = c.s->dep_per_sm;
   return a;
 }
 
@@ -1307,6 +1313,7 @@ hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
   s->prev_end = p->end_index;
   hps_beam_t b = c.b;
   cudaStream_t st = b->stream;
+  b->d.sweep_cap = s->sweep_cap;
   p->monitor = s->mon_host && s->mon_cap >= (uint32_t)n;
   if (p->monitor && s->mon_dev_cap < (uint32_t)n) {
     if (s->mon_dev) cudaFree(s->mon_dev);
@@ -1348,6 +1355,10 @@ hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
     key = mix(key, (uint64_t)b->prec);
     key = mixd(key, b->d.phi_ref);
     key = mixd(key, b->d.w_ref);
+    // launch shapes
+    key = mix(key, (uint64_t)s->sweep_cap);
+    key = mix(key, (uint64_t)s->dep_per_sm);
+    key = mix(key, c.sc ? (uint64_t)c.sc->contraction : 0);
     p->key = key | 1ull;
   }
   return HPS_OK;
@@ -1654,6 +1665,279 @@ hps_status hps_batch_last_time_ms(hps_batch_t bt, double *ms) {
   if (!bt || !ms) return fail(HPS_ERR_INVALID, "bad argument");
   *ms = bt->last_ms;
   return HPS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// autotuner
+// ---------------------------------------------------------------------------
+namespace {
+
+// A simulator's state before tuning: the beam on the device, its host-side
+// fields, the solver's device state and the engine's host state, so that
+// every trial starts from the same point and tuning leaves no trace.
+struct Snapshot {
+  hps_sim_t s = nullptr;
+  void *dev[8] = {};
+  BeamStats st{};
+  ScState sc{};
+  double b_design_w = 0, b_freq = 0, b_current = 0, phi_ref = 0, w_ref = 0;
+  double design_w = 0, wavelen = 0, fraction = 0, interval = 0;
+  uint32_t cur_id = 0, ccl = 0;
+  int prev_end = -1;
+};
+
+void snap_free(Snapshot &z) {
+  for (void *&p : z.dev)
+    if (p) { cudaFree(p); p = nullptr; }
+}
+
+hps_status snap_take(hps_sim_t s, Snapshot &z) {
+  hps_beam_t b = s->beam;
+  z.s = s;
+  const size_t nd = (size_t)b->n * esize(b), nu = (size_t)b->n * 4;
+  for (int k = 0; k < 8; ++k) {
+    const size_t bytes = k < 6 ? nd : nu;
+    CK(cudaMalloc(&z.dev[k], bytes ? bytes : 1));
+    const void *src = k < 6 ? coord_ptr(b, k) : (k == 6 ? (void *)b->d.loss : (void *)b->d.lloss);
+    CK(cudaMemcpyAsync(z.dev[k], src, bytes, cudaMemcpyDeviceToDevice, b->stream));
+  }
+  CK(cudaMemcpyAsync(&z.st, b->d.st, sizeof(BeamStats), cudaMemcpyDeviceToHost, b->stream));
+  if (s->sc) CK(cudaMemcpyAsync(&z.sc, s->sc->d, sizeof(ScState), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  z.b_design_w = b->design_w; z.b_freq = b->freq; z.b_current = b->current;
+  z.phi_ref = b->d.phi_ref; z.w_ref = b->d.w_ref;
+  z.design_w = s->design_w; z.wavelen = s->wavelen; z.cur_id = s->cur_id; z.ccl = s->ccl_cell_num;
+  z.prev_end = s->prev_end;
+  if (s->sc) { z.fraction = s->sc->fraction; z.interval = s->sc->interval; }
+  return HPS_OK;
+}
+
+hps_status snap_put(const Snapshot &z) {
+  hps_sim_t s = z.s;
+  hps_beam_t b = s->beam;
+  const size_t nd = (size_t)b->n * esize(b), nu = (size_t)b->n * 4;
+  for (int k = 0; k < 8; ++k) {
+    void *dst = k < 6 ? coord_ptr(b, k) : (k == 6 ? (void *)b->d.loss : (void *)b->d.lloss);
+    CK(cudaMemcpyAsync(dst, z.dev[k], k < 6 ? nd : nu, cudaMemcpyDeviceToDevice, b->stream));
+  }
+  CK(cudaMemcpyAsync(b->d.st, &z.st, sizeof(BeamStats), cudaMemcpyHostToDevice, b->stream));
+  if (s->sc) CK(cudaMemcpyAsync(s->sc->d, &z.sc, sizeof(ScState), cudaMemcpyHostToDevice, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  b->design_w = z.b_design_w; b->freq = z.b_freq; b->current = z.b_current;
+  b->d.phi_ref = z.phi_ref; b->d.w_ref = z.w_ref;
+  s->design_w = z.design_w; s->wavelen = z.wavelen; s->cur_id = z.cur_id; s->ccl_cell_num = z.ccl;
+  s->prev_end = z.prev_end;
+  if (s->sc) { s->sc->fraction = z.fraction; s->sc->interval = z.interval; }
+  return HPS_OK;
+}
+
+// one launch shape: contraction kernel of FP32 beams (solver parameter 10),
+// deposit blocks per SM, sweep blocks per SM (0: all the SM holds)
+struct Shape {
+  int contraction;
+  uint32_t dep_per_sm, sweep_cap;
+};
+
+hps_status shape_apply(hps_sim_t s, const Shape &sh) {
+  s->dep_per_sm = sh.dep_per_sm;
+  s->sweep_cap = sh.sweep_cap;
+  if (s->sc && s->sc->contraction != sh.contraction) {
+    hps_status e = hps_scheff_set(s->sc, 10, (double)sh.contraction);
+    if (e) return e;
+  }
+  return HPS_OK;
+}
+
+std::mutex g_tune_mutex;
+std::map<std::string, Shape> g_tune_cache;
+
+// the cache key: device, mesh, particle count (power-of-two bucket), precision
+std::string tune_key(hps_sim_t s, const char *what) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp pr{};
+  cudaGetDeviceProperties(&pr, dev);
+  uint32_t bucket = 0;
+  while ((1u << bucket) < s->beam->n && bucket < 31) ++bucket;
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "%s|%d|%s|%u|%u|%u|%d", what, dev, pr.name, s->sc ? s->sc->nx_max : 0u,
+                s->sc ? s->sc->nz_max : 0u, bucket, s->beam->prec);
+  return buf;
+}
+
+// The search: coordinate descent over the three knobs (contraction kernel,
+// then deposit blocks per SM, then sweep blocks per SM), each candidate
+// timed as the median of `reps` runs after one untimed run (which captures
+// its graph), every run from the snapshot.  run() simulates and returns the
+// device time in ms.
+template <class Run, class Restore>
+hps_status tune_search(const std::vector<hps_sim_t> &sims, bool fp32, bool tc_ok, int reps, Run run,
+                       Restore restore, Shape *best_out, std::vector<double> *times) {
+  Shape best{sims[0]->sc ? sims[0]->sc->contraction : 0, sims[0]->dep_per_sm, sims[0]->sweep_cap};
+  if (!fp32) { *best_out = best; return HPS_OK; }
+  auto measure = [&](const Shape &sh, double *ms) -> hps_status {
+    for (hps_sim_t s : sims) {
+      hps_status e = shape_apply(s, sh);
+      if (e) return e;
+    }
+    std::vector<double> v;
+    for (int r = 0; r <= reps; ++r) {
+      hps_status e = restore();
+      if (e) return e;
+      double t = 0.0;
+      e = run(&t);
+      if (e) return e;
+      if (r > 0) v.push_back(t);
+    }
+    std::sort(v.begin(), v.end());
+    *ms = v[v.size() / 2];
+    if (times) times->push_back(*ms);
+    return HPS_OK;
+  };
+  double best_ms = 0.0;
+  hps_status e = measure(best, &best_ms);
+  if (e) return e;
+  std::vector<Shape> cands;
+  if (tc_ok) cands.push_back({1 - best.contraction, best.dep_per_sm, best.sweep_cap});
+  for (int stage = 0; stage < 3; ++stage) {
+    if (stage == 1) {
+      for (uint32_t d : {2u, 3u, 4u})
+        if (d != best.dep_per_sm) cands.push_back({best.contraction, d, best.sweep_cap});
+    } else if (stage == 2) {
+      for (uint32_t c : {0u, 2u})
+        if (c != best.sweep_cap) cands.push_back({best.contraction, best.dep_per_sm, c});
+    }
+    for (const Shape &sh : cands) {
+      double ms = 0.0;
+      if ((e = measure(sh, &ms))) return e;
+      if (ms < best_ms) { best_ms = ms; best = sh; }
+    }
+    cands.clear();
+  }
+  *best_out = best;
+  return HPS_OK;
+}
+
+void report(const Shape &b, const std::vector<double> &t, int32_t *shape_out, double *ms_out, uint32_t ms_cap,
+            uint32_t *n_out) {
+  if (shape_out) { shape_out[0] = b.contraction; shape_out[1] = (int32_t)b.dep_per_sm; shape_out[2] = (int32_t)b.sweep_cap; }
+  if (ms_out)
+    for (size_t k = 0; k < t.size() && k < ms_cap; ++k) ms_out[k] = t[k];
+  if (n_out) *n_out = (uint32_t)t.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+hps_status hps_sim_autotune(hps_sim_t s, int32_t start, int32_t end, int32_t reps, int32_t *shape_out, double *ms_out,
+                            uint32_t ms_cap, uint32_t *n_timed) {
+  if (!s || reps < 1 || reps > 64) return fail(HPS_ERR_INVALID, "sim_autotune: bad argument");
+  const std::string key = tune_key(s, "sim");
+  std::vector<double> times;
+  Shape best{};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      hps_status e = shape_apply(s, it->second);
+      if (e) return e;
+      report(it->second, times, shape_out, ms_out, ms_cap, n_timed);
+      return HPS_OK;
+    }
+  }
+  Snapshot z;
+  hps_status e = snap_take(s, z);
+  if (e) { snap_free(z); return e; }
+  const bool fp32 = f32(s->beam) && s->sc && s->sc_on;
+  const bool tc_ok = fp32 && sc32_tc_mesh(s->sc->nx_max, s->sc->nz_max);
+  auto run = [&](double *ms) -> hps_status {
+    hps_status r = hps_sim_simulate(s, start, end);
+    if (r) return r;
+    *ms = s->last_ms;
+    return HPS_OK;
+  };
+  auto restore = [&]() { return snap_put(z); };
+  e = tune_search({s}, fp32, tc_ok, reps, run, restore, &best, &times);
+  if (!e) e = shape_apply(s, best);
+  if (!e) e = snap_put(z);
+  snap_free(z);
+  if (e) return e;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = best;
+  }
+  report(best, times, shape_out, ms_out, ms_cap, n_timed);
+  return HPS_OK;
+}
+
+hps_status hps_batch_autotune(hps_batch_t bt, int32_t start, int32_t end, int32_t reps, int32_t *shape_out,
+                              double *ms_out, uint32_t ms_cap, uint32_t *n_timed) {
+  if (!bt || bt->sims.empty() || reps < 1 || reps > 64) return fail(HPS_ERR_INVALID, "batch_autotune: bad argument");
+  const std::string key = tune_key(bt->sims[0], "batch") + "|" + std::to_string(bt->sims.size());
+  std::vector<double> times;
+  Shape best{};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      for (hps_sim_t s : bt->sims) {
+        hps_status e = shape_apply(s, it->second);
+        if (e) return e;
+      }
+      report(it->second, times, shape_out, ms_out, ms_cap, n_timed);
+      return HPS_OK;
+    }
+  }
+  std::vector<Snapshot> zs(bt->sims.size());
+  hps_status e = HPS_OK;
+  for (size_t k = 0; k < zs.size() && !e; ++k) e = snap_take(bt->sims[k], zs[k]);
+  bool fp32 = true, tc_ok = true;
+  for (hps_sim_t s : bt->sims) {
+    fp32 = fp32 && f32(s->beam) && s->sc && s->sc_on;
+    tc_ok = tc_ok && s->sc && sc32_tc_mesh(s->sc->nx_max, s->sc->nz_max);
+  }
+  auto run = [&](double *ms) -> hps_status {
+    hps_status r = hps_batch_simulate(bt, start, end);
+    if (r) return r;
+    *ms = bt->last_ms;
+    return HPS_OK;
+  };
+  auto restore = [&]() -> hps_status {
+    for (const Snapshot &z : zs) {
+      hps_status r = snap_put(z);
+      if (r) return r;
+    }
+    return HPS_OK;
+  };
+  if (!e) e = tune_search(bt->sims, fp32, fp32 && tc_ok, reps, run, restore, &best, &times);
+  for (hps_sim_t s : bt->sims)
+    if (!e) e = shape_apply(s, best);
+  if (!e) e = restore();
+  for (Snapshot &z : zs) snap_free(z);
+  if (e) return e;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = best;
+  }
+  report(best, times, shape_out, ms_out, ms_cap, n_timed);
+  return HPS_OK;
+}
+
+hps_status hps_sim_get_shape(hps_sim_t s, int32_t *shape_out) {
+  if (!s || !shape_out) return fail(HPS_ERR_INVALID, "sim_get_shape: bad argument");
+  shape_out[0] = s->sc ? s->sc->contraction : 0;
+  shape_out[1] = (int32_t)s->dep_per_sm;
+  shape_out[2] = (int32_t)s->sweep_cap;
+  return HPS_OK;
+}
+
+hps_status hps_sim_set_shape(hps_sim_t s, const int32_t *shape) {
+  if (!s || !shape || shape[0] < 0 || shape[0] > 1 || shape[1] < 1 || shape[1] > 8 || shape[2] < 0 || shape[2] > 16)
+    return fail(HPS_ERR_INVALID, "sim_set_shape: bad argument");
+  return shape_apply(s, Shape{shape[0], (uint32_t)shape[1], (uint32_t)shape[2]});
 }
 
 }  // extern "C"

@@ -565,8 +565,8 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   size_t hb = 0;
   DepQ q{};
   if (a.deposit_ok) {
-    // three blocks per SM at most, in whole clusters
-    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, 3u * 152u);
+    // dep_per_sm blocks per SM at most (three unless tuned), in whole clusters
+    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, (a.dep_per_sm ? a.dep_per_sm : 3u) * 152u);
     ndep = (ndep + kDepCluster - 1) / kDepCluster * kDepCluster;
     hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
     if (hb > kMaxHistSmem) hb = 0;

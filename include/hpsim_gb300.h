@@ -301,6 +301,32 @@ hps_status hps_batch_destroy(hps_batch_t batch);
 hps_status hps_batch_simulate(hps_batch_t batch, int32_t start, int32_t end);
 hps_status hps_batch_last_time_ms(hps_batch_t batch, double *ms);
 
+/* ---- autotuner (no reference counterpart; it replaces the reference's fixed
+ * launch geometry, e.g. the 64-block cap of src/beam/src/beam.cu:419 and the
+ * contraction grid of src/simulation/src/space_charge.cu:189-200).  A launch
+ * shape of an FP32 beam's simulation is shape[3] = {contraction kernel (0
+ * split-BF16 tensor cores where the mesh allows, 1 FP32 CUDA cores),
+ * deposit blocks per SM (1..8), particle-sweep blocks per SM (0: as many as
+ * an SM holds, else a cap 1..16)}.  hps_sim_autotune times candidate shapes
+ * on the simulator's own simulate(start, end) with CUDA events (coordinate
+ * descent over the three knobs; each candidate the median of `reps` runs
+ * after an untimed one that captures its graph; every run starts from a
+ * snapshot of the beam, solver and engine state, which is restored at the
+ * end), keeps the fastest and caches it per (device, mesh, power-of-two
+ * particle-count bucket, precision): a later call with the same key applies
+ * the cached shape without timing (n_timed = 0).  shape_out receives the
+ * chosen shape, ms_out up to ms_cap candidate times (ms), n_timed their
+ * count.  FP64 beams have nothing to tune (the shape is returned as is).
+ * hps_batch_autotune does the same for a batch (objective: the batch's
+ * launch; the shape is applied to every simulator).  Tuning must not run
+ * during a stream capture. */
+hps_status hps_sim_autotune(hps_sim_t sim, int32_t start, int32_t end, int32_t reps, int32_t *shape_out,
+                            double *ms_out, uint32_t ms_cap, uint32_t *n_timed);
+hps_status hps_batch_autotune(hps_batch_t batch, int32_t start, int32_t end, int32_t reps, int32_t *shape_out,
+                              double *ms_out, uint32_t ms_cap, uint32_t *n_timed);
+hps_status hps_sim_get_shape(hps_sim_t sim, int32_t *shape_out /* 3 */);
+hps_status hps_sim_set_shape(hps_sim_t sim, const int32_t *shape /* 3 */);
+
 /* ---- SCHEFF field surrogate: network layers (no reference counterpart).
  * Device pointers; tensors [batch][channel][z][r]; x, w, y BF16, bias, dy,
  * dz, dx, dw, db FP32.  dims = {batch, c_in, c_out, h_in, w_in, stride (1|2),

@@ -77,3 +77,57 @@ def test_batch_rejects_shared_beams():
     sim2 = HPSim.Simulator(beam, bl, HPSim.SpaceCharge(32, 128, 0.1, 0))
     with pytest.raises(Exception):
         HPSim.Batch([sim, sim2])
+
+
+def test_autotune_leaves_no_trace_and_its_shape_reproduces():
+    """The autotuner times candidate launch shapes on the simulator's own
+    run and restores the beam, solver and engine state: a simulation after
+    tuning equals, bit for bit, a fresh simulator of the same beam run with
+    the chosen shape set by hand; a second tuning of the same configuration
+    comes from the cache (nothing timed)."""
+    import numpy as np
+    from hpsim_gb300 import HPSim, lattices as L
+
+    def make():
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=65536, precision="fp32")
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 5)
+        beam.set_ref_w(0.75)
+        beam.set_ref_phi(0.0)
+        sc = HPSim.SpaceCharge(32, 128)
+        sc.set_remesh_threshold(0.0)
+        return beam, sc, HPSim.Simulator(beam, HPSim.BeamLine(elements=L.dtl_like(n_gaps=10)), sc)
+
+    beam, sc, sim = make()
+    res = sim.autotune(reps=2)
+    assert len(res["ms"]) >= 4 and all(t > 0 for t in res["ms"])
+    assert sim.get_shape() == res["shape"]
+    assert res["shape"]["contraction"] in (0, 1) and 2 <= res["shape"]["deposit_blocks_per_sm"] <= 4
+    sim.enable_monitor(True)
+    sim.simulate()
+    tuned = sim.monitor.copy(), beam._coord("xp")
+    beam2, sc2, sim2 = make()
+    sim2.set_shape(res["shape"])
+    sim2.enable_monitor(True)
+    sim2.simulate()
+    assert np.array_equal(tuned[0], sim2.monitor)
+    assert np.array_equal(tuned[1], beam2._coord("xp"))
+    beam3, sc3, sim3 = make()
+    again = sim3.autotune(reps=2)
+    assert again["ms"] == [] and again["shape"] == res["shape"]
+
+
+def test_batch_autotune():
+    from hpsim_gb300 import HPSim, lattices as L
+    objs = []
+    for sb in L.batched_scan(6, n_min=16384, n_max=65536):
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=sb.num, precision="fp32")
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, sb.seed)
+        beam.set_ref_w(0.75)
+        sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
+        objs.append((beam, sc, HPSim.Simulator(beam, HPSim.BeamLine(elements=L.scan_lattice(sb)), sc)))
+    batch = HPSim.Batch([o[2] for o in objs])
+    res = batch.autotune(reps=1)
+    assert len(res["ms"]) >= 4
+    for o in objs:
+        assert o[2].get_shape() == res["shape"]
+    batch.simulate()
