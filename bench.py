@@ -60,6 +60,10 @@ def parse():
                    help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
                         "(a network file; default the shipped 32x128 network), and report both")
     p.add_argument("--surrogate-tol", type=float, default=0.02)
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default launch shapes instead of timing candidates before the warm-up")
+    p.add_argument("--tune-elements", type=int, default=60,
+                   help="the autotuner times runs over the lattice's first N elements")
     p.add_argument("--surrogate-batch", type=int, default=8,
                    help="dtl_like on one GPU: also time this many set-point-perturbed beams of the same size in one "
                         "batch launch, without and with the learned field surrogate, and report the ratio to the "
@@ -449,6 +453,9 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
     batch = HPSim.Batch([o[3] for o in objs])
     n_elem = len(base)
     total = sum(sb.num for sb in scan)
+    tune = None
+    if not args.no_autotune:
+        tune = batch.autotune(0, min(n_elem, args.tune_elements) - 1, reps=2)
 
     def step():
         for o in objs:
@@ -492,6 +499,7 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
            "lattice": "dtl_like with per-beam RF amplitude x U(0.99, 1.01), RF phase offset U(-1, +1) deg, "
                       "quad gradients x U(0.97, 1.03)",
            "network": os.path.relpath(net_path, ROOT), "tol": tol,
+           "launch_shape": objs[0][3].get_shape(), "autotune": tune,
            "plain_single_value": plain_value, "plain_batched_value": plain_b, "plain_batched_ms_per_step": plain_ms,
            "surrogate_batched_value": sur_b, "surrogate_batched_ms_per_step": sur_ms,
            "surrogate_batched_over_plain": sur_b / plain_value, "plain_batched_over_plain": plain_b / plain_value,
@@ -575,6 +583,12 @@ def run_batched(args):
     n_elem = len(objs[0][1])
     total = sum(sb.num for sb in scan)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    tune = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        tune = batch.autotune(0, min(n_elem, args.tune_elements) - 1, reps=2)
+        tune["seconds"] = time.perf_counter() - t0
+        tune["elements"] = min(n_elem, args.tune_elements)
 
     def step():
         for o in objs:
@@ -625,7 +639,8 @@ def run_batched(args):
                                     f"graph launch per step"), "beams": args.beams, "particles": total,
                        "parallelism": f"beams partitioned over {ws} GPU(s), balanced by particle count",
                        "elements": n_elem, "precision": args.precision,
-                       "l2": "flushed between steps (256 MB write)"},
+                       "l2": "flushed between steps (256 MB write)",
+                       "launch_shape": objs[0][3].get_shape(), "autotune": tune},
             "sequential": {"ms_per_step": 1000 * t_seq, "value": total * n_elem / t_seq,
                            "note": "one simulate() per beam in turn, wall clock"},
             "e2e": None, "gpu_launches": int(launches), "clocks": clocks.summary()}
@@ -657,6 +672,12 @@ def main():
     n_elem = len(elems)
     beam, bl, sc, sim = make_sim(args, elems, seed=12345 + rank)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    tune = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        tune = sim.autotune(0, min(n_elem, args.tune_elements) - 1, reps=3)
+        tune["seconds"] = time.perf_counter() - t0
+        tune["elements"] = min(n_elem, args.tune_elements)
 
     def barrier():
         torch.cuda.synchronize()
@@ -813,7 +834,8 @@ def main():
                    "particles": args.particles, "elements": n_elem, "precision": args.precision,
                    "parallelism": f"replicas x{ws}", "l2": "flushed between steps (256 MB write)",
                    "wall_s": wall, "sc_kicks_per_step": n_elem,
-                   "sc_uncertified_kicks_per_step": stat_sweeps},
+                   "sc_uncertified_kicks_per_step": stat_sweeps,
+                   "launch_shape": sim.get_shape(), "autotune": tune},
         "roofline": {"bound": "hbm", "kernel_phase": dom,
                      "kernels": PHASE_KERNELS[args.precision].get(dom, dom),
                      "bytes_per_particle": ALG_BYTES[args.precision].get(dom, STEP_BYTES[args.precision]),

@@ -252,6 +252,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
   float *qc = (float *)(sm + S * stage + (size_t)16 * L * 2);
   volatile int *abort = &abort_flag;
 
+  // the charge column first: its loads overlap the set-up below
+  if (warp < 4)
+    for (uint32_t zs = tid; zs < nz; zs += kTcProducers) qc[zs] = tc_charge(__ldg(t.bin_fx + zs * nr + rs));
   if (tid == 0) {
     for (uint32_t s = 0; s < S; ++s) {
       mbar_init(&full[s], kTcProducers + 1);
@@ -288,16 +291,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
         bulk_g2s(st + 2 * 16384 + BT, src + BT, BT, &full[i]);
       }
     }
-    for (uint32_t zs = tid; zs < nz; zs += kTcProducers) qc[zs] = tc_charge(t.bin_fx[zs * nr + rs]);
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    // copy s, element x holds R(x + s - 128), R(v) = q(nz - 1 - v) inside the mesh
-    for (uint32_t e = tid; e < 8 * L; e += kTcProducers) {
-      const uint32_t s = e / L, x = e % L;
-      const int v = (int)x + (int)s - 128;
-      const float q = (v >= 0 && v < (int)nz) ? qc[nz - 1 - v] : 0.0f;
-      const __nv_bfloat16 hi = __float2bfloat16_rn(q);
-      cp[s * L + x] = hi;
-      cp[(8 + s) * L + x] = __float2bfloat16_rn(q - __bfloat162float(hi));
+    // copy s, element x holds R(x + s - 128), R(v) = q(nz - 1 - v) inside the
+    // mesh; eight elements per 16-byte store (L is a multiple of 8)
+    const uint32_t groups = L / 8;
+    for (uint32_t e = tid; e < 8 * groups; e += kTcProducers) {
+      const uint32_t s = e / groups, x0 = (e % groups) * 8;
+      __align__(16) __nv_bfloat16 hv[8], lv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int v = (int)(x0 + j) + (int)s - 128;
+        const float q = (v >= 0 && v < (int)nz) ? qc[nz - 1 - v] : 0.0f;
+        hv[j] = __float2bfloat16_rn(q);
+        lv[j] = __float2bfloat16_rn(q - __bfloat162float(hv[j]));
+      }
+      *(uint4 *)(cp + s * L + x0) = *(const uint4 *)hv;
+      *(uint4 *)(cp + (8 + s) * L + x0) = *(const uint4 *)lv;
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
     const uint32_t m = tid;  // the A row this thread writes

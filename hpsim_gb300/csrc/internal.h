@@ -205,8 +205,15 @@ void contract32(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t 
                 cudaStream_t st);
 void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                 cudaStream_t st);
+// a fork of a beam's stream: kernels on `side` between ev_fork and ev_join
+// run beside the kernels on `main` (a parallel branch of a captured graph)
+struct Fork {
+  cudaStream_t main, side;
+  cudaEvent_t ev_fork, ev_join;
+};
+// fork (may be null): the Green's table runs beside the deposit
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
-               cudaStream_t st, const SurNet *sur = nullptr);
+               cudaStream_t st, const SurNet *sur = nullptr, const Fork *fork = nullptr);
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
 // the statistics after a PUSH_SCSTATS map that could not certify its own:
 // the longitudinal-loss test and the SCHEFF moments in one sweep, repeated

@@ -63,6 +63,9 @@ struct hps_beam_s {
   double mass = 0, charge = 0, current = 0, freq = 0, design_w = 0;
   uint32_t grid_size = 1, blck_size = 1;
   cudaStream_t stream = nullptr;
+  // a second stream and two events: kernels that do not depend on each
+  // other run side by side (a fork and a join in a captured graph)
+  Fork fork{};
   DevBeam d{};
   PassScratch scr{};
   // device snapshots for Save/Restore (slot 0 initial, 1 intermediate)
@@ -269,6 +272,13 @@ hps_status hps_beam_create(uint32_t num, double mass, double charge, double curr
   hps_status s = HPS_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete b; return fail(HPS_ERR_CUDA, cudaGetErrorString(e)); }
+  b->fork.main = b->stream;
+  if ((e = cudaStreamCreateWithFlags(&b->fork.side, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->fork.ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->fork.ev_join, cudaEventDisableTiming)) != cudaSuccess) {
+    hps_beam_destroy(b);
+    return fail(HPS_ERR_CUDA, cudaGetErrorString(e));
+  }
   DevBeam &d = b->d;
   d.n = num; d.mass = mass; d.charge = charge;
   if (precision == HPS_PREC_FP64) {
@@ -302,6 +312,9 @@ hps_status hps_beam_destroy(hps_beam_t b) {
     if (b->save_loss[s]) cudaFree(b->save_loss[s]);
     if (b->save_lloss[s]) cudaFree(b->save_lloss[s]);
   }
+  if (b->fork.side) { cudaStreamSynchronize(b->fork.side); cudaStreamDestroy(b->fork.side); }
+  if (b->fork.ev_fork) cudaEventDestroy(b->fork.ev_fork);
+  if (b->fork.ev_join) cudaEventDestroy(b->fork.ev_join);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return HPS_OK;
@@ -1058,11 +1071,11 @@ void sc_apply(Ctx &c, double length, bool fused = false) {
     sc32_configure();
     if (fused) {
       PHASE(HPS_PROF_SC_STATS, sc32_stats_after_push(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
-      PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur));
+      PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur, &b->fork));
       return;
     }
     PHASE(HPS_PROF_SC_STATS, sc32_stats(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
-    PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur));
+    PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur, &b->fork));
     PHASE(HPS_PROF_SC_KICK, sc32_kick(b->d, c.sc->d, c.sc->t, a, b->stream));
     return;
   }

@@ -555,7 +555,7 @@ void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, con
 }
 
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
-               cudaStream_t st, const SurNet *sur) {
+               cudaStream_t st, const SurNet *sur, const Fork *fork) {
   ScTables u = tables32(t);
   if (a.adj_possible) {  // the mesh is sized from r_max only with adjacent bunches
     launch_pass_f(Op32AdjMesh{b, sc, u.c32, sc32_host(b, a)}, b.n, s, st);
@@ -588,6 +588,19 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
     sur_solve(b, sc, u, a, *sur, st, 1);
     k32_green<<<ngreen, kBlock, 0, st>>>(sc, u);
     note_launch();
+  } else if (fork && ndep) {
+    // the Green's table on the side stream, beside the deposit: it needs no
+    // shared memory, so its blocks take the warp slots the deposit's
+    // shared-memory histograms leave free (in one launch they would queue
+    // behind the deposit blocks, which size every block's shared memory)
+    const uint32_t ng = 4u * ngreen;
+    cudaEventRecord(fork->ev_fork, st);
+    cudaStreamWaitEvent(fork->side, fork->ev_fork, 0);
+    k32_green<<<ng, kBlock, 0, fork->side>>>(sc, u);
+    cudaEventRecord(fork->ev_join, fork->side);
+    launch_k(k32_green_deposit, dim3(ndep), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, 0u);
+    cudaStreamWaitEvent(st, fork->ev_join, 0);
+    note_launch(2);
   } else {
     launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
     note_launch();
