@@ -4,14 +4,18 @@
 // src/simulation/src/space_charge.cu:189-218).
 //
 // The sum E[zp][rp] = sum over bins (zs, rs) of q(zs, rs) g(rp, rs, zp - zs)
-// (g the sign-folded Green's table of contract.cuh) is, for the interior
-// points zp < nz, rp < nr, a matrix product
+// (g the sign-folded Green's table of contract.cuh) is, for the field rows
+// zp < nz, a matrix product
 //   D[zp][n] = sum over (rs, k) of A[zp][(rs, k)] B[(rs, k)][n],
 //   A[zp][(rs, k)] = q(zp - k, rs)   (zero outside the mesh),
-//   B[(rs, k)][n]  = g(rp, rs, k)    (n = 2 rp + component),
+//   B[(rs, k)][n]  = g(rp, rs, k)    (n = 2 rp + component, rp = 0 .. nr),
 // with k = zp - zs running over the folded range -(nz - 1) .. nz.  Each CTA
 // takes one 128-row tile of zp (the MMA's M) and one source radius rs: K =
-// the 127 + nz offsets that tile needs, in chunks of 64, N = 2 nr.
+// the 127 + nz offsets that tile needs, in chunks of 64, N = 2 (nr + 1)
+// rounded up to a multiple of 16 (the padding rows of B are zero).  The
+// last field row zp = nz needs offsets k = 1 .. nz only, which are all in
+// the last tile's chunks: that tile's producer threads sum it from the B
+// tiles while they are staged, one row of B (one (rp, component)) each.
 //
 // Precision: split BF16.  Both operands are written as hi = bf16(x), lo =
 // bf16(x - hi); the three products hi*hi + hi*lo + lo*hi are accumulated in
@@ -33,10 +37,8 @@
 // (about a second); a wait that gives up sets the solver's error word, and
 // the CTA drains its copies and MMAs before it frees the tensor memory.
 //
-// The per-radius partial tiles are summed in a fixed order by
-// k_tc_reduce, whose other blocks compute the last row (zp = nz) and
-// column (rp = nr) with CUDA cores from the FP32 table: results are
-// deterministic.
+// The per-radius partial tiles (and last-row partials) are summed in a
+// fixed order by k_tc_reduce: results are deterministic.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -54,24 +56,32 @@ constexpr int kTcThreads = 160;     // 4 producer / epilogue warps + 1 MMA warp
 constexpr int kTcProducers = 128;
 constexpr size_t kTcSmemMax = 227 * 1024;
 
-// meshes the tensor-core path takes: nz a multiple of the tile height, N =
-// 2 nr at most 256 (one MMA) and at least 32 (the smallest tensor-memory
-// allocation), powers of two as every SCHEFF mesh
+// meshes the tensor-core path takes: nz a multiple of the tile height, N
+// (below) at most 256 (one MMA), powers of two as every SCHEFF mesh
 __host__ __device__ inline bool tc_mesh_ok(uint32_t nr, uint32_t nz) {
-  return nz >= 128 && nz <= 512 && (nz & (nz - 1)) == 0 && nr >= 16 && nr <= 128 && (nr & (nr - 1)) == 0;
+  return nz >= 128 && nz <= 512 && (nz & (nz - 1)) == 0 && nr >= 16 && nr <= 64 && (nr & (nr - 1)) == 0;
+}
+// MMA columns: (E_r, E_z) of the nr + 1 field radii, rounded up to 16
+__host__ __device__ inline uint32_t tc_n(uint32_t nr) { return (2 * (nr + 1) + 15) / 16 * 16; }
+// tensor-memory columns: the power of two >= N (at least 32)
+__host__ __device__ inline uint32_t tc_tmem_cols(uint32_t N) {
+  uint32_t c = 32;
+  while (c < N) c *= 2;
+  return c;
 }
 
 // launch shape of one mesh
 struct TcDims {
   uint32_t nr, nz;
-  uint32_t N;        // 2 nr
+  uint32_t N;        // MMA columns, tc_n(nr)
+  uint32_t cols;     // tensor-memory columns allocated
   uint32_t NC;       // chunks of the folded range (2 nz / 64)
   uint32_t CPT;      // chunks a tile needs (nz / 64 + 2)
   uint32_t BT;       // bytes of one B tile (N rows x 128 B)
   uint32_t S;        // pipeline stages
   uint32_t L;        // elements of one shifted copy of the padded charge column
   uint32_t tiles;    // nz / 128
-  uint32_t red_blocks, edge_blocks;
+  uint32_t red_blocks;
   size_t smem;       // dynamic shared memory of k_contract_tc
 };
 
@@ -79,20 +89,22 @@ __host__ __device__ inline size_t tc_stage_bytes(uint32_t BT) { return 2 * 16384
 
 inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
   TcDims d{};
-  d.nr = nr; d.nz = nz; d.N = 2 * nr; d.NC = 2 * nz / kTcKC; d.CPT = nz / kTcKC + 2;
+  d.nr = nr; d.nz = nz; d.N = tc_n(nr); d.cols = tc_tmem_cols(d.N); d.NC = 2 * nz / kTcKC; d.CPT = nz / kTcKC + 2;
   d.BT = d.N * 128; d.L = nz + 264; d.tiles = nz / kTcM;
   // 256 bytes are left for the kernel's static shared memory (barriers)
   const size_t fixed = 1024 + (size_t)16 * d.L * 2 + (size_t)nz * 4 + 256;
   d.S = fixed + 3 * tc_stage_bytes(d.BT) <= kTcSmemMax ? 3 : 2;
   d.smem = fixed + d.S * tc_stage_bytes(d.BT);
-  d.red_blocks = (nz * nr + 255) / 256;
-  d.edge_blocks = nz + nr + 1;  // one block per edge point
+  d.red_blocks = ((nz + 1) * (nr + 1) + 255) / 256;  // one thread per field point
   return d;
 }
 
-// bytes of the folded split-BF16 table and of the partial tiles
-inline size_t tc_table_bytes(uint32_t nr, uint32_t nz) { return (size_t)nr * (2 * nz / kTcKC) * 2 * (2 * nr) * 128; }
-inline size_t tc_partial_bytes(uint32_t nr, uint32_t nz) { return (size_t)(nz / kTcM) * nr * (2 * nr) * kTcM * 4; }
+// bytes of the folded split-BF16 table and of the partials (tiles, then the
+// last row's per-radius partials)
+inline size_t tc_table_bytes(uint32_t nr, uint32_t nz) { return (size_t)nr * (2 * nz / kTcKC) * 2 * tc_n(nr) * 128; }
+inline size_t tc_partial_bytes(uint32_t nr, uint32_t nz) {
+  return ((size_t)(nz / kTcM) * nr * tc_n(nr) * kTcM + (size_t)nr * tc_n(nr)) * 4;
+}
 
 // the tensor-core path runs this kick: FP32 tables sized for this mesh
 __device__ inline bool tc_go(const ScState *sc, const ScTables &t) {
@@ -105,13 +117,13 @@ __host__ __device__ inline uint32_t tc_swz(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024 + (r & 7) * 128 + ((((j >> 3) ^ (r & 7)) & 7) << 4) + ((j & 7) << 1);
 }
 
-// the Green's kernel's share: entry (rp < nr, rs, dz) of component comp
+// the Green's kernel's share: entry (rp <= nr, rs, dz) of component comp
 // (value v, E_z already carrying its sign for k >= 1) at both folded
 // offsets k = dz + 1 and k = -dz (E_z negated there), hi and lo
 __device__ inline void tc_put_green(const ScTables &t, uint32_t nr, uint32_t nz, uint32_t rp, uint32_t rs,
                                     uint32_t dz, float er, float ez) {
   unsigned char *base = (unsigned char *)t.tcg;
-  const uint32_t NC = 2 * nz / kTcKC, BT = 2 * nr * 128;
+  const uint32_t NC = 2 * nz / kTcKC, BT = tc_n(nr) * 128;
   const uint32_t kid[2] = {dz + nz, nz - 1 - dz};
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
@@ -266,7 +278,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
   }
   if (warp == 4) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_slot)),
-                 "r"(N)
+                 "r"(d.cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     tc_fence_before();
@@ -309,6 +321,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
     const uint32_t m = tid;  // the A row this thread writes
+    // the last tile's threads also sum the last field row from B rows tid
+    // and tid + 128 (n < N) of the chunks of offsets 1 .. nz
+    const bool last_row = tile + 1 == d.tiles;
+    float lr0 = 0.0f, lr1 = 0.0f;
     for (uint32_t i = 0; i < nch && !*abort; ++i) {
       const uint32_t s = i % S, use = i / S;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort)) break;
@@ -334,6 +350,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
       }
       fence_async_smem();
       mbar_arrive(&full[s]);
+      const uint32_t c = c0 + i;  // this chunk's offsets: kidx = 64 c + j
+      if (last_row && c * kTcKC >= nz) {
+        // B landed (the phase also needs the tile's bytes); offset kidx
+        // k = kidx - (nz - 1) takes the charge of row zs = 2 nz - 1 - kidx
+        if (!mbar_wait(&full[s], use & 1, abort)) break;
+        const unsigned char *bh = st + 2 * 16384, *bl = bh + BT;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const uint32_t n = tid + 128 * half;
+          if (n >= N) continue;
+          const uint32_t row = (n >> 3) * 1024 + (n & 7) * 128;
+          float acc = 0.0f;
+#pragma unroll
+          for (uint32_t jj = 0; jj < 8; ++jj) {
+            const uint32_t off = row + (((jj ^ (n & 7)) & 7) << 4);
+            const uint4 vh = *(const uint4 *)(bh + off), vl = *(const uint4 *)(bl + off);
+            const __nv_bfloat16 *h8 = (const __nv_bfloat16 *)&vh, *l8 = (const __nv_bfloat16 *)&vl;
+#pragma unroll
+            for (uint32_t u = 0; u < 8; ++u) {
+              const uint32_t zs = 2 * nz - 1 - (c * kTcKC + 8 * jj + u);
+              acc = fmaf(qc[zs], __bfloat162float(h8[u]) + __bfloat162float(l8[u]), acc);
+            }
+          }
+          if (half == 0) lr0 += acc;
+          else lr1 += acc;
+        }
+      }
+    }
+    if (last_row && !*abort) {
+      float *pl = t.tcp + (size_t)d.tiles * nr * N * kTcM + (size_t)rs * N;
+      pl[tid] = lr0;
+      if (tid + 128 < N) pl[tid + 128] = lr1;
     }
   } else if (lane == 0) {
     // ---- the MMA thread ----
@@ -391,101 +439,55 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
   }
   if (warp == 4) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(d.cols) : "memory");
   }
 }
 
-// The partial tiles summed over the source radii in order (blocks [0,
-// red_blocks): one thread per interior point), and the last row and column
-// of the field table from the FP32 Green's table (the other blocks: one warp
-// per point, lanes over the bins, a fixed shuffle tree).
+// The partials summed over the source radii in radius order, one thread
+// per field point: tile partials for the rows zp < nz, the last tile's
+// last-row partials for zp = nz.
 __global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t, TcDims d) {
   if (!tc_go(sc, t)) return;
   const uint32_t nr = d.nr, nz = d.nz, N = d.N, nrow = nr + 1;
-  float *out = t.ffld2;
-  if (blockIdx.x < d.red_blocks) {
-    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= nz * nr) return;
-    const uint32_t rp = id / nz, zp = id % nz, tile = zp / kTcM, m = zp % kTcM;
-    const float *p = t.tcp + ((size_t)tile * nr * N + 2 * rp) * kTcM + m;
-    float ex = 0.0f, ez = 0.0f;
-    // nr is a multiple of 8: eight radii's loads in flight, summed in order
-    for (uint32_t g0 = 0; g0 < nr; g0 += 8) {
-      float vx[8], vz[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        vx[u] = __ldcg(p + (size_t)(g0 + u) * N * kTcM);
-        vz[u] = __ldcg(p + (size_t)(g0 + u) * N * kTcM + kTcM);
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        ex += vx[u];
-        ez += vz[u];
-      }
-    }
-    const size_t pt = (size_t)zp * nrow + rp;
-    out[2 * pt] = ex;
-    out[2 * pt + 1] = ez;
-    return;
+  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (nz + 1) * nrow) return;
+  const uint32_t rp = id / (nz + 1), zp = id % (nz + 1);
+  const float *p;
+  size_t stride, comp;
+  if (zp < nz) {
+    p = t.tcp + ((size_t)(zp / kTcM) * nr * N + 2 * rp) * kTcM + zp % kTcM;
+    stride = (size_t)N * kTcM;
+    comp = kTcM;
+  } else {
+    p = t.tcp + (size_t)d.tiles * nr * N * kTcM + 2 * rp;
+    stride = N;
+    comp = 1;
   }
-  // one block per edge point: the threads stride over the bins four at a
-  // time (loads in flight together), then a fixed shuffle tree and the
-  // warps in order
-  __shared__ float red[2][8];
-  const uint32_t e = blockIdx.x - d.red_blocks, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t zp = e <= nr ? nz : e - (nr + 1), rp = e <= nr ? e : nr;
-  const float2 *G = (const float2 *)t.ffld1 + (size_t)rp * nr * nz;  // [dz][rs]
-  const uint32_t nb = nr * nz;
-  float ax = 0.0f, az = 0.0f;
-  for (uint32_t k0 = threadIdx.x; k0 < nb; k0 += 4 * blockDim.x) {
-    float q[4];
-    float2 g[4];
-    bool below[4];
+  float ex = 0.0f, ez = 0.0f;
+  // nr is a multiple of 8: eight radii's loads in flight, summed in order
+  for (uint32_t g0 = 0; g0 < nr; g0 += 8) {
+    float vx[8], vz[8];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t k = k0 + u * blockDim.x;
-      q[u] = 0.0f;
-      g[u] = make_float2(0.0f, 0.0f);
-      below[u] = true;
-      if (k < nb) {
-        const uint32_t zs = k / nr, rs = k % nr;
-        const int kk = (int)zp - (int)zs;
-        below[u] = kk >= 1;
-        q[u] = tc_charge(__ldg(t.bin_fx + k));
-        g[u] = __ldg(G + (size_t)(below[u] ? kk - 1 : -kk) * nr + rs);
-      }
+    for (int u = 0; u < 8; ++u) {
+      vx[u] = __ldcg(p + (g0 + u) * stride);
+      vz[u] = __ldcg(p + (g0 + u) * stride + comp);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      ax = fmaf(q[u], g[u].x, ax);
-      az = fmaf(q[u], below[u] ? g[u].y : -g[u].y, az);
+    for (int u = 0; u < 8; ++u) {
+      ex += vx[u];
+      ez += vz[u];
     }
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    ax += __shfl_down_sync(0xffffffffu, ax, off);
-    az += __shfl_down_sync(0xffffffffu, az, off);
-  }
-  if (lane == 0) {
-    red[0][warp] = ax;
-    red[1][warp] = az;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float sx = 0.0f, sz = 0.0f;
-    for (uint32_t w = 0; w < blockDim.x / 32; ++w) {
-      sx += red[0][w];
-      sz += red[1][w];
-    }
-    const size_t pt = (size_t)zp * nrow + rp;
-    out[2 * pt] = sx;
-    out[2 * pt + 1] = sz;
-  }
+  const size_t pt = (size_t)zp * nrow + rp;
+  t.ffld2[2 * pt] = ex;
+  t.ffld2[2 * pt + 1] = ez;
 }
 
+// the dynamic shared-memory limit of the largest mesh the path takes (static
+// and dynamic shared memory together stay within the 227 KB a CTA may have)
 inline cudaError_t contract_tc_configure() {
   size_t most = 0;
-  for (uint32_t nr = 16; nr <= 128; nr *= 2)
+  for (uint32_t nr = 16; nr <= 64; nr *= 2)
     for (uint32_t nz = 128; nz <= 512; nz *= 2) most = std::max(most, tc_dims(nr, nz).smem);
   return cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
 }
@@ -494,7 +496,7 @@ inline cudaError_t contract_tc_configure() {
 inline void contract_tc_launch(const ScState *sc, const ScTables &t, uint32_t nr, uint32_t nz, cudaStream_t st) {
   const TcDims d = tc_dims(nr, nz);
   k_contract_tc<<<dim3(d.tiles, nr), kTcThreads, d.smem, st>>>(sc, t, d);
-  k_tc_reduce<<<d.red_blocks + d.edge_blocks, 256, 0, st>>>(sc, t, d);
+  k_tc_reduce<<<d.red_blocks, 256, 0, st>>>(sc, t, d);
 }
 
 }  // namespace

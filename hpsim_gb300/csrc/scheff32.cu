@@ -339,7 +339,7 @@ __device__ void green_blocks(const ScState *sc, const ScTables &t, uint32_t bid,
     // stored [rp][dz][rs] (rs fastest) for the contraction's lanes
     const float2 v = make_float2(c1 * g.er, c1 * g.ez);
     out[((size_t)rpi * nz + tz) * nr + kk] = v;
-    if (tc && rpi < nr) tc_put_green(t, nr, nz, rpi, kk, tz, v.x, v.y);
+    if (tc) tc_put_green(t, nr, nz, rpi, kk, tz, v.x, v.y);
   }
 }
 
@@ -375,7 +375,10 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
   namespace cg = cooperative_groups;
   const uint32_t nx = sc->nx, nz = sc->nz, nb = nx * nz;
   if (q.smem) {
-    for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) hist32[k] = 0;
+    if (nb % 4 == 0)
+      for (uint32_t k = threadIdx.x; k < nb / 4; k += blockDim.x) ((int4 *)hist32)[k] = make_int4(0, 0, 0, 0);
+    else
+      for (uint32_t k = threadIdx.x; k < nb; k += blockDim.x) hist32[k] = 0;
     __syncthreads();
   }
   const Sc32Consts &kc = *t.c32;
@@ -450,11 +453,36 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
   cg::cluster_group cl = cg::this_cluster();
   cl.sync();  // every histogram of the cluster is complete
   const uint32_t nc = cl.num_blocks(), r = cl.block_rank();
-  const uint32_t per = (nb + nc - 1) / nc, k0 = r * per, k1 = min(nb, k0 + per);
-  for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-    long long v = 0;  // up to nc block sums of < 2^30 each
-    for (uint32_t c = 0; c < nc; ++c) v += *cl.map_shared_rank(hist32 + k, c);
-    if (v) atomicAdd(t.bin_fx + k, (unsigned long long)(v * m));
+  if (nc == (uint32_t)kDepCluster && nb % (4 * kDepCluster) == 0) {
+    // slice r of the cluster's histograms, four bins per 16-byte load from
+    // every CTA of the cluster at once (all loads in flight together), the
+    // CTAs summed in rank order
+    const uint32_t per = nb / kDepCluster, k0 = r * per;
+    const int4 *src[kDepCluster];
+#pragma unroll
+    for (int c = 0; c < kDepCluster; ++c) src[c] = (const int4 *)cl.map_shared_rank(hist32 + k0, c);
+    for (uint32_t k4 = threadIdx.x; k4 < per / 4; k4 += blockDim.x) {
+      int4 v[kDepCluster];
+#pragma unroll
+      for (int c = 0; c < kDepCluster; ++c) v[c] = src[c][k4];
+      long long s0 = 0, s1 = 0, s2 = 0, s3 = 0;  // up to 8 block sums of < 2^30 each
+#pragma unroll
+      for (int c = 0; c < kDepCluster; ++c) {
+        s0 += v[c].x; s1 += v[c].y; s2 += v[c].z; s3 += v[c].w;
+      }
+      unsigned long long *dst = t.bin_fx + k0 + 4 * k4;
+      if (s0) atomicAdd(dst, (unsigned long long)(s0 * m));
+      if (s1) atomicAdd(dst + 1, (unsigned long long)(s1 * m));
+      if (s2) atomicAdd(dst + 2, (unsigned long long)(s2 * m));
+      if (s3) atomicAdd(dst + 3, (unsigned long long)(s3 * m));
+    }
+  } else {
+    const uint32_t per = (nb + nc - 1) / nc, k0 = r * per, k1 = min(nb, k0 + per);
+    for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      long long v = 0;  // up to nc block sums of < 2^30 each
+      for (uint32_t c = 0; c < nc; ++c) v += *cl.map_shared_rank(hist32 + k, c);
+      if (v) atomicAdd(t.bin_fx + k, (unsigned long long)(v * m));
+    }
   }
   cl.sync();  // no CTA leaves while the others read its histogram
 }
@@ -693,7 +721,7 @@ hps_status hps_scheff_field_f32_kernel(uint32_t nr, uint32_t nz, const double *b
   if (kernel == 2 && !tc_mesh_ok(nr, nz))
     return (hps_status)set_error(HPS_ERR_UNSUPPORTED,
                                  "scheff_field_f32: the tensor-core contraction takes nz in 128..512 and nr in "
-                                 "16..128 (powers of two)");
+                                 "16..64 (powers of two)");
   const bool tc = kernel == 2 || (kernel == 0 && tc_mesh_ok(nr, nz));
   sc32_configure();
   size_t nb = (size_t)nr * nz, n1 = (size_t)(nr + 1) * nr * nz * 2, n2 = (size_t)(nz + 1) * (nr + 1) * 2;
@@ -711,6 +739,8 @@ hps_status hps_scheff_field_f32_kernel(uint32_t nr, uint32_t nz, const double *b
   if (e == cudaSuccess) e = cudaMalloc((void **)&f1, n1 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void **)&f2, n2 * sizeof(float));
   if (e == cudaSuccess && tc) e = cudaMalloc(&tcg, tc_table_bytes(nr, nz));
+  // the padding rows of the MMA tiles (beyond the field's 2 (nr + 1) values) stay zero
+  if (e == cudaSuccess && tc) e = cudaMemset(tcg, 0, tc_table_bytes(nr, nz));
   if (e == cudaSuccess && tc) e = cudaMalloc((void **)&tcp, tc_partial_bytes(nr, nz));
   if (e == cudaSuccess) e = cudaMemset(sc, 0, sizeof(ScState));
   if (e == cudaSuccess) e = cudaMemset(c32, 0, sizeof(Sc32Consts));

@@ -196,7 +196,7 @@ hps_status hps_scheff_destroy(hps_scheff_t s);
  * (the element map before the kick could not certify them).
  * No reference counterpart: 10 the contraction kernel of FP32 beams (0, the
  * default: split-BF16 tensor cores where the mesh allows -- nz a power of
- * two in 128..512, nr in 16..128 -- else the FP32 ring convolution; 1: the
+ * two in 128..512, nr in 16..64 -- else the FP32 ring convolution; 1: the
  * ring convolution always); read-only: 11 the solver holds the tensor-core
  * buffers, 12 a bounded wait of the tensor-core kernel gave up (1). */
 hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
@@ -241,7 +241,7 @@ hps_status hps_scheff_field_f32(uint32_t nr, uint32_t nz, const double *bins, co
 /* hps_scheff_field_f32 with the contraction kernel chosen: 0 the one FP32
  * beams use for the mesh (the tensor cores where the mesh allows), 1 the
  * FP32 ring convolution on CUDA cores, 2 the split-BF16 tensor-core product
- * (tcgen05; nz a power of two in 128..512, nr in 16..128, else
+ * (tcgen05; nz a power of two in 128..512, nr in 16..64, else
  * HPS_ERR_UNSUPPORTED).  Same computation as UpdateFinalFldTblKernelCall,
  * src/simulation/src/space_charge.cu:189-218; the kernel choice has no
  * counterpart in the reference. */

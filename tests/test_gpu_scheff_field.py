@@ -125,7 +125,7 @@ def _bunched(nr, nz, sz=0.12, sr=0.25):
     return (np.round(q * 2 ** 20) / 2 ** 20).ravel()
 
 
-@pytest.mark.parametrize("nr,nz", [(16, 128), (32, 128), (32, 256), (64, 256), (128, 512)])
+@pytest.mark.parametrize("nr,nz", [(16, 128), (32, 128), (32, 256), (64, 256), (16, 512), (64, 512)])
 def test_tensor_core_contraction_against_fp64(nr, nz):
     """The split-BF16 tcgen05 contraction (kernel 2) on bunched and random
     charge tables: within 2e-5 of the largest field component of the FP64
@@ -152,7 +152,7 @@ def test_tensor_core_contraction_adjacent_bunches():
 def test_tensor_core_contraction_rejects_other_meshes():
     from hpsim_gb300._capi import HPSimError
     mesh = np.array([2.0e-4, 1.0e-4, 0.43, 805.0, 1048576, 1.6e-5, 0.0])
-    for nr, nz in ((8, 64), (8, 128), (32, 64)):
+    for nr, nz in ((8, 64), (8, 128), (32, 64), (128, 256)):
         with pytest.raises(HPSimError):
             field_f32_kernel(nr, nz, np.ones(nr * nz), mesh, 2)
         # the default kernel takes the FP32 ring convolution there
