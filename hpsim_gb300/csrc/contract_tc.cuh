@@ -379,8 +379,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
       }
     }
     if (last_row && !*abort) {
+      // rows n < N only: a thread beyond them would write into the next
+      // radius's partials
       float *pl = t.tcp + (size_t)d.tiles * nr * N * kTcM + (size_t)rs * N;
-      pl[tid] = lr0;
+      if (tid < N) pl[tid] = lr0;
       if (tid + 128 < N) pl[tid + 128] = lr1;
     }
   } else if (lane == 0) {
