@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--surrogate-tol", type=float, default=0.02)
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shapes instead of timing candidates before the warm-up")
+    p.add_argument("--shape", default=None,
+                   help="contraction,deposit_blocks_per_sm,sweep_blocks_per_sm: set this launch shape instead of "
+                        "tuning (reproducible profiling runs)")
     p.add_argument("--tune-elements", type=int, default=60,
                    help="the autotuner times runs over the lattice's first N elements")
     p.add_argument("--surrogate-batch", type=int, default=8,
@@ -673,7 +676,9 @@ def main():
     beam, bl, sc, sim = make_sim(args, elems, seed=12345 + rank)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     tune = None
-    if not args.no_autotune:
+    if args.shape:
+        sim.set_shape(dict(zip(HPSim.Simulator.SHAPE_KEYS, (int(v) for v in args.shape.split(",")))))
+    elif not args.no_autotune:
         t0 = time.perf_counter()
         tune = sim.autotune(0, min(n_elem, args.tune_elements) - 1, reps=3)
         tune["seconds"] = time.perf_counter() - t0

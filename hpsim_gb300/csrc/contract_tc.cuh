@@ -81,7 +81,6 @@ struct TcDims {
   uint32_t S;        // pipeline stages
   uint32_t L;        // elements of one shifted copy of the padded charge column
   uint32_t tiles;    // nz / 128
-  uint32_t red_blocks;
   size_t smem;       // dynamic shared memory of k_contract_tc
 };
 
@@ -95,7 +94,6 @@ inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
   const size_t fixed = 1024 + (size_t)16 * d.L * 2 + (size_t)nz * 4 + 256;
   d.S = fixed + 3 * tc_stage_bytes(d.BT) <= kTcSmemMax ? 3 : 2;
   d.smem = fixed + d.S * tc_stage_bytes(d.BT);
-  d.red_blocks = ((nz + 1) * (nr + 1) + 255) / 256;  // one thread per field point
   return d;
 }
 
@@ -445,44 +443,53 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
   }
 }
 
-// The partials summed over the source radii in radius order, one thread
-// per field point: tile partials for the rows zp < nz, the last tile's
-// last-row partials for zp = nz.
+// The partials summed over the source radii: a block takes 64 consecutive
+// field rows of one field radius (blockIdx.y), its four thread quarters a
+// quarter of the source radii each (rows adjacent in memory, so every load
+// of a warp is coalesced), summed in radius order within a quarter and the
+// quarters in order: deterministic.  Tile partials for the rows zp < nz, the
+// last tile's last-row partials for zp = nz.
 __global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t, TcDims d) {
   if (!tc_go(sc, t)) return;
+  __shared__ float red[2][4][64];
   const uint32_t nr = d.nr, nz = d.nz, N = d.N, nrow = nr + 1;
-  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= (nz + 1) * nrow) return;
-  const uint32_t rp = id / (nz + 1), zp = id % (nz + 1);
-  const float *p;
-  size_t stride, comp;
-  if (zp < nz) {
-    p = t.tcp + ((size_t)(zp / kTcM) * nr * N + 2 * rp) * kTcM + zp % kTcM;
-    stride = (size_t)N * kTcM;
-    comp = kTcM;
-  } else {
-    p = t.tcp + (size_t)d.tiles * nr * N * kTcM + 2 * rp;
-    stride = N;
-    comp = 1;
-  }
+  const uint32_t q = threadIdx.x / 64, ml = threadIdx.x % 64;
+  const uint32_t zp = blockIdx.x * 64 + ml, rp = blockIdx.y;
   float ex = 0.0f, ez = 0.0f;
-  // nr is a multiple of 8: eight radii's loads in flight, summed in order
-  for (uint32_t g0 = 0; g0 < nr; g0 += 8) {
-    float vx[8], vz[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      vx[u] = __ldcg(p + (g0 + u) * stride);
-      vz[u] = __ldcg(p + (g0 + u) * stride + comp);
+  if (zp <= nz) {
+    const float *p;
+    size_t stride, comp;
+    if (zp < nz) {
+      p = t.tcp + ((size_t)(zp / kTcM) * nr * N + 2 * rp) * kTcM + zp % kTcM;
+      stride = (size_t)N * kTcM;
+      comp = kTcM;
+    } else {
+      p = t.tcp + (size_t)d.tiles * nr * N * kTcM + 2 * rp;
+      stride = N;
+      comp = 1;
     }
+    const uint32_t per = nr / 4, g0 = q * per;  // nr >= 16: a multiple of 4 radii per quarter
+    for (uint32_t g = g0; g < g0 + per; g += 4) {
+      float vx[4], vz[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      ex += vx[u];
-      ez += vz[u];
+      for (int u = 0; u < 4; ++u) {
+        vx[u] = __ldcg(p + (g + u) * stride);
+        vz[u] = __ldcg(p + (g + u) * stride + comp);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ex += vx[u];
+        ez += vz[u];
+      }
     }
   }
+  red[0][q][ml] = ex;
+  red[1][q][ml] = ez;
+  __syncthreads();
+  if (q != 0 || zp > nz) return;
   const size_t pt = (size_t)zp * nrow + rp;
-  t.ffld2[2 * pt] = ex;
-  t.ffld2[2 * pt + 1] = ez;
+  t.ffld2[2 * pt] = ((red[0][0][ml] + red[0][1][ml]) + red[0][2][ml]) + red[0][3][ml];
+  t.ffld2[2 * pt + 1] = ((red[1][0][ml] + red[1][1][ml]) + red[1][2][ml]) + red[1][3][ml];
 }
 
 // the dynamic shared-memory limit of the largest mesh the path takes (static
@@ -498,7 +505,7 @@ inline cudaError_t contract_tc_configure() {
 inline void contract_tc_launch(const ScState *sc, const ScTables &t, uint32_t nr, uint32_t nz, cudaStream_t st) {
   const TcDims d = tc_dims(nr, nz);
   k_contract_tc<<<dim3(d.tiles, nr), kTcThreads, d.smem, st>>>(sc, t, d);
-  k_tc_reduce<<<d.red_blocks, 256, 0, st>>>(sc, t, d);
+  k_tc_reduce<<<dim3((nz + 1 + 63) / 64, nr + 1), 256, 0, st>>>(sc, t, d);
 }
 
 }  // namespace

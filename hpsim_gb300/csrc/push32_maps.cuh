@@ -244,11 +244,13 @@ struct Gap2Map {
     const float sinp1 = G.sinF * cd + G.cosF * sd, cosp1 = G.cosF * cd - G.sinF * sd;
     const float prome1 = -G.con1 * (tp * (sinp1 - G.sinps) + sp * (cosp1 - G.cosps));
     const float eps = delta + (prome1 - G.prome1_r);
-    float se, ce;
-    sincosf(eps, &se, &ce);
+    // sin and cos of eps from those of eps/2 (one evaluation instead of two;
+    // 2 sin^2(eps/2) = 1 - cos(eps) is the form dcos needs anyway)
+    float sh, ch;
+    sincosf(0.5f * eps, &sh, &ch);
+    const float se = 2.0f * sh * ch, omc = 2.0f * sh * sh, ce = 1.0f - omc;
     const float sinp = G.sinP * ce + G.cosP * se, cosp = G.cosP * ce - G.sinP * se;
-    const float sh = sinf(0.5f * eps);
-    const float dcos = -G.cosP * 2.0f * sh * sh - G.sinP * se;
+    const float dcos = -G.cosP * omc - G.sinP * se;
     const float rs_p = x * x + y * y, rrp = x * xp + y * yp;
     const float ris = sqrtf(rs_p), fkrris = G.fkr * ris;
     float b0m1;
