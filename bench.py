@@ -56,6 +56,9 @@ def parse():
                         "small-FODO topology in one graph launch; ccl_batch: 16 beams of 1,048,576 particles "
                         "through the CCL lattice with perturbed set points in one graph launch")
     p.add_argument("--beams", type=int, default=None, help="batched: 256, ccl_batch: 16")
+    p.add_argument("--lockstep", action="store_true",
+                   help="batches run in lockstep (one launch per kernel for all beams) instead of as per-simulator "
+                        "child graphs")
     p.add_argument("--surrogate", nargs="?", const=SURROGATE_NET, default=None,
                    help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
                         "(a network file; default the shipped 32x128 network), and report both")
@@ -454,6 +457,7 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
         sc.set_remesh_threshold(0.0)
         objs.append((beam, bl, sc, HPSim.Simulator(beam, bl, sc)))
     batch = HPSim.Batch([o[3] for o in objs])
+    batch.set_lockstep(args.lockstep)
     n_elem = len(base)
     total = sum(sb.num for sb in scan)
     tune = None
@@ -486,12 +490,14 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
         return mon
 
     plain_b, plain_ms = timed()
+    plain_mode = batch.last_mode()
     mon_plain = beam0_monitor()
     net = np.load(net_path)
     for o in objs:
         o[2].set_surrogate(net, tol=tol)
     stats0 = [o[2].surrogate_stats() for o in objs]
     sur_b, sur_ms = timed()
+    sur_mode = batch.last_mode()
     stats1 = [o[2].surrogate_stats() for o in objs]
     acc_n = sum(b[0] - a[0] for a, b in zip(stats0, stats1)) / args.steps / len(objs)
     rej_n = sum(b[1] - a[1] for a, b in zip(stats0, stats1)) / args.steps / len(objs)
@@ -503,6 +509,7 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
                       "quad gradients x U(0.97, 1.03)",
            "network": os.path.relpath(net_path, ROOT), "tol": tol,
            "launch_shape": objs[0][3].get_shape(), "autotune": tune,
+           "batch_form": {"plain": plain_mode[0], "surrogate": sur_mode[0], "surrogate_why": sur_mode[1] or None},
            "plain_single_value": plain_value, "plain_batched_value": plain_b, "plain_batched_ms_per_step": plain_ms,
            "surrogate_batched_value": sur_b, "surrogate_batched_ms_per_step": sur_ms,
            "surrogate_batched_over_plain": sur_b / plain_value, "plain_batched_over_plain": plain_b / plain_value,
@@ -583,6 +590,7 @@ def run_batched(args):
         sc.set_remesh_threshold(0.0)
         objs.append((beam, bl, sc, HPSim.Simulator(beam, bl, sc)))
     batch = HPSim.Batch([o[3] for o in objs])
+    batch.set_lockstep(args.lockstep)
     n_elem = len(objs[0][1])
     total = sum(sb.num for sb in scan)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
@@ -615,7 +623,20 @@ def run_batched(args):
     if ws > 1:
         torch.distributed.barrier()
     launches = HPSim.kernel_launch_count() - launches0
+    mode = batch.last_mode()
     t = slowest(sum(ms) / len(ms) / 1000.0, ws, device=f"cuda:{local}")
+    # the same step in the other batch form, for comparison
+    batch.set_lockstep(not args.lockstep)
+    for _ in range(2):
+        step()
+    other_ms = []
+    for _ in range(max(1, min(args.steps, 3))):
+        flush.zero_()
+        torch.cuda.synchronize()
+        other_ms.append(step())
+    other_mode = batch.last_mode()
+    t_other = slowest(sum(other_ms) / len(other_ms) / 1000.0, ws, device=f"cuda:{local}")
+    batch.set_lockstep(args.lockstep)
     # the same step with one simulate() per beam, one after another (each its
     # own graph launch), for comparison
     for o in objs:
@@ -643,7 +664,10 @@ def run_batched(args):
                        "parallelism": f"beams partitioned over {ws} GPU(s), balanced by particle count",
                        "elements": n_elem, "precision": args.precision,
                        "l2": "flushed between steps (256 MB write)",
-                       "launch_shape": objs[0][3].get_shape(), "autotune": tune},
+                       "launch_shape": objs[0][3].get_shape(), "autotune": tune,
+                       "batch_form": {"mode": mode[0], "why_not_lockstep": mode[1] or None}},
+            "other_batch_form": {"mode": other_mode[0], "ms_per_step": 1000 * t_other,
+                                 "value": all_total * n_elem / t_other},
             "sequential": {"ms_per_step": 1000 * t_seq, "value": total * n_elem / t_seq,
                            "note": "one simulate() per beam in turn, wall clock"},
             "e2e": None, "gpu_launches": int(launches), "clocks": clocks.summary()}

@@ -683,9 +683,11 @@ def kernel_launch_count():
 
 class Batch:
     """Addition (no reference counterpart): several simulators, each with its
-    own beam and SpaceCharge, advanced by one graph launch.  ``simulate``
-    takes the same start/end as Simulator.simulate; the results are those of
-    running each simulator alone."""
+    own beam and SpaceCharge, advanced by one graph launch of per-simulator
+    child graphs (or, with set_lockstep, one launch per kernel for all
+    beams when their launch sequences match).  ``simulate`` takes the same start/end as
+    Simulator.simulate; the results are those of running each simulator
+    alone."""
 
     def __init__(self, simulators):
         self._sims = list(simulators)  # keep the simulators (and their beams) alive
@@ -713,6 +715,20 @@ class Batch:
         v = C.c_double()
         call("hps_batch_last_time_ms", self._h, C.byref(v))
         return v.value
+
+    def set_lockstep(self, on=True):
+        """Lockstep form on or off (the default): one launch per kernel for
+        every beam when the simulators issue the same launch sequence, else a
+        graph of per-simulator child graphs (results agree to FP32
+        rounding)."""
+        call("hps_batch_set_lockstep", self._h, 1 if on else 0)
+
+    def last_mode(self):
+        """("lockstep", "") or ("graphs", why) for the last simulate."""
+        on = C.c_int()
+        why = C.create_string_buffer(256)
+        call("hps_batch_last_mode", self._h, C.byref(on), why, 256)
+        return ("lockstep", "") if on.value else ("graphs", why.value.decode())
 
     def autotune(self, start=None, end=None, reps=3):
         """Simulator.autotune for the whole batch (objective: the batch's

@@ -114,6 +114,8 @@ def lib():
         "hps_batch_destroy": (st, [vp]),
         "hps_batch_simulate": (st, [vp, i32, i32]),
         "hps_batch_last_time_ms": (st, [vp, dp]),
+        "hps_batch_set_lockstep": (st, [vp, i32]),
+        "hps_batch_last_mode": (st, [vp, ip, C.c_char_p, C.c_size_t]),
         "hps_sim_autotune": (st, [vp, i32, i32, i32, ip, dp, u32, C.POINTER(u32)]),
         "hps_batch_autotune": (st, [vp, i32, i32, i32, ip, dp, u32, C.POINTER(u32)]),
         "hps_sim_get_shape": (st, [vp, ip]),

@@ -22,6 +22,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "lockstep.cuh"
 
 namespace hps {
 namespace {
@@ -121,10 +122,10 @@ __device__ inline V cpair(T x, T y) { return V{x, y}; }
 // tiled form.
 template <class T, int TR, bool M, int S>
 __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables &t, T *sm,
-                                               typename CTab<T>::V (*upper)[kCG][kCP]) {
+                                               typename CTab<T>::V (*upper)[kCG][kCP], uint32_t bx, uint32_t by) {
   using V = typename CTab<T>::V;
   const uint32_t nx = sc->nx, nz = sc->nz, fld_sz = nx * nz, nrow = nx + 1;
-  const uint32_t rp = blockIdx.x, zb0 = blockIdx.y * kCZ * S;
+  const uint32_t rp = bx, zb0 = by * kCZ * S;
   const uint32_t tr = TR > 0 ? (uint32_t)TR : contract_tile<T, M>(nx, nz);
   V *gz = (V *)sm;                     // M: [k + nz - 1][tr]; else [dz][tr] holding g(dz + 1)
   T *qs = sm + (M ? 4 : 2) * nz * tr;  // [zs][tr]
@@ -261,17 +262,33 @@ __device__ __forceinline__ void contract_block(const ScState *sc, const ScTables
 // contract_smem<T>(nr_max, nz_max) bytes, M = contract_mirrored<T>(nr_max,
 // nz_max), S = contract_slabs<T>(nz_max)
 template <class T, bool M, int S>
-__global__ void __launch_bounds__(kContractThreads) k_contract_m(const ScState *sc, ScTables t) {
+__device__ __forceinline__ void contract_m_body(const ScState *sc, const ScTables &t, uint32_t bx, uint32_t by) {
   if (!sc->remesh || sc->sur_accepted) return;
   // FP32 tables of a tensor-core mesh: contract_tc.cuh's kernels take the solve
   if (sizeof(T) == 4 && t.tcg && sc->nx == t.tc_nr && sc->nz == t.tc_nz) return;
   const uint32_t nx = sc->nx, nz = sc->nz;
-  if (blockIdx.x > nx || blockIdx.y * kCZ * S > nz) return;
+  if (bx > nx || by * kCZ * S > nz) return;
   extern __shared__ __align__(16) unsigned char contract_raw[];
   __shared__ typename CTab<T>::V upper[S][kCG][kCP];  // second halves' sums
   T *sm = (T *)contract_raw;
-  if (nx == 32 && contract_tile<T, M>(nx, nz) == 32) contract_block<T, 32, M, S>(sc, t, sm, upper);
-  else contract_block<T, 0, M, S>(sc, t, sm, upper);
+  if (nx == 32 && contract_tile<T, M>(nx, nz) == 32) contract_block<T, 32, M, S>(sc, t, sm, upper, bx, by);
+  else contract_block<T, 0, M, S>(sc, t, sm, upper, bx, by);
+}
+
+template <class T, bool M, int S>
+__global__ void __launch_bounds__(kContractThreads) k_contract_m(const ScState *sc, ScTables t) {
+  contract_m_body<T, M, S>(sc, t, blockIdx.x, blockIdx.y);
+}
+
+// a solver's tables, one per beam of a lockstep launch (grid z: the beam)
+struct MeshSeg {
+  const ScState *sc;
+  ScTables t;
+};
+template <class T, bool M, int S, int B>
+__global__ void __launch_bounds__(kContractThreads) k_contract_m_seg(const __grid_constant__ SegArgs<MeshSeg, B> a) {
+  const MeshSeg &p = a.p[blockIdx.z];
+  contract_m_body<T, M, S>(p.sc, p.t, blockIdx.x, blockIdx.y);
 }
 
 // slabs per block: FP32 meshes of 256 rows and more have blocks enough to
@@ -281,8 +298,41 @@ inline int contract_slabs(uint32_t nz_max) { return sizeof(T) == 4 && nz_max >= 
 
 // the launch: the layout and slab count for the largest mesh the solver takes
 template <class T>
+inline void contract_m_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+  uint32_t dims[2];
+  std::memcpy(dims, recs[0]->p.data() + sizeof(MeshSeg), sizeof(dims));
+  const uint32_t nx_max = dims[0], nz_max = dims[1];
+  const int S = contract_slabs<T>(nz_max);
+  const size_t smem = contract_smem<T>(nx_max, nz_max);
+  const bool mir = contract_mirrored<T>(nx_max, nz_max);
+  std::vector<Rec> heads(recs.size());  // the MeshSeg heads of the records
+  std::vector<const Rec *> hp(recs.size());
+  for (size_t k = 0; k < recs.size(); ++k) {
+    heads[k].p.assign(recs[k]->p.begin(), recs[k]->p.begin() + sizeof(MeshSeg));
+    hp[k] = &heads[k];
+  }
+  seg_chunks<MeshSeg>(hp, [&](const auto &a, uint32_t) {
+    constexpr int B = std::decay_t<decltype(a)>::kB;
+    const dim3 cg(nx_max + 1, (nz_max + 1 + kCZ * S - 1) / (kCZ * S), a.nb);
+    if (S == 4) {
+      if (mir) k_contract_m_seg<T, true, 4, B><<<cg, kContractThreads, smem, st>>>(a);
+      else k_contract_m_seg<T, false, 4, B><<<cg, kContractThreads, smem, st>>>(a);
+    } else {
+      if (mir) k_contract_m_seg<T, true, 1, B><<<cg, kContractThreads, smem, st>>>(a);
+      else k_contract_m_seg<T, false, 1, B><<<cg, kContractThreads, smem, st>>>(a);
+    }
+  });
+}
+
+template <class T>
 inline void contract_launch(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max,
                             cudaStream_t st) {
+  if (recorder()) {  // a lockstep range: the solver's tables and the mesh
+    struct { MeshSeg m; uint32_t dims[2]; } p{{sc, t}, {nx_max, nz_max}};
+    static_assert(sizeof(p) >= sizeof(MeshSeg) + 2 * sizeof(uint32_t), "layout");
+    record("contract_m", &contract_m_merge<T>, 0, p, (uint64_t)p.dims[0] << 32 | p.dims[1]);
+    return;
+  }
   const int S = contract_slabs<T>(nz_max);
   const dim3 cg(nx_max + 1, (nz_max + 1 + kCZ * S - 1) / (kCZ * S));
   const size_t smem = contract_smem<T>(nx_max, nz_max);
@@ -296,12 +346,22 @@ inline void contract_launch(const ScState *sc, const ScTables &t, uint32_t nx_ma
   }
 }
 
+template <class T, int B>
+inline void contract_seg_configure() {
+  cudaFuncSetAttribute(k_contract_m_seg<T, true, 1, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m_seg<T, false, 1, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m_seg<T, true, 4, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  cudaFuncSetAttribute(k_contract_m_seg<T, false, 4, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+}
 template <class T>
 inline void contract_configure() {
   cudaFuncSetAttribute(k_contract_m<T, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
   cudaFuncSetAttribute(k_contract_m<T, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
   cudaFuncSetAttribute(k_contract_m<T, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
   cudaFuncSetAttribute(k_contract_m<T, false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+  contract_seg_configure<T, 4>();
+  contract_seg_configure<T, 16>();
+  contract_seg_configure<T, SegCap<MeshSeg>::value>();
 }
 
 }  // namespace

@@ -46,6 +46,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "contract.cuh"
 
 namespace hps {
 namespace {
@@ -245,15 +246,15 @@ __device__ __forceinline__ float tc_charge(unsigned long long v) {
 }
 
 // ---- the product ------------------------------------------------------------
-// grid (tiles, nr): tile blockIdx.x of field rows, source radius blockIdx.y
-__global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc, ScTables t, TcDims d) {
+// the CTA of field-row tile `tile` and source radius `rs`
+__device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTables &t, const TcDims &d,
+                                                 uint32_t tile, uint32_t rs) {
   if (!tc_go(sc, t)) return;
   extern __shared__ unsigned char tc_raw[];
   __shared__ uint64_t full[3], empty[3], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t tile = blockIdx.x, rs = blockIdx.y;
   const uint32_t N = d.N, nz = d.nz, nr = d.nr, S = d.S, BT = d.BT, L = d.L;
   // 1024-byte aligned stage buffers, then the shifted charge copies and the column
   unsigned char *sm = (unsigned char *)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
@@ -443,18 +444,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc
   }
 }
 
+// grid (tiles, nr): tile blockIdx.x of field rows, source radius blockIdx.y
+__global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc, ScTables t, TcDims d) {
+  contract_tc_body(sc, t, d, blockIdx.x, blockIdx.y);
+}
+// the lockstep form: grid z over the beams, one solver's tables each
+template <int B>
+__global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc_seg(const __grid_constant__ SegArgs<MeshSeg, B> a,
+                                                                 TcDims d) {
+  const MeshSeg &p = a.p[blockIdx.z];
+  contract_tc_body(p.sc, p.t, d, blockIdx.x, blockIdx.y);
+}
+
 // The partials summed over the source radii: a block takes 64 consecutive
 // field rows of one field radius (blockIdx.y), its four thread quarters a
 // quarter of the source radii each (rows adjacent in memory, so every load
 // of a warp is coalesced), summed in radius order within a quarter and the
 // quarters in order: deterministic.  Tile partials for the rows zp < nz, the
 // last tile's last-row partials for zp = nz.
-__global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t, TcDims d) {
+__device__ __forceinline__ void tc_reduce_body(const ScState *sc, const ScTables &t, const TcDims &d, uint32_t bx,
+                                               uint32_t by) {
   if (!tc_go(sc, t)) return;
   __shared__ float red[2][4][64];
   const uint32_t nr = d.nr, nz = d.nz, N = d.N, nrow = nr + 1;
   const uint32_t q = threadIdx.x / 64, ml = threadIdx.x % 64;
-  const uint32_t zp = blockIdx.x * 64 + ml, rp = blockIdx.y;
+  const uint32_t zp = bx * 64 + ml, rp = by;
   float ex = 0.0f, ez = 0.0f;
   if (zp <= nz) {
     const float *p;
@@ -492,17 +506,55 @@ __global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t
   t.ffld2[2 * pt + 1] = ((red[1][0][ml] + red[1][1][ml]) + red[1][2][ml]) + red[1][3][ml];
 }
 
+__global__ void __launch_bounds__(256) k_tc_reduce(const ScState *sc, ScTables t, TcDims d) {
+  tc_reduce_body(sc, t, d, blockIdx.x, blockIdx.y);
+}
+template <int B>
+__global__ void __launch_bounds__(256) k_tc_reduce_seg(const __grid_constant__ SegArgs<MeshSeg, B> a, TcDims d) {
+  const MeshSeg &p = a.p[blockIdx.z];
+  tc_reduce_body(p.sc, p.t, d, blockIdx.x, blockIdx.y);
+}
+
 // the dynamic shared-memory limit of the largest mesh the path takes (static
 // and dynamic shared memory together stay within the 227 KB a CTA may have)
 inline cudaError_t contract_tc_configure() {
   size_t most = 0;
   for (uint32_t nr = 16; nr <= 64; nr *= 2)
     for (uint32_t nz = 128; nz <= 512; nz *= 2) most = std::max(most, tc_dims(nr, nz).smem);
-  return cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  cudaError_t e = cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_contract_tc_seg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_contract_tc_seg<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_contract_tc_seg<SegCap<MeshSeg>::value>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)most);
+  return e;
+}
+
+inline void contract_tc_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+  uint32_t dims[2];
+  std::memcpy(dims, recs[0]->p.data() + sizeof(MeshSeg), sizeof(dims));
+  const uint32_t nr = dims[0], nz = dims[1];
+  const TcDims d = tc_dims(nr, nz);
+  std::vector<Rec> heads(recs.size());  // the MeshSeg heads of the records
+  std::vector<const Rec *> hp(recs.size());
+  for (size_t k = 0; k < recs.size(); ++k) {
+    heads[k].p.assign(recs[k]->p.begin(), recs[k]->p.begin() + sizeof(MeshSeg));
+    hp[k] = &heads[k];
+  }
+  seg_chunks<MeshSeg>(hp, [&](const auto &a, uint32_t) {
+    constexpr int B = std::decay_t<decltype(a)>::kB;
+    k_contract_tc_seg<B><<<dim3(d.tiles, nr, a.nb), kTcThreads, d.smem, st>>>(a, d);
+    k_tc_reduce_seg<B><<<dim3((nz + 1 + 63) / 64, nr + 1, a.nb), 256, 0, st>>>(a, d);
+  });
 }
 
 // both launches of a tensor-core solve on a mesh of nr x nz
 inline void contract_tc_launch(const ScState *sc, const ScTables &t, uint32_t nr, uint32_t nz, cudaStream_t st) {
+  if (recorder()) {
+    struct { MeshSeg m; uint32_t dims[2]; } p{{sc, t}, {nr, nz}};
+    record("contract_tc", &contract_tc_merge, 0, p, (uint64_t)p.dims[0] << 32 | p.dims[1]);
+    return;
+  }
   const TcDims d = tc_dims(nr, nz);
   k_contract_tc<<<dim3(d.tiles, nr), kTcThreads, d.smem, st>>>(sc, t, d);
   k_tc_reduce<<<dim3((nz + 1 + 63) / 64, nr + 1), 256, 0, st>>>(sc, t, d);

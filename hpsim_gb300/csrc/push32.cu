@@ -80,10 +80,11 @@ int sweep_grid(const void *kernel, uint32_t n, uint32_t cap) {
 }
 
 template <class Map>
-__global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m, Shift sh) {
+__device__ __forceinline__ void push_body(const DevBeam &b, const Map &m, const Shift &sh, uint32_t bid,
+                                          uint32_t nblk) {
   const bool moves = sh.dph != 0.0f || sh.dw != 0.0f;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < b.n; base += kSweepBatch * stride) {
+  const uint32_t stride = nblk * blockDim.x;
+  for (uint32_t base = bid * blockDim.x + threadIdx.x; base < b.n; base += kSweepBatch * stride) {
     Part p[kSweepBatch];
 #pragma unroll
     for (int u = 0; u < kSweepBatch; ++u)
@@ -95,6 +96,11 @@ __global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m, Shift sh) {
       store_part(b, i, p[u], step(p[u], m, sh));
     }
   }
+}
+
+template <class Map>
+__global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m, Shift sh) {
+  push_body(b, m, sh, blockIdx.x, gridDim.x);
 }
 
 // The map, then every statistic the SCHEFF kick after it takes from the new
@@ -198,12 +204,13 @@ struct OpPushScStats {
 // ApplySpchKickKernel on the particles it kicks (alive, not longitudinally
 // lost, outside the skipped set), then the map on every live particle
 template <class Map>
-__global__ void __launch_bounds__(kBlock) k32_kick_push(DevBeam b, const ScState *sc, ScTables t, RefK rk,
-                                                       uint64_t skip_mask, Map m, Shift sh) {
+__device__ __forceinline__ void kick_push_body(const DevBeam &b, const ScState *sc, const ScTables &t, const RefK &rk,
+                                               uint64_t skip_mask, const Map &m, const Shift &sh, uint32_t bid,
+                                               uint32_t nblk) {
   const KickEnv e = kick_env(sc, t, rk);
   const bool moves = sh.dph != 0.0f || sh.dw != 0.0f;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < b.n; base += kSweepBatch * stride) {
+  const uint32_t stride = nblk * blockDim.x;
+  for (uint32_t base = bid * blockDim.x + threadIdx.x; base < b.n; base += kSweepBatch * stride) {
     Part p[kSweepBatch];
     uint32_t ll[kSweepBatch];
 #pragma unroll
@@ -227,12 +234,74 @@ __global__ void __launch_bounds__(kBlock) k32_kick_push(DevBeam b, const ScState
   }
 }
 
+template <class Map>
+__global__ void __launch_bounds__(kBlock) k32_kick_push(DevBeam b, const ScState *sc, ScTables t, RefK rk,
+                                                       uint64_t skip_mask, Map m, Shift sh) {
+  kick_push_body(b, sc, t, rk, skip_mask, m, sh, blockIdx.x, gridDim.x);
+}
+
+// lockstep forms: one beam's share of a merged launch
+template <class Map>
+struct PushSeg {
+  DevBeam b;
+  Map m;
+  Shift sh;
+};
+template <class Map, int B>
+__global__ void __launch_bounds__(kBlock) k32_push_seg(const __grid_constant__ SegArgs<PushSeg<Map>, B> a) {
+  uint32_t bid, nblk;
+  const PushSeg<Map> &p = a.p[seg_find(a, blockIdx.x, bid, nblk)];
+  push_body(p.b, p.m, p.sh, bid, nblk);
+}
+template <class Map>
+struct KickPushSeg {
+  DevBeam b;
+  const ScState *sc;
+  ScTables t;
+  RefK rk;
+  uint64_t skip_mask;
+  Map m;
+  Shift sh;
+};
+template <class Map, int B>
+__global__ void __launch_bounds__(kBlock) k32_kick_push_seg(const __grid_constant__ SegArgs<KickPushSeg<Map>, B> a) {
+  uint32_t bid, nblk;
+  const KickPushSeg<Map> &p = a.p[seg_find(a, blockIdx.x, bid, nblk)];
+  kick_push_body(p.b, p.sc, p.t, p.rk, p.skip_mask, p.m, p.sh, bid, nblk);
+}
+template <class Map>
+void push_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+  seg_chunks<PushSeg<Map>>(recs, [&](const auto &a, uint32_t blocks) {
+    k32_push_seg<Map, std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
+  });
+}
+template <class Map>
+void kick_push_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+  seg_chunks<KickPushSeg<Map>>(recs, [&](const auto &a, uint32_t blocks) {
+    k32_kick_push_seg<Map, std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
+  });
+}
+
 // b carries the synchronous particle after the element; rk is it before
 // (the kick of PUSH_AFTER_KICK happens there), phi0 / w0 its phase and energy
 template <class Map>
 void launch_map(const DevBeam &b, const Map &m, const RefK &rk, double phi0, double w0, cudaStream_t st,
                 const PushFuse *pf) {
   const Shift sh{(float)(b.phi_ref - phi0), (float)(b.w_ref - w0)};
+  if (recorder()) {  // a lockstep range is being recorded
+    if (!pf) {
+      record("push", &push_merge<Map>, (uint32_t)sweep_grid((const void *)k32_push<Map>, b.n, b.sweep_cap),
+             PushSeg<Map>{b, m, sh});
+    } else if (pf->mode == PUSH_SCSTATS) {
+      launch_pass_f(OpPushScStats<Map>{b, m, sh, pf->s_last, pf->sc, pf->t, pf->freq, pf->frac, pf->h}, b.n, pf->scr,
+                    st, b.sweep_cap, "push_scstats");
+    } else {
+      record("kick_push", &kick_push_merge<Map>,
+             (uint32_t)sweep_grid((const void *)k32_kick_push<Map>, b.n, b.sweep_cap),
+             KickPushSeg<Map>{b, (const ScState *)pf->sc, pf->t, rk, pf->skip_mask, m, sh});
+    }
+    return;
+  }
   if (!pf) {
     launch_k(k32_push<Map>, dim3(sweep_grid((const void *)k32_push<Map>, b.n, b.sweep_cap)), dim3(kBlock), 0, st, b,
              m, sh);
@@ -246,9 +315,19 @@ void launch_map(const DevBeam &b, const Map &m, const RefK &rk, double phi0, dou
   note_launch();
 }
 
-__global__ void k32_aperture(DevBeam b, int rect, float aper, float xl, float xr, float yt, float yb, uint32_t eid) {
-  float cx = (float)b.st->st[X_AVG], cy = (float)b.st->st[Y_AVG];
-  PARTICLES(b) {
+struct AptArgs {
+  DevBeam b;
+  int rect;
+  float aper, xl, xr, yt, yb;
+  uint32_t eid;
+};
+__device__ __forceinline__ void aperture_body(const AptArgs &a, uint32_t bid, uint32_t nblk) {
+  const DevBeam &b = a.b;
+  const float cx = (float)b.st->st[X_AVG], cy = (float)b.st->st[Y_AVG];
+  const int rect = a.rect;
+  const float aper = a.aper, xl = a.xl, xr = a.xr, yt = a.yt, yb = a.yb;
+  const uint32_t eid = a.eid;
+  for (uint32_t i = bid * blockDim.x + threadIdx.x; i < b.n; i += nblk * blockDim.x) {
     const uint32_t lo = b.loss[i];
     const float x = b.fx[i], y = b.fy[i];
     if (i == 0 || lo != 0u) continue;
@@ -259,6 +338,17 @@ __global__ void k32_aperture(DevBeam b, int rect, float aper, float xl, float xr
       b.loss[i] = eid;
     }
   }
+}
+__global__ void k32_aperture(AptArgs a) { aperture_body(a, blockIdx.x, gridDim.x); }
+template <int B>
+__global__ void k32_aperture_seg(const __grid_constant__ SegArgs<AptArgs, B> a) {
+  uint32_t bid, nblk;
+  aperture_body(a.p[seg_find(a, blockIdx.x, bid, nblk)], bid, nblk);
+}
+void aperture_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+  seg_chunks<AptArgs>(recs, [&](const auto &a, uint32_t blocks) {
+    k32_aperture_seg<std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
+  });
 }
 
 // T(beta) = sum_k a_k beta^k re-expanded as sum_j c_j (beta - b0)^j
@@ -522,8 +612,13 @@ void push32_rotation(DevBeam &b, double angle, cudaStream_t st) {
 }
 
 void push32_aperture(DevBeam &b, int rect, const double *p, uint32_t eid, cudaStream_t st) {
-  launch_k(k32_aperture, dim3(grid_for(b.n)), dim3(kBlock), 0, st, b, rect, (float)p[HPS_P_APERTURE],
-             (float)p[HPS_P_APT_XL], (float)p[HPS_P_APT_XR], (float)p[HPS_P_APT_YT], (float)p[HPS_P_APT_YB], eid);
+  const AptArgs a{b, rect, (float)p[HPS_P_APERTURE], (float)p[HPS_P_APT_XL], (float)p[HPS_P_APT_XR],
+                  (float)p[HPS_P_APT_YT], (float)p[HPS_P_APT_YB], eid};
+  if (recorder()) {
+    record("aperture", &aperture_merge, (uint32_t)grid_for(b.n), a);
+    return;
+  }
+  launch_k(k32_aperture, dim3(grid_for(b.n)), dim3(kBlock), 0, st, a);
   note_launch();
 }
 

@@ -18,6 +18,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "lockstep.cuh"
 
 namespace hps {
 
@@ -156,8 +157,9 @@ __device__ inline float comb_k(int k, float a, float b) {
   return k >= MF ? fmaxf(a, b) : C::comb(a, b);
 }
 
+// block bid of nblk blocks of the pass over particles 0..n-1
 template <class Op>
-__global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
+__device__ __forceinline__ void pass_body_f(const Op &op, uint32_t n, PassScratch scr, uint32_t bid, uint32_t nblk) {
   constexpr int K = Op::K;
   constexpr int B = op_batch<Op>::value;
   using C = typename Op::Comb;
@@ -174,8 +176,8 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
   float acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = k >= MF ? -INFINITY : 0.0f;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += B * stride) {
+  const uint32_t stride = nblk * blockDim.x;
+  for (uint32_t base = bid * blockDim.x + threadIdx.x; base < n; base += B * stride) {
     typename Op::P p[B];
 #pragma unroll
     for (int u = 0; u < B; ++u) {
@@ -209,18 +211,18 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
       const int k = threadIdx.x;
       float v = k >= MF ? -INFINITY : 0.0f;
       for (int w = 0; w < kBlock / 32; ++w) v = comb_k<C, MF>(k, v, smf[w][k]);
-      partf[blockIdx.x * K + k] = v;
+      partf[bid * K + k] = v;
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == nblk - 1);
     __syncthreads();
     if (!is_last) return;
     __threadfence();
     // warp w combines slots w, w + 8, ...: the slots' chains run side by side
     for (int k = warp; k < K; k += kBlock / 32) {
       float v = k >= MF ? -INFINITY : 0.0f;
-      for (uint32_t b = lane; b < gridDim.x; b += 32) v = comb_k<C, MF>(k, v, __ldcg(partf + (size_t)b * K + k));
+      for (uint32_t b = lane; b < nblk; b += 32) v = comb_k<C, MF>(k, v, __ldcg(partf + (size_t)b * K + k));
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v = comb_k<C, MF>(k, v, __shfl_down_sync(0xffffffffu, v, off));
       if (lane == 0) tot[k] = (double)v;
@@ -238,19 +240,54 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassS
     if (threadIdx.x < K) {
       double v = C::ident();
       for (int w = 0; w < kBlock / 32; ++w) v = C::comb(v, sm[w][threadIdx.x]);
-      scr.part[blockIdx.x * K + threadIdx.x] = v;
+      scr.part[bid * K + threadIdx.x] = v;
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) is_last = (atomicAdd(scr.counter, 1u) == nblk - 1);
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    combine_partials<C, K>(scr.part, gridDim.x, sm, tot);
+    combine_partials<C, K>(scr.part, nblk, sm, tot);
   }
   op.finalize(tot, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) *scr.counter = 0u;
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
+  pass_body_f(op, n, scr, blockIdx.x, gridDim.x);
+}
+
+// one beam's share of a lockstep launch of pass_kernel_f
+template <class Op>
+struct PassSeg {
+  Op op;
+  uint32_t n;
+  PassScratch scr;
+};
+template <class Op, int B>
+__global__ void __launch_bounds__(kBlock) pass_kernel_f_seg(const __grid_constant__ SegArgs<PassSeg<Op>, B> a) {
+  uint32_t bid, nblk;
+  const PassSeg<Op> &p = a.p[seg_find(a, blockIdx.x, bid, nblk)];
+  pass_body_f(p.op, p.n, p.scr, bid, nblk);
+}
+template <class Op>
+inline void pass_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+  seg_chunks<PassSeg<Op>>(recs, [&](const auto &a, uint32_t blocks) {
+    pass_kernel_f_seg<Op, std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
+  });
+}
+// a pass_kernel_f launch of `blocks` blocks, or its record under a lockstep recorder
+template <class Op>
+inline void launch_pass_f_grid(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s, uint32_t blocks,
+                               const char *site) {
+  if (recorder()) {
+    record(site, &pass_merge<Op>, blocks, PassSeg<Op>{op, n, scr});
+    return;
+  }
+  launch_k(pass_kernel_f<Op>, dim3(blocks), dim3(kBlock), 0, s, op, n, scr);
 }
 
 // With the FP64 combine, at most two blocks per SM: the last block sums
@@ -276,10 +313,11 @@ inline int pass_resident() {
 
 // cap: at most this many blocks per SM (0: no cap)
 template <class Op>
-inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s, uint32_t cap = 0) {
+inline void launch_pass_f(const Op &op, uint32_t n, PassScratch scr, cudaStream_t s, uint32_t cap = 0,
+                          const char *site = "pass") {
   int per_sm = op_fast<Op>::value ? pass_resident<Op>() : 2;
   if (cap && (uint32_t)per_sm > cap) per_sm = (int)cap;
-  launch_k(pass_kernel_f<Op>, dim3(pass_blocks_f(n, per_sm)), dim3(kBlock), 0, s, op, n, scr);
+  launch_pass_f_grid(op, n, scr, s, (uint32_t)pass_blocks_f(n, per_sm), site);
 }
 
 // FP32 version of rel_phase for offsets that are already small

@@ -23,11 +23,17 @@
 
 #include "../../include/hpsim_gb300.h"
 #include "internal.h"
+#include "lockstep.cuh"
 
 namespace hps {
 
 static std::atomic<uint64_t> g_launches{0};
-void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+static thread_local Recorder *g_recorder = nullptr;
+Recorder *&recorder() { return g_recorder; }
+// launches handed to a lockstep recorder are counted when the merged graph runs
+void note_launch(int n) {
+  if (!g_recorder) g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed);
+}
 
 static thread_local std::string g_err;
 
@@ -143,6 +149,13 @@ struct hps_sim_s {
 
 // Many simulators run as one graph launch: each simulator's captured range
 // is a child graph of one parent graph, with no edges between them.
+// The host-side state of a simulator that a range advances (engine, beam
+// and solver fields), saved and put back around a lockstep recording.
+struct HostState {
+  double design_w, wavelen, beam_freq, beam_current, beam_design_w, phi_ref, w_ref, fraction, interval;
+  uint32_t ccl_cell_num, cur_id;
+};
+
 struct hps_batch_s {
   std::vector<hps_sim_t> sims;
   cudaStream_t stream = nullptr;
@@ -150,6 +163,15 @@ struct hps_batch_s {
   std::vector<uint64_t> serials;  // the child captures the parent was built from
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  // lockstep form (lockstep.cuh): one launch per kernel for every beam
+  bool lockstep = false;
+  int last_mode = 0;                 // 1: the last range ran in lockstep
+  std::string ls_why;                // why it did not
+  cudaStream_t side = nullptr;       // the Green's-table branch
+  cudaGraphExec_t ls_exec = nullptr;
+  uint64_t ls_key = 0, ls_nodes = 0;
+  std::vector<HostState> ls_after;   // every simulator's host state after the range
+  Arena arena;
 };
 
 // ---------------------------------------------------------------------------
@@ -1590,6 +1612,9 @@ hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *
   hps_batch_t bt = new hps_batch_s();
   bt->sims = v;
   if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&bt->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&bt->arena.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&bt->arena.ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&bt->ev0) != cudaSuccess || cudaEventCreate(&bt->ev1) != cudaSuccess) {
     hps_batch_destroy(bt);
     return fail(HPS_ERR_CUDA, "batch_create: stream or events");
@@ -1602,6 +1627,10 @@ hps_status hps_batch_destroy(hps_batch_t bt) {
   if (!bt) return HPS_OK;
   if (bt->stream) cudaStreamSynchronize(bt->stream);
   if (bt->exec) cudaGraphExecDestroy(bt->exec);
+  if (bt->ls_exec) cudaGraphExecDestroy(bt->ls_exec);
+  if (bt->arena.ev_fork) cudaEventDestroy(bt->arena.ev_fork);
+  if (bt->arena.ev_join) cudaEventDestroy(bt->arena.ev_join);
+  if (bt->side) cudaStreamDestroy(bt->side);
   if (bt->ev0) cudaEventDestroy(bt->ev0);
   if (bt->ev1) cudaEventDestroy(bt->ev1);
   if (bt->stream) cudaStreamDestroy(bt->stream);
@@ -1612,6 +1641,138 @@ hps_status hps_batch_destroy(hps_batch_t bt) {
 // Simulator::Simulate(start, end) on every simulator of the batch in one
 // graph launch.  Each simulator must be able to run as a graph (graphs on,
 // profiling off, no mesh-size cut-off energy).
+}  // extern "C"
+
+namespace {
+
+HostState host_get(hps_sim_t s) {
+  HostState h;
+  hps_beam_t b = s->beam;
+  h.design_w = s->design_w; h.wavelen = s->wavelen; h.ccl_cell_num = s->ccl_cell_num; h.cur_id = s->cur_id;
+  h.beam_freq = b->freq; h.beam_current = b->current; h.beam_design_w = b->design_w;
+  h.phi_ref = b->d.phi_ref; h.w_ref = b->d.w_ref;
+  h.fraction = s->sc ? s->sc->fraction : 0.0;
+  h.interval = s->sc ? s->sc->interval : 0.0;
+  return h;
+}
+void host_put(hps_sim_t s, const HostState &h) {
+  hps_beam_t b = s->beam;
+  s->design_w = h.design_w; s->wavelen = h.wavelen; s->ccl_cell_num = h.ccl_cell_num; s->cur_id = h.cur_id;
+  b->freq = h.beam_freq; b->current = h.beam_current; b->design_w = h.beam_design_w;
+  b->d.phi_ref = h.phi_ref; b->d.w_ref = h.w_ref;
+  if (s->sc) { s->sc->fraction = h.fraction; s->sc->interval = h.interval; }
+}
+
+// The batch's range in lockstep (lockstep.cuh): the cached graph when every
+// simulator's plan matches, else each simulator's range recorded (its launches
+// handed to the recorder; a stray launch is swallowed by a throw-away stream
+// capture and makes the batch fall back), the records merged into one
+// captured graph.  *ran = false: the range has a launch without a lockstep
+// form (every simulator's host state is put back).  Nothing is launched.
+hps_status lockstep_prepare(hps_batch_t bt, std::vector<RunPlan> &plans, bool *ran) {
+  const size_t m = bt->sims.size();
+  *ran = false;
+  uint64_t key = 0x6c6f636b73746570ull;
+  for (const RunPlan &p : plans) key = mix(key, p.key);
+  if (bt->ls_exec && key == bt->ls_key) {
+    for (size_t k = 0; k < m; ++k) host_put(bt->sims[k], bt->ls_after[k]);
+    note_launch((int)bt->ls_nodes);
+    *ran = true;
+    return HPS_OK;
+  }
+  std::vector<HostState> before(m);
+  for (size_t k = 0; k < m; ++k) before[k] = host_get(bt->sims[k]);
+  std::vector<Recorder> recs(m);
+  std::string why;
+  for (size_t k = 0; k < m && why.empty(); ++k) {
+    const RunPlan &p = plans[k];
+    cudaStream_t st = bt->sims[k]->beam->stream;
+    recorder() = &recs[k];
+    const cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    hps_status e = HPS_OK;
+    if (ce == cudaSuccess) {
+      RunPlan q = p;
+      e = run_range(q.c, q.start_index, q.end_index, false);
+    }
+    cudaGraph_t junk = nullptr;
+    const cudaError_t ee = ce == cudaSuccess ? cudaStreamEndCapture(st, &junk) : ce;
+    size_t stray = 0;  // work that went to the stream instead of the recorder
+    if (junk) {
+      cudaGraphGetNodes(junk, nullptr, &stray);
+      cudaGraphDestroy(junk);
+    }
+    recorder() = nullptr;
+    cudaGetLastError();
+    if (e || ce != cudaSuccess || ee != cudaSuccess) why = "recording the range failed";
+    else if (!recs[k].unsupported.empty()) why = recs[k].unsupported;
+    else if (stray) why = "a launch or copy without a lockstep form";
+  }
+  for (size_t k = 1; k < m && why.empty(); ++k) {
+    if (recs[k].recs.size() != recs[0].recs.size()) { why = "the simulators' launch sequences differ"; break; }
+    for (size_t j = 0; j < recs[0].recs.size(); ++j)
+      if (recs[k].recs[j].merge != recs[0].recs[j].merge || recs[k].recs[j].p.size() != recs[0].recs[j].p.size() ||
+          recs[k].recs[j].shape != recs[0].recs[j].shape) {
+        why = "the simulators' launch sequences differ";
+        break;
+      }
+  }
+  if (recs.empty() || recs[0].recs.empty()) why = why.empty() ? "nothing to launch" : why;
+  if (!why.empty()) {
+    for (size_t k = 0; k < m; ++k) host_put(bt->sims[k], before[k]);
+    bt->ls_why = why;
+    return HPS_OK;
+  }
+  std::vector<HostState> after(m);
+  for (size_t k = 0; k < m; ++k) after[k] = host_get(bt->sims[k]);
+  Arena &a = bt->arena;
+  auto merge_all = [&]() {
+    std::vector<const Rec *> v(m);
+    for (size_t j = 0; j < recs[0].recs.size(); ++j) {
+      for (size_t k = 0; k < m; ++k) v[k] = &recs[k].recs[j];
+      v[0]->merge(v, a, bt->stream, bt->side);
+    }
+  };
+  cudaGraph_t gr = nullptr;
+  CK(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+  merge_all();
+  const cudaError_t ce = cudaStreamEndCapture(bt->stream, &gr);
+  if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("lockstep capture: ") + cudaGetErrorString(ce));
+  size_t nodes = 0;
+  cudaGraphGetNodes(gr, nullptr, &nodes);
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&ex, gr, 0);
+  cudaGraphDestroy(gr);
+  if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("lockstep instantiate: ") + cudaGetErrorString(ie));
+  if (bt->ls_exec) cudaGraphExecDestroy(bt->ls_exec);
+  bt->ls_exec = ex;
+  bt->ls_key = key;
+  bt->ls_nodes = nodes;
+  bt->ls_after = after;
+  note_launch((int)nodes);
+  *ran = true;
+  return HPS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hps_status hps_batch_set_lockstep(hps_batch_t bt, int on) {
+  if (!bt) return fail(HPS_ERR_INVALID, "bad batch handle");
+  bt->lockstep = on != 0;
+  return HPS_OK;
+}
+
+hps_status hps_batch_last_mode(hps_batch_t bt, int *lockstep, char *why, size_t why_cap) {
+  if (!bt || !lockstep) return fail(HPS_ERR_INVALID, "bad argument");
+  *lockstep = bt->last_mode;
+  if (why && why_cap) {
+    std::strncpy(why, bt->last_mode ? "" : bt->ls_why.c_str(), why_cap - 1);
+    why[why_cap - 1] = 0;
+  }
+  return HPS_OK;
+}
+
 hps_status hps_batch_simulate(hps_batch_t bt, int32_t start, int32_t end) {
   if (!bt) return fail(HPS_ERR_INVALID, "bad batch handle");
   const size_t m = bt->sims.size();
@@ -1623,6 +1784,31 @@ hps_status hps_batch_simulate(hps_batch_t bt, int32_t start, int32_t end) {
     if (!plans[k].empty && !plans[k].graph)
       return fail(HPS_ERR_STATE, "batch_simulate: a simulator cannot run as a graph (graphs off, profiling on, "
                                  "or a mesh-size cut-off energy)");
+  }
+  bool ls = bt->lockstep && m > 1;
+  for (const RunPlan &p : plans)
+    if (p.empty || p.monitor) ls = false;
+  if (!ls) bt->ls_why = bt->lockstep ? "a simulator records monitors or has an empty range, or one simulator"
+                                     : "lockstep switched off";
+  bt->last_mode = 0;
+  if (ls) {
+    bool ran = false;
+    hps_status e = lockstep_prepare(bt, plans, &ran);
+    if (e) return e;
+    if (ran) {
+      CK(cudaEventRecord(bt->ev0, bt->stream));
+      CK(cudaGraphLaunch(bt->ls_exec, bt->stream));
+      CK(cudaEventRecord(bt->ev1, bt->stream));
+      e = last_launch_status("batch_simulate");
+      if (e) return e;
+      CK(cudaStreamSynchronize(bt->stream));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, bt->ev0, bt->ev1);
+      bt->last_ms = ms;
+      for (size_t k = 0; k < m; ++k) bt->sims[k]->last_ms = ms;
+      bt->last_mode = 1;
+      return HPS_OK;
+    }
   }
   std::vector<uint64_t> serials(m, 0);
   for (size_t k = 0; k < m; ++k) {
@@ -1889,7 +2075,8 @@ hps_status hps_sim_autotune(hps_sim_t s, int32_t start, int32_t end, int32_t rep
 hps_status hps_batch_autotune(hps_batch_t bt, int32_t start, int32_t end, int32_t reps, int32_t *shape_out,
                               double *ms_out, uint32_t ms_cap, uint32_t *n_timed) {
   if (!bt || bt->sims.empty() || reps < 1 || reps > 64) return fail(HPS_ERR_INVALID, "batch_autotune: bad argument");
-  const std::string key = tune_key(bt->sims[0], "batch") + "|" + std::to_string(bt->sims.size());
+  const std::string key = tune_key(bt->sims[0], bt->lockstep ? "batch-lockstep" : "batch") + "|" +
+                          std::to_string(bt->sims.size());
   std::vector<double> times;
   Shape best{};
   {

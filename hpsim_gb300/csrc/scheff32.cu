@@ -348,6 +348,14 @@ __global__ void k32_green(const ScState *sc, ScTables t) {
   green_blocks(sc, t, blockIdx.x, gridDim.x);
 }
 
+// lockstep form: grid y over the beams
+template <int B>
+__global__ void k32_green_seg(const __grid_constant__ SegArgs<MeshSeg, B> a) {
+  const MeshSeg &p = a.p[blockIdx.y];
+  if (!p.sc->remesh || p.sc->sur_accepted) return;
+  green_blocks(p.sc, p.t, blockIdx.x, gridDim.x);
+}
+
 // ---- deposit -----------------------------------------------------------------
 struct DepQ {
   float scale;   // 2^s: fixed-point scale of the per-block histogram
@@ -497,6 +505,49 @@ __global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
   else green_blocks(sc, t, blockIdx.x - ndep, ngreen);
 }
 
+// lockstep form of the deposit: every beam's blocks (whole clusters, so a
+// cluster never spans two beams) in one flat launch
+struct DepSeg {
+  DevBeam bm;
+  ScState *sc;
+  ScTables t;
+  DepQ q;
+  size_t hb;  // shared-memory histogram bytes (the same for every beam of a batch)
+};
+template <int B>
+__global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
+    k32_deposit_seg(const __grid_constant__ SegArgs<DepSeg, B> a) {
+  uint32_t bid, nblk;
+  const DepSeg &p = a.p[seg_find(a, blockIdx.x, bid, nblk)];
+  if (!p.sc->remesh) return;
+  deposit_blocks(p.bm, p.sc, p.t, p.q, bid, nblk);
+}
+
+// the side-stream branch: fork, the Green's tables of every beam, join
+void green_merge(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t st, cudaStream_t side) {
+  uint32_t blocks = 0;  // the table entries are independent of the block count
+  for (const Rec *r : recs) blocks = std::max(blocks, r->blocks);
+  cudaEventRecord(a.ev_fork, st);
+  cudaStreamWaitEvent(side, a.ev_fork, 0);
+  seg_chunks<MeshSeg>(recs, [&](const auto &g, uint32_t) {
+    k32_green_seg<std::decay_t<decltype(g)>::kB><<<dim3(blocks, g.nb), kBlock, 0, side>>>(g);
+  });
+  cudaEventRecord(a.ev_join, side);
+}
+// the deposit on the main stream, then the join of the Green's branch
+void deposit_merge(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t st, cudaStream_t) {
+  size_t hb = 0;  // the largest histogram of the beams that deposit through shared memory
+  for (const Rec *r : recs) {
+    DepSeg d;
+    std::memcpy(&d, r->p.data(), sizeof(DepSeg));
+    if (d.q.smem) hb = std::max(hb, d.hb);
+  }
+  seg_chunks<DepSeg>(recs, [&](const auto &g, uint32_t blocks) {
+    launch_k(k32_deposit_seg<std::decay_t<decltype(g)>::kB>, dim3(blocks), dim3(kBlock), hb, st, g);
+  });
+  cudaStreamWaitEvent(st, a.ev_join, 0);
+}
+
 // ---- kick ----------------------------------------------------------------------
 // ApplySpchKickKernel (space_charge_kernel.cu:573-706) in FP32.  The skipped
 // set (i % skip_stride == 0) is tested as i & skip_mask == 0: the reference's
@@ -577,9 +628,9 @@ void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, con
                            PassScratch s, cudaStream_t st) {
   ScTables u = tables32(t);
   const Sc32Host h = sc32_host(b, a);
-  launch_k(pass_kernel_f<Op32LlossScStats>, dim3(pass_blocks_f(b.n, 1)), dim3(kBlock), 0, st,
-           Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s);
-  note_launch();
+  launch_pass_f_grid(Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st, (uint32_t)pass_blocks_f(b.n, 1),
+                     "stats_fallback");
+  if (!recorder()) note_launch();
 }
 
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
@@ -605,6 +656,16 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   uint32_t ngreen = std::min<uint32_t>(
       (uint32_t)(((size_t)(a.nx_max + 1) * a.nx_max * a.nz_max + kBlock - 1) / kBlock), 152u);
   ngreen = (ngreen + kDepCluster - 1) / kDepCluster * kDepCluster;
+  if (recorder()) {  // a lockstep range: the forked Green's tables and the deposit
+    if (sur || a.adj_possible || !fork || !ndep) {
+      recorder()->unsupported = "space-charge mesh with a surrogate, adjacent bunches or no deposit";
+      return;
+    }
+    record("green", &green_merge, 4u * ngreen, MeshSeg{sc, u});
+    record("deposit", &deposit_merge, ndep, DepSeg{b, sc, u, q, hb});
+    contract32(sc, u, a.nx_max, a.nz_max, a.mesh_fixed, st);
+    return;
+  }
   if (sur) {
     // field surrogate: the deposit alone, the network and its check, then
     // the Green's table and the contraction, which return at once when the
@@ -651,6 +712,10 @@ void sc32_configure() {
   static PerDevice configured;
   configured.once([] {
     cudaFuncSetAttribute(k32_green_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
+    cudaFuncSetAttribute(k32_deposit_seg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
+    cudaFuncSetAttribute(k32_deposit_seg<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHistSmem);
+    cudaFuncSetAttribute(k32_deposit_seg<SegCap<DepSeg>::value>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kMaxHistSmem);
     contract_configure<float>();
     const cudaError_t e = contract_tc_configure();
     if (e != cudaSuccess) set_error(HPS_ERR_CUDA, cudaGetErrorString(e));
@@ -671,13 +736,14 @@ size_t sc32_tc_bytes(uint32_t nr, uint32_t nz, size_t *partial_bytes) {
 void contract32(const ScState *sc, const ScTables &t, uint32_t nx_max, uint32_t nz_max, bool mesh_fixed,
                 cudaStream_t st) {
   const bool tc = t.tcg != nullptr && t.tc_nr == nx_max && t.tc_nz == nz_max;
+  const bool rec = recorder() != nullptr;
   if (tc) {
     contract_tc_launch(sc, t, nx_max, nz_max, st);
-    note_launch(2);
+    if (!rec) note_launch(2);
   }
   if (!tc || !mesh_fixed) {
     contract_launch<float>(sc, t, nx_max, nz_max, st);
-    note_launch();
+    if (!rec) note_launch();
   }
 }
 

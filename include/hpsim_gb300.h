@@ -300,6 +300,24 @@ hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *
 hps_status hps_batch_destroy(hps_batch_t batch);
 hps_status hps_batch_simulate(hps_batch_t batch, int32_t start, int32_t end);
 hps_status hps_batch_last_time_ms(hps_batch_t batch, double *ms);
+/* Lockstep form (default off): when every simulator of the batch issues the
+ * same sequence of FP32 launches over the range (same element kinds in the
+ * same order, same space-charge mesh and contraction kernel; set points,
+ * beams and particle counts may differ), each launch runs once for all
+ * beams: particle kernels over a grid of every beam's blocks, mesh kernels
+ * with a grid dimension over the beams, the per-beam parameters in the
+ * kernels' parameter space (up to 64 beams a launch).  Each beam keeps its
+ * own block count, so its reductions run in the order they have alone; the
+ * merged kernels are separate compilations, so results agree with the
+ * child-graph form to FP32 rounding.  It is off by default because the
+ * child-graph form is faster on the batch workloads measured (beams at
+ * different phases overlap: a mesh kernel of one beam beside a particle
+ * sweep of another).  A range with a launch that has no lockstep form
+ * (FP64 beams, monitors, the field surrogate, adjacent bunches) runs as
+ * child graphs.  hps_batch_last_mode reports which form the last simulate
+ * ran in (1: lockstep) and, if not lockstep, why. */
+hps_status hps_batch_set_lockstep(hps_batch_t batch, int on);
+hps_status hps_batch_last_mode(hps_batch_t batch, int *lockstep, char *why, size_t why_cap);
 
 /* ---- autotuner (no reference counterpart; it replaces the reference's fixed
  * launch geometry, e.g. the 64-block cap of src/beam/src/beam.cu:419 and the
