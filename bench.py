@@ -252,9 +252,9 @@ STEP_BYTES = {"fp32": 56, "fp64": 104}
 PHASE_KERNELS = {
     "fp32": {"quad": "pass_kernel_f<OpPushScStats<QuadMap>>", "gap1": "pass_kernel_f<OpPushScStats<Gap1Map>>",
              "drift": "pass_kernel_f<OpPushScStats<DriftMap>>",
-             "sc_stats": "pass_kernel_f<Op32LlossScStats> + pass_kernel_f<Op32ScStats> (sweep only without "
-                         "the certificate)",
-             "sc_mesh": "k32_green_deposit + k32_contract", "sc_kick": "k32_kick_push<QuadMap|Gap2Map|DriftMap>"},
+             "sc_stats": "none at a fused kick (the statistics are in the sweep before it); "
+                         "pass_kernel_f<Op32ScStats> elsewhere",
+             "sc_mesh": "k32_green + k32_green_deposit + k_contract_m | k_contract_tc + k_tc_reduce", "sc_kick": "k32_kick_push<QuadMap|Gap2Map|DriftMap>"},
     "fp64": {},
 }
 

@@ -47,6 +47,7 @@
 
 #include "common.cuh"
 #include "contract.cuh"
+#include "tc_ptx.cuh"
 
 namespace hps {
 namespace {
@@ -110,12 +111,6 @@ __device__ inline bool tc_go(const ScState *sc, const ScTables &t) {
   return t.tcg != nullptr && sc->remesh && !sc->sur_accepted && sc->nx == t.tc_nr && sc->nz == t.tc_nz;
 }
 
-// byte offset of element (row r, column j) in a K-major tile with the
-// 128-byte swizzle: rows of 128 bytes, 16-byte chunks permuted by r mod 8
-__host__ __device__ inline uint32_t tc_swz(uint32_t r, uint32_t j) {
-  return (r >> 3) * 1024 + (r & 7) * 128 + ((((j >> 3) ^ (r & 7)) & 7) << 4) + ((j & 7) << 1);
-}
-
 // the Green's kernel's share: entry (rp <= nr, rs, dz) of component comp
 // (value v, E_z already carrying its sign for k >= 1) at both folded
 // offsets k = dz + 1 and k = -dz (E_z negated there), hi and lo
@@ -138,104 +133,6 @@ __device__ inline void tc_put_green(const ScTables &t, uint32_t nr, uint32_t nz,
       *(__nv_bfloat16 *)(tile + BT + off) = lo;
     }
   }
-}
-
-// ---- PTX wrappers -----------------------------------------------------------
-__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t tc_now() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(tc_smem(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(tc_smem(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(tc_smem(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-constexpr uint64_t kTcWaitNs = 1000000000ull;  // a wait gives up after one second
-
-// wait for the phase of the given parity; false when it gave up (or another
-// thread of the CTA already gave up: *abort set)
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
-  if (mbar_test(bar, parity)) return true;
-  const uint64_t t0 = tc_now();
-  for (uint32_t it = 0;; ++it) {
-    if (mbar_test(bar, parity)) return true;
-    if ((it & 63) == 63) {
-      if (*abort) return false;
-      if (tc_now() - t0 > kTcWaitNs) {
-        *abort = 1;
-        return false;
-      }
-    }
-  }
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   tc_smem(dst)),
-               "l"(src), "r"(bytes), "r"(tc_smem(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// K-major operand with the 128-byte swizzle: start address, leading offset
-// (unused with this swizzle), 1024 bytes between 8-row groups, descriptor
-// version 1, swizzle mode 2
-__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-// kind::f16 instruction: FP32 accumulator, BF16 A and B, both K-major,
-// N columns, M = 128
-__host__ __device__ constexpr uint32_t tc_idesc(uint32_t N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(accum)
-      : "memory");
-}
-__device__ __forceinline__ void tc_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
 // 2^-36 fixed-point charge as FP32 (two 32-bit conversions)

@@ -148,9 +148,9 @@ int sur_read(const SurNet &n, double *accepted, double *rejected, double *residu
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
 // An element map fused with the space-charge sweep next to it:
 //  PUSH_SCSTATS     the map, then every statistic of the kick after it from
-//                   the new state, the decision and the kick's constants,
-//                   when the sweep can certify them (else sc_redo = 2 and
-//                   sc32_stats_after_push completes them);
+//                   the new state, the decision and the kick's constants
+//                   (when the sweep cannot certify its statistics, its
+//                   finalising block runs the loss test and the moments);
 //  PUSH_AFTER_KICK  the SCHEFF kick, then the map, in one sweep.
 enum { PUSH_SCSTATS = 1, PUSH_AFTER_KICK = 2 };
 struct PushFuse {
@@ -215,12 +215,6 @@ struct Fork {
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
                cudaStream_t st, const SurNet *sur = nullptr, const Fork *fork = nullptr);
 void sc32_kick(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, cudaStream_t st);
-// the statistics after a PUSH_SCSTATS map that could not certify its own:
-// the longitudinal-loss test and the SCHEFF moments in one sweep, repeated
-// only when the test flagged a particle (the good set, hence <phi>_good,
-// changed).  Both sweeps return at once when they are not needed.
-void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
-                           PassScratch s, cudaStream_t st);
 // constants of the FP32 kernels of a kick
 Sc32Host sc32_host(const DevBeam &b, const ScKickArgs &a);
 
