@@ -116,6 +116,13 @@ void sc_green(const ScState *sc, const ScTables &t, uint32_t num_part, double cu
 void nn_conv_forward(const int32_t *dims, const void *x, const void *w, const float *bias, int relu,
                      const void *skip, void *y, cudaStream_t st);
 void nn_gmean_forward(void *y, int planes, int hw, cudaStream_t st);
+// the tensor-core forward (inference): bytes of a layer's weight tiles (0:
+// the kernel does not take the shape), their layout from BF16 weights, and
+// the layer; *err is set when a pipeline wait gave up
+size_t conv_tc_tile_bytes(const int32_t *dims);
+void conv_tc_prepare(const int32_t *dims, const void *w, void *tiles, cudaStream_t st);
+void nn_conv_forward_tc(const int32_t *dims, const void *x, const void *tiles, const float *bias, int relu,
+                        const void *skip, void *y, unsigned int *err, cudaStream_t st);
 
 // A trained network attached to a solver, its device buffers (batch of one)
 // and its acceptance test

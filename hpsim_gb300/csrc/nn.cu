@@ -17,6 +17,7 @@
 
 #include "../../include/hpsim_gb300.h"
 #include "internal.h"
+#include "tc_ptx.cuh"
 
 namespace hps {
 
@@ -452,6 +453,325 @@ void nn_gmean_forward(void *y, int planes, int hw, cudaStream_t st) {
   note_launch();
 }
 
+// ---- the forward convolution on the tensor cores (inference) ---------------
+// One CTA computes 128 output pixels (the MMA's M) x all output channels
+// (N = c_out rounded up to 16) of one batch plane as an implicit GEMM over
+// K = (tap, input channel): D[p][co] = sum_k A[p][k] W[co][k], A[p][(t, ci)]
+// = the input at pixel p's tap t of channel ci.  A cluster of cl CTAs
+// splits the input channels (cpr = c_in / cl each, a power of two); its CTAs
+// add their accumulators through distributed shared memory in rank order.
+// A CTA first copies the input rows its pixels read (its channels only) into
+// shared memory, then per chunk of 64 K values four producer warps write the
+// A tile (one pixel row each, 16-byte stores, 128-byte swizzle) from there
+// while the chunk's weight tile arrives by bulk copy; one thread of the
+// fifth warp issues the BF16 MMAs (FP32 accumulation in tensor memory).  The
+// weights are laid out once per layer as those tiles (conv_tc_prepare).
+// Every wait is bounded; a wait that gives up sets *err and the CTA drains
+// its copies and MMAs, still takes part in both cluster barriers, and frees
+// its tensor memory.
+namespace {
+
+constexpr int kCvThreads = 160;
+constexpr int kCvStages = 4;
+constexpr size_t kCvSlabMax = 64 * 1024;
+constexpr size_t kCvSmemMax = 220 * 1024;
+
+struct ConvTc {
+  ConvShape s;
+  int tiles;   // 128-pixel tiles of an output plane
+  int cl;      // CTAs per cluster
+  int cpr;     // input channels per CTA (power of two)
+  int lg;      // log2(cpr)
+  int kc;      // 64-wide K chunks per CTA (9 cpr rounded up)
+  int np;      // MMA N: c_out rounded up to 16
+  int cols;    // tensor-memory columns
+  int rows;    // input rows a tile reads (largest over the tiles)
+  uint32_t bt;    // bytes of one weight tile (np rows of 128 bytes)
+  uint32_t smem;  // dynamic shared memory
+};
+
+// the source rows [r0, r1] that output pixels [128 tile, 128 tile + 127] read
+__host__ __device__ inline void cv_rows(const ConvShape &s, int tile, int &r0, int &r1) {
+  const int npix = s.Ho * s.Wo, p0 = tile * 128, p1 = min(npix, p0 + 128) - 1;
+  const int ylo = (p0 / s.Wo) * s.stride - 1, yhi = (p1 / s.Wo) * s.stride + 1;
+  r0 = ylo < 0 ? 0 : ylo / s.up;
+  r1 = min(s.Hi - 1, yhi / s.up);
+}
+
+inline bool conv_tc_ok(const ConvShape &s) {
+  return s.Co <= 128 && s.Ci >= 1 && s.Ci <= kMaxCi && (s.Ci & (s.Ci - 1)) == 0 && s.Wi % 2 == 0 && s.B <= 65535;
+}
+
+inline ConvTc conv_tc_plan(const ConvShape &s) {
+  ConvTc p{};
+  p.s = s;
+  const int npix = s.Ho * s.Wo;
+  p.tiles = (npix + 127) / 128;
+  p.np = (s.Co + 15) / 16 * 16;
+  p.cols = 32;
+  while (p.cols < p.np) p.cols *= 2;
+  p.rows = 0;
+  for (int t = 0; t < p.tiles; ++t) {
+    int r0, r1;
+    cv_rows(s, t, r0, r1);
+    p.rows = std::max(p.rows, r1 - r0 + 1);
+  }
+  // split the input channels while the layer has fewer CTAs than SMs (a
+  // CTA keeps at least 8 channels), and until a CTA's input rows fit
+  int cl = 1;
+  while (cl < 8 && s.Ci % (2 * cl) == 0 && s.Ci / (2 * cl) >= 8 && (long long)p.tiles * 2 * cl * s.B <= 152) cl *= 2;
+  while (cl < 8 && s.Ci % (2 * cl) == 0 && (size_t)(s.Ci / cl) * p.rows * s.Wi * 2 > kCvSlabMax) cl *= 2;
+  p.cl = cl;
+  p.cpr = s.Ci / cl;
+  p.lg = 0;
+  while ((1 << p.lg) < p.cpr) ++p.lg;
+  p.kc = (9 * p.cpr + 63) / 64;
+  p.bt = (uint32_t)p.np * 128;
+  const size_t slab = ((size_t)p.cpr * p.rows * s.Wi * 2 + 15) / 16 * 16;
+  p.smem = (uint32_t)(1024 + (size_t)kCvStages * (16384 + p.bt) + slab);
+  return p;
+}
+
+// W[co][ci][3][3] as the kernel's weight tiles: CTA rank r, chunk c, row co,
+// column j holds K value k = 64 c + j = (tap t = k / cpr, channel r cpr + k %
+// cpr); zero beyond the channels, taps and output channels
+__global__ void k_conv_tc_prep(const __nv_bfloat16 *w, ConvTc p, unsigned char *wt) {
+  const long long total = (long long)p.cl * p.kc * p.np * 64;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e % 64), n = (int)((e / 64) % p.np), c = (int)((e / (64 * p.np)) % p.kc);
+    const int r = (int)(e / (64LL * p.np * p.kc));
+    const int k = 64 * c + j, t = k >> p.lg, ci = r * p.cpr + (k & (p.cpr - 1));
+    const __nv_bfloat16 v =
+        (n < p.s.Co && t < 9 && ci < p.s.Ci) ? w[((size_t)n * p.s.Ci + ci) * 9 + t] : __float2bfloat16_rn(0.0f);
+    *(__nv_bfloat16 *)(wt + (size_t)(r * p.kc + c) * p.bt + tc_swz((uint32_t)n, (uint32_t)j)) = v;
+  }
+}
+
+template <int S, int U>
+__global__ void __launch_bounds__(kCvThreads, 1)
+    k_conv_tc(ConvTc p, const __nv_bfloat16 *x, const unsigned char *wt, const float *bias, int relu,
+              const __nv_bfloat16 *skip, __nv_bfloat16 *y, unsigned int *err) {
+  extern __shared__ unsigned char cv_raw[];
+  __shared__ uint64_t full[kCvStages], empty[kCvStages], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  cg::cluster_group cluster = cg::this_cluster();
+  const ConvShape &s = p.s;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int rank = (int)cluster.block_rank(), tile = blockIdx.x / p.cl, b = blockIdx.y;
+  const int npix = s.Ho * s.Wo, cpr = p.cpr, kc = p.kc;
+  const uint32_t bt = p.bt, stage = 16384 + bt;
+  unsigned char *sm = (unsigned char *)(((uintptr_t)cv_raw + 1023) & ~(uintptr_t)1023);
+  __nv_bfloat16 *slab = (__nv_bfloat16 *)(sm + kCvStages * stage);
+  volatile int *abort = &abort_flag;
+  int r0, r1;
+  cv_rows(s, tile, r0, r1);
+  const int R = r1 - r0 + 1, plane = R * s.Wi;
+
+  // this CTA's input rows, two BF16 values per load (rows are even-sized)
+  if (warp < 4) {
+    const uint32_t half = (uint32_t)plane / 2, words = (uint32_t)cpr * half;
+    const __nv_bfloat16 *src0 = x + (((size_t)b * s.Ci + (size_t)rank * cpr) * s.Hi + r0) * s.Wi;
+    for (uint32_t q = tid; q < words; q += 128) {
+      const uint32_t ci = q / half, o = q - ci * half;
+      ((uint32_t *)slab)[q] = __ldg((const uint32_t *)(src0 + (size_t)ci * s.Hi * s.Wi) + o);
+    }
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kCvStages; ++i) {
+      mbar_init(&full[i], 128 + 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&done, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 4) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_slot)),
+                 "r"(p.cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc_fence_before();
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  bool issued_mma = false;
+  const int m = (int)tid, pix = tile * 128 + m;
+  const bool live = warp < 4 && pix < npix;
+  const int oy = live ? pix / s.Wo : 0, ox = live ? pix % s.Wo : 0;
+
+  if (warp < 4) {
+    // ---- producers ----
+    const unsigned char *wsrc = wt + (size_t)rank * kc * bt;
+    if (tid == 0)
+      for (int i = 0; i < kCvStages && i < kc; ++i) {
+        mbar_arrive_tx(&full[i], bt);
+        bulk_g2s(sm + i * stage + 16384, wsrc + (size_t)i * bt, bt, &full[i]);
+      }
+    unsigned char *arow = nullptr;
+    for (int c = 0; c < kc && !*abort; ++c) {
+      const int st = c % kCvStages, use = c / kCvStages;
+      if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1, abort)) break;
+      unsigned char *sb = sm + st * stage;
+      if (tid == 0 && use > 0) {
+        mbar_arrive_tx(&full[st], bt);
+        bulk_g2s(sb + 16384, wsrc + (size_t)c * bt, bt, &full[st]);
+      }
+      arow = sb + (m >> 3) * 1024 + (m & 7) * 128;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = 64 * c + 8 * e + u, t = k >> p.lg, ci = k & (cpr - 1);
+          float val = 0.0f;
+          if (live && t < 9) {
+            const int ky = t / 3, kx = t - 3 * ky;
+            const int Y = oy * S + ky - 1, X = ox * S + kx - 1;
+            if (Y >= 0 && X >= 0 && Y < s.Hi * U && X < s.Wi * U)
+              val = __bfloat162float(slab[ci * plane + (Y / U - r0) * s.Wi + X / U]);
+          }
+          v[u] = __float2bfloat16_rn(val);
+        }
+        *(uint4 *)(arow + (((e ^ (m & 7)) & 7) << 4)) = *(const uint4 *)v;
+      }
+      fence_async_smem();
+      mbar_arrive(&full[st]);
+    }
+  } else if (lane == 0) {
+    // ---- the MMA thread ----
+    const uint32_t idesc = tc_idesc((uint32_t)p.np);
+    for (int c = 0; c < kc; ++c) {
+      const int st = c % kCvStages, use = c / kCvStages;
+      if (!mbar_wait(&full[st], use & 1, abort)) break;
+      tc_fence_after();
+      const uint32_t a0 = tc_smem(sm + st * stage);
+      const uint64_t ad = tc_desc(a0), bd = tc_desc(a0 + 16384);
+#pragma unroll
+      for (uint32_t ks = 0; ks < 4; ++ks) tc_mma(tmem, ad + 2 * ks, bd + 2 * ks, idesc, (c | (int)ks) != 0);
+      issued_mma = true;
+      tc_commit(&empty[st]);
+    }
+    if (issued_mma) tc_commit(&done);
+  }
+
+  // ---- epilogue ----
+  auto emit = [&](int co, float a) {
+    a += bias[co];
+    if (relu && a < 0.0f) a = 0.0f;
+    const size_t o = ((size_t)b * s.Co + co) * npix + pix;
+    y[o] = skip ? __float2bfloat16_rn(__bfloat162float(__float2bfloat16_rn(a)) + __bfloat162float(skip[o]))
+                : __float2bfloat16_rn(a);
+  };
+  bool ok = false;
+  if (warp < 4) {
+    ok = !*abort && mbar_wait(&done, 0, abort);
+    if (ok) {
+      tc_fence_after();
+      const uint32_t tl = tmem + ((32 * warp) << 16);
+      float *red = (float *)sm;  // [np][128]: the stages are free once every MMA completed
+      for (int c0 = 0; c0 < p.np; c0 += 16) {
+        float v[16];
+        tc_ld16(tl + (uint32_t)c0, v);
+        if (p.cl == 1) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if (live && c0 + k < s.Co) emit(c0 + k, v[k]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) red[(c0 + k) * 128 + m] = v[k];
+        }
+      }
+    }
+    tc_fence_before();
+  }
+  if (p.cl > 1) {
+    cluster.sync();  // every CTA's sums are in its shared memory
+    // rank r: output channels [r np / cl, (r + 1) np / cl), the CTAs' sums in rank order
+    const int per = p.np / p.cl;
+    if (warp < 4 && live)
+      for (int co = rank * per; co < (rank + 1) * per && co < s.Co; ++co) {
+        float a = 0.0f;
+        for (int q = 0; q < p.cl; ++q) a += cluster.map_shared_rank((float *)sm, q)[co * 128 + m];
+        emit(co, a);
+      }
+    cluster.sync();  // no CTA leaves while the others read its sums
+  }
+  __syncthreads();
+  if (*abort) {
+    if (tid == 0) atomicOr(err, 1u);
+    if (warp == 4 && lane == 0 && issued_mma) {
+      tc_commit(&done);
+      int dummy = 0;
+      (void)mbar_wait(&done, 0, &dummy);
+    }
+    const uint64_t t0 = tc_now();
+    while (tc_now() - t0 < 100000ull) {
+    }
+    __syncthreads();
+  }
+  if (warp == 4) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)p.cols)
+                 : "memory");
+  }
+}
+
+template <int S, int U>
+void conv_tc_launch(const ConvTc &p, const __nv_bfloat16 *x, const unsigned char *wt, const float *bias, int relu,
+                    const __nv_bfloat16 *skip, __nv_bfloat16 *y, unsigned int *err, cudaStream_t st) {
+  static PerDevice configured;
+  configured.once([] {
+    cudaFuncSetAttribute(k_conv_tc<S, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCvSmemMax);
+  });
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p.tiles * p.cl, p.s.B);
+  cfg.blockDim = dim3(kCvThreads);
+  cfg.dynamicSmemBytes = p.smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = p.cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_conv_tc<S, U>, p, x, wt, bias, relu, skip, y, err);
+}
+
+}  // namespace
+
+size_t conv_tc_tile_bytes(const int32_t *dims) {
+  const ConvShape s = shape(dims);
+  if (!conv_tc_ok(s)) return 0;
+  const ConvTc p = conv_tc_plan(s);
+  if (p.smem > kCvSmemMax) return 0;
+  return (size_t)p.cl * p.kc * p.bt;
+}
+
+void conv_tc_prepare(const int32_t *dims, const void *w, void *tiles, cudaStream_t st) {
+  const ConvTc p = conv_tc_plan(shape(dims));
+  const long long total = (long long)p.cl * p.kc * p.np * 64;
+  const int blocks = (int)std::min<long long>((total + kNnBlock - 1) / kNnBlock, 1024);
+  k_conv_tc_prep<<<blocks, kNnBlock, 0, st>>>((const __nv_bfloat16 *)w, p, (unsigned char *)tiles);
+  note_launch();
+}
+
+void nn_conv_forward_tc(const int32_t *dims, const void *x, const void *tiles, const float *bias, int relu,
+                        const void *skip, void *y, unsigned int *err, cudaStream_t st) {
+  const ConvTc p = conv_tc_plan(shape(dims));
+  auto xb = (const __nv_bfloat16 *)x, kb = (const __nv_bfloat16 *)skip;
+  auto wt = (const unsigned char *)tiles;
+  auto yb = (__nv_bfloat16 *)y;
+  if (p.s.stride == 1 && p.s.up == 1) conv_tc_launch<1, 1>(p, xb, wt, bias, relu, kb, yb, err, st);
+  else if (p.s.stride == 2 && p.s.up == 1) conv_tc_launch<2, 1>(p, xb, wt, bias, relu, kb, yb, err, st);
+  else if (p.s.stride == 1) conv_tc_launch<1, 2>(p, xb, wt, bias, relu, kb, yb, err, st);
+  else conv_tc_launch<2, 2>(p, xb, wt, bias, relu, kb, yb, err, st);
+  note_launch();
+}
+
 }  // namespace hps
 
 extern "C" {
@@ -469,6 +789,31 @@ hps_status hps_nn_conv_forward(const int32_t dims[7], const void *x, const void 
   if (!shape_ok(dims) || !x || !w || !bias || !y) return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_forward: bad argument");
   nn_conv_forward(dims, x, w, bias, relu, skip, y, (cudaStream_t)stream);
   return nn_status("nn_conv_forward");
+}
+
+hps_status hps_nn_conv_forward_tc(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,
+                                  const void *skip, void *y, void *stream) {
+  if (!shape_ok(dims) || !x || !w || !bias || !y) return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_forward_tc: bad argument");
+  const size_t tb = conv_tc_tile_bytes(dims);
+  if (!tb) return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_forward_tc: layer shape not taken by the tensor-core kernel");
+  cudaStream_t st = (cudaStream_t)stream;
+  void *tiles = nullptr;
+  unsigned int *err = nullptr;
+  if (cudaMalloc(&tiles, tb) != cudaSuccess || cudaMalloc((void **)&err, sizeof(unsigned int)) != cudaSuccess) {
+    cudaFree(tiles);
+    return nn_status("nn_conv_forward_tc: allocation");
+  }
+  cudaMemsetAsync(err, 0, sizeof(unsigned int), st);
+  conv_tc_prepare(dims, w, tiles, st);
+  nn_conv_forward_tc(dims, x, tiles, bias, relu, skip, y, err, st);
+  unsigned int h = 0;
+  cudaMemcpyAsync(&h, err, sizeof(h), cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(tiles);
+  cudaFree(err);
+  if (e != cudaSuccess) return (hps_status)set_error(HPS_ERR_CUDA, (std::string("nn_conv_forward_tc: ") + cudaGetErrorString(e)).c_str());
+  if (h) return (hps_status)set_error(HPS_ERR_CUDA, "nn_conv_forward_tc: a pipeline wait timed out");
+  return nn_status("nn_conv_forward_tc");
 }
 
 hps_status hps_nn_conv_backward(const int32_t dims[7], const void *x, const void *w, const void *y, int relu,

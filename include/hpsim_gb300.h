@@ -354,6 +354,14 @@ hps_status hps_sim_set_shape(hps_sim_t sim, const int32_t *shape /* 3 */);
  * (same shape as y, BF16, rounded again) when skip != NULL. */
 hps_status hps_nn_conv_forward(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,
                                const void *skip, void *y, void *stream);
+/* The same layer on the tensor cores (tcgen05 BF16 MMA, FP32 accumulation;
+ * the inference kernel of a network attached to a solver): c_out <= 128,
+ * c_in a power of two, w_in even.  This entry point lays the weights out as
+ * the kernel's tiles in a temporary buffer, runs the layer and waits for it
+ * (a test and measurement entry; attached networks keep their tiles).
+ * HPS_ERR_INVALID for a shape the kernel does not take. */
+hps_status hps_nn_conv_forward_tc(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,
+                                  const void *skip, void *y, void *stream);
 /* dz = dy masked by the ReLU of y; dw, db = weight and bias gradients; dx
  * (may be NULL) = input gradient */
 hps_status hps_nn_conv_backward(const int32_t dims[7], const void *x, const void *w, const void *y, int relu,
