@@ -63,6 +63,8 @@ def parse():
                    help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
                         "(a network file; default the shipped 32x128 network), and report both")
     p.add_argument("--surrogate-tol", type=float, default=0.02)
+    p.add_argument("--surrogate-kernel", choices=["tensor", "cuda"], default="cuda",
+                   help="the surrogate's layers on CUDA cores (default: faster at one plane) or on the tensor cores")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shapes instead of timing candidates before the warm-up")
     p.add_argument("--shape", default=None,
@@ -495,6 +497,7 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
     net = np.load(net_path)
     for o in objs:
         o[2].set_surrogate(net, tol=tol)
+        o[2].set_surrogate_kernel(args.surrogate_kernel)
     stats0 = [o[2].surrogate_stats() for o in objs]
     sur_b, sur_ms = timed()
     sur_mode = batch.last_mode()
@@ -507,7 +510,7 @@ def surrogate_batched(args, plain_value, local, flush, net_path, tol):
     out = {"beams": len(objs), "particles_per_beam": args.particles, "elements": n_elem,
            "lattice": "dtl_like with per-beam RF amplitude x U(0.99, 1.01), RF phase offset U(-1, +1) deg, "
                       "quad gradients x U(0.97, 1.03)",
-           "network": os.path.relpath(net_path, ROOT), "tol": tol,
+           "network": os.path.relpath(net_path, ROOT), "tol": tol, "layers": args.surrogate_kernel,
            "launch_shape": objs[0][3].get_shape(), "autotune": tune,
            "batch_form": {"plain": plain_mode[0], "surrogate": sur_mode[0], "surrogate_why": sur_mode[1] or None},
            "plain_single_value": plain_value, "plain_batched_value": plain_b, "plain_batched_ms_per_step": plain_ms,
@@ -745,7 +748,8 @@ def main():
         mon_plain = monitored()
         net = np.load(args.surrogate)
         sc.set_surrogate(net, tol=args.surrogate_tol)
-        sur = {"network": os.path.relpath(args.surrogate, ROOT), "tol": args.surrogate_tol,
+        sc.set_surrogate_kernel(args.surrogate_kernel)
+        sur = {"network": os.path.relpath(args.surrogate, ROOT), "tol": args.surrogate_tol, "layers": args.surrogate_kernel,
                "plain_value": plain_value, "plain_ms_per_step": sum(plain_ms) / len(plain_ms),
                "network_val_field_err_median": float(net["meta_val_median"]) if "meta_val_median" in net else None}
 

@@ -531,12 +531,14 @@ class SpaceCharge:
     def get_counter(self, name):
         """Counters and flags kept on the device (not in the reference's API):
         'solves' (field solves since creation), 'stat_sweeps' (kicks of an
-        FP32 beam whose statistics took the separate loss-test and moments
-        sweeps), 'tensor_cores' (1: FP32 beams' contractions run on the
-        tensor cores), 'tc_error' (1: a bounded wait of that kernel gave up)."""
+        FP32 beam whose statistics took the loss-test and moments sweeps),
+        'tensor_cores' (1: FP32 beams' contractions run on the tensor cores),
+        'tc_error' (1: a bounded wait of that kernel gave up),
+        'surrogate_tc_layers' (layers of the attached network on the tensor
+        cores), 'surrogate_tc_error' (1: a bounded wait of one gave up)."""
         out = C.c_double()
-        call("hps_scheff_get", self._h, {"solves": 8, "stat_sweeps": 9, "tensor_cores": 11, "tc_error": 12}[name],
-             C.byref(out))
+        call("hps_scheff_get", self._h, {"solves": 8, "stat_sweeps": 9, "tensor_cores": 11, "tc_error": 12,
+                                         "surrogate_tc_layers": 14, "surrogate_tc_error": 15}[name], C.byref(out))
         return int(out.value)
 
     def set_contraction(self, kernel):
@@ -544,6 +546,13 @@ class SpaceCharge:
         'tensor' (the default: split-BF16 tcgen05 products where the mesh
         allows) or 'cuda' (the FP32 ring convolution on CUDA cores)."""
         call("hps_scheff_set", self._h, 10, {"tensor": 0.0, "cuda": 1.0}[kernel])
+
+    def set_surrogate_kernel(self, kernel):
+        """Kernel of the attached surrogate's layers (not in the reference's
+        API): 'cuda' (the default: the CUDA-core convolution, slightly faster
+        on the one plane a solver evaluates) or 'tensor' (tcgen05 BF16 MMA
+        where the layer's shape allows; what training uses for its batches)."""
+        call("hps_scheff_set", self._h, 13, {"tensor": 0.0, "cuda": 1.0}[kernel])
 
     def set_surrogate(self, net, tol=0.02, n_samples=64):
         """Attach a trained field surrogate (not in the reference's API):

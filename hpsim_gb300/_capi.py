@@ -104,6 +104,9 @@ def lib():
         "hps_sim_profile_read": (st, [vp, dp, C.POINTER(C.c_uint64), i32]),
         "hps_nn_conv_forward": (st, [ip, vp, vp, vp, i32, vp, vp, vp]),
         "hps_nn_conv_forward_tc": (st, [ip, vp, vp, vp, i32, vp, vp, vp]),
+        "hps_nn_conv_tc_tile_bytes": (st, [ip, C.POINTER(C.c_uint64)]),
+        "hps_nn_conv_tc_prepare": (st, [ip, vp, vp, vp]),
+        "hps_nn_conv_forward_tiles": (st, [ip, vp, vp, vp, i32, vp, vp, vp, vp]),
         "hps_nn_conv_backward": (st, [ip, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]),
         "hps_nn_gmean_forward": (st, [vp, i32, i32, vp]),
         "hps_nn_gmean_backward": (st, [vp, i32, i32, vp]),

@@ -132,6 +132,8 @@ struct SurNet {
   std::vector<int> hw, skip;             // output plane size; layer whose output is added (-1: none)
   int gmean_after = -1;
   std::vector<void *> w, act;            // BF16 weights and outputs
+  std::vector<void *> wt;                // per layer: weight tiles of the tensor-core kernel (null: not taken)
+  bool use_tc = true;                    // layers with tiles run on the tensor cores
   std::vector<float *> b;
   void *x = nullptr, *spot = nullptr, *d = nullptr;
   uint32_t nr = 0, nz = 0, n_samples = 0;
@@ -151,6 +153,8 @@ int sur_build(SurNet &n, int n_layers, const int32_t *arch, int gmean_after, con
 void sur_solve(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, const SurNet &n,
                cudaStream_t st, int fp32 = 0);
 int sur_read(const SurNet &n, double *accepted, double *rejected, double *residual);
+// layers on the tensor cores; whether a tensor-core layer's wait gave up
+int sur_conv_state(const SurNet &n, int *tc_layers, unsigned int *err);
 
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
 // An element map fused with the space-charge sweep next to it:

@@ -556,6 +556,7 @@ __global__ void __launch_bounds__(kCvThreads, 1)
   __shared__ uint64_t full[kCvStages], empty[kCvStages], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
+  __shared__ float sbias[128];
   cg::cluster_group cluster = cg::this_cluster();
   const ConvShape &s = p.s;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -569,15 +570,7 @@ __global__ void __launch_bounds__(kCvThreads, 1)
   cv_rows(s, tile, r0, r1);
   const int R = r1 - r0 + 1, plane = R * s.Wi;
 
-  // this CTA's input rows, two BF16 values per load (rows are even-sized)
-  if (warp < 4) {
-    const uint32_t half = (uint32_t)plane / 2, words = (uint32_t)cpr * half;
-    const __nv_bfloat16 *src0 = x + (((size_t)b * s.Ci + (size_t)rank * cpr) * s.Hi + r0) * s.Wi;
-    for (uint32_t q = tid; q < words; q += 128) {
-      const uint32_t ci = q / half, o = q - ci * half;
-      ((uint32_t *)slab)[q] = __ldg((const uint32_t *)(src0 + (size_t)ci * s.Hi * s.Wi) + o);
-    }
-  }
+  if (tid < (uint32_t)s.Co) sbias[tid] = bias[tid];
   if (tid == 0) {
     for (int i = 0; i < kCvStages; ++i) {
       mbar_init(&full[i], 128 + 1);
@@ -586,6 +579,27 @@ __global__ void __launch_bounds__(kCvThreads, 1)
     mbar_init(&done, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // the first stages' weight tiles in flight before the input rows are read
+    for (int i = 0; i < kCvStages && i < kc; ++i) {
+      mbar_arrive_tx(&full[i], bt);
+      bulk_g2s(sm + i * stage + 16384, wt + ((size_t)rank * kc + i) * bt, bt, &full[i]);
+    }
+  }
+  // this CTA's input rows, two BF16 values per load (rows are even-sized)
+  if (warp < 4) {
+    const uint32_t half = (uint32_t)plane / 2, words = (uint32_t)cpr * half;
+    const uint32_t *src0 =
+        (const uint32_t *)(x + (((size_t)b * s.Ci + (size_t)rank * cpr) * s.Hi + r0) * s.Wi);
+    const uint32_t cstride = (uint32_t)(s.Hi * s.Wi) / 2;  // words between channel planes
+    uint32_t ci = tid / half, o = tid - ci * half;
+    for (uint32_t q = tid; q < words; q += 128) {
+      ((uint32_t *)slab)[q] = __ldg(src0 + (size_t)ci * cstride + o);
+      o += 128;
+      while (o >= half) {
+        o -= half;
+        ++ci;
+      }
+    }
   }
   if (warp == 4) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_slot)),
@@ -601,15 +615,17 @@ __global__ void __launch_bounds__(kCvThreads, 1)
   const int m = (int)tid, pix = tile * 128 + m;
   const bool live = warp < 4 && pix < npix;
   const int oy = live ? pix / s.Wo : 0, ox = live ? pix % s.Wo : 0;
+  // offset of each tap's input value in a channel's rows (-1: padding or a dead pixel)
+  int off[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) {
+    const int Y = oy * S + t / 3 - 1, X = ox * S + t % 3 - 1;
+    off[t] = (live && Y >= 0 && X >= 0 && Y < s.Hi * U && X < s.Wi * U) ? (Y / U - r0) * s.Wi + X / U : -1;
+  }
 
   if (warp < 4) {
     // ---- producers ----
     const unsigned char *wsrc = wt + (size_t)rank * kc * bt;
-    if (tid == 0)
-      for (int i = 0; i < kCvStages && i < kc; ++i) {
-        mbar_arrive_tx(&full[i], bt);
-        bulk_g2s(sm + i * stage + 16384, wsrc + (size_t)i * bt, bt, &full[i]);
-      }
     unsigned char *arow = nullptr;
     for (int c = 0; c < kc && !*abort; ++c) {
       const int st = c % kCvStages, use = c / kCvStages;
@@ -620,22 +636,41 @@ __global__ void __launch_bounds__(kCvThreads, 1)
         bulk_g2s(sb + 16384, wsrc + (size_t)c * bt, bt, &full[st]);
       }
       arow = sb + (m >> 3) * 1024 + (m & 7) * 128;
+      const unsigned short *sl = (const unsigned short *)slab;
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
-        __align__(16) __nv_bfloat16 v[8];
+        const int k0 = 64 * c + 8 * e;
+        uint32_t w[4];
+        if (cpr >= 8) {
+          // the 8 values share one tap (uniform over the CTA): 8 channels at one offset
+          const int t = k0 >> p.lg, ci0 = k0 & (cpr - 1);
+          const int o = t < 9 ? off[0] : -1;
+          int ot = o;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int k = 64 * c + 8 * e + u, t = k >> p.lg, ci = k & (cpr - 1);
-          float val = 0.0f;
-          if (live && t < 9) {
-            const int ky = t / 3, kx = t - 3 * ky;
-            const int Y = oy * S + ky - 1, X = ox * S + kx - 1;
-            if (Y >= 0 && X >= 0 && Y < s.Hi * U && X < s.Wi * U)
-              val = __bfloat162float(slab[ci * plane + (Y / U - r0) * s.Wi + X / U]);
+          for (int tt = 1; tt < 9; ++tt) ot = t == tt ? off[tt] : ot;
+          if (t >= 9) ot = -1;
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const uint32_t lo = ot >= 0 ? sl[(ci0 + 2 * h) * plane + ot] : 0u;
+            const uint32_t hi = ot >= 0 ? sl[(ci0 + 2 * h + 1) * plane + ot] : 0u;
+            w[h] = lo | (hi << 16);
           }
-          v[u] = __float2bfloat16_rn(val);
+        } else {
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            uint32_t pair[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int k = k0 + 2 * h + j, t = k >> p.lg, ci = k & (cpr - 1);
+              int ot = off[0];
+#pragma unroll
+              for (int tt = 1; tt < 9; ++tt) ot = t == tt ? off[tt] : ot;
+              pair[j] = (t < 9 && ot >= 0) ? sl[ci * plane + ot] : 0u;
+            }
+            w[h] = pair[0] | (pair[1] << 16);
+          }
         }
-        *(uint4 *)(arow + (((e ^ (m & 7)) & 7) << 4)) = *(const uint4 *)v;
+        *(uint4 *)(arow + (((e ^ (m & 7)) & 7) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
       }
       fence_async_smem();
       mbar_arrive(&full[st]);
@@ -658,12 +693,18 @@ __global__ void __launch_bounds__(kCvThreads, 1)
   }
 
   // ---- epilogue ----
-  auto emit = [&](int co, float a) {
-    a += bias[co];
+  // output (co, this pixel) from its sum a, the bias, the ReLU and the skip value sk
+  auto emit = [&](int co, float a, float sk) {
+    a += sbias[co];
     if (relu && a < 0.0f) a = 0.0f;
     const size_t o = ((size_t)b * s.Co + co) * npix + pix;
-    y[o] = skip ? __float2bfloat16_rn(__bfloat162float(__float2bfloat16_rn(a)) + __bfloat162float(skip[o]))
-                : __float2bfloat16_rn(a);
+    y[o] = skip ? __float2bfloat16_rn(__bfloat162float(__float2bfloat16_rn(a)) + sk) : __float2bfloat16_rn(a);
+  };
+  // the skip value of (co, this pixel), read-only (loaded ahead of the stores)
+  auto skip_at = [&](int co) -> float {
+    if (!skip) return 0.0f;
+    const unsigned short u = __ldg((const unsigned short *)skip + ((size_t)b * s.Co + co) * npix + pix);
+    return __bfloat162float(__ushort_as_bfloat16(u));
   };
   bool ok = false;
   if (warp < 4) {
@@ -676,9 +717,14 @@ __global__ void __launch_bounds__(kCvThreads, 1)
         float v[16];
         tc_ld16(tl + (uint32_t)c0, v);
         if (p.cl == 1) {
+          if (live) {
+            float sk[16];
 #pragma unroll
-          for (int k = 0; k < 16; ++k)
-            if (live && c0 + k < s.Co) emit(c0 + k, v[k]);
+            for (int k = 0; k < 16; ++k) sk[k] = c0 + k < s.Co ? skip_at(c0 + k) : 0.0f;
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+              if (c0 + k < s.Co) emit(c0 + k, v[k], sk[k]);
+          }
         } else {
 #pragma unroll
           for (int k = 0; k < 16; ++k) red[(c0 + k) * 128 + m] = v[k];
@@ -689,14 +735,34 @@ __global__ void __launch_bounds__(kCvThreads, 1)
   }
   if (p.cl > 1) {
     cluster.sync();  // every CTA's sums are in its shared memory
-    // rank r: output channels [r np / cl, (r + 1) np / cl), the CTAs' sums in rank order
-    const int per = p.np / p.cl;
-    if (warp < 4 && live)
-      for (int co = rank * per; co < (rank + 1) * per && co < s.Co; ++co) {
-        float a = 0.0f;
-        for (int q = 0; q < p.cl; ++q) a += cluster.map_shared_rank((float *)sm, q)[co * 128 + m];
-        emit(co, a);
+    // rank r: output channels [r np / cl, (r + 1) np / cl), the CTAs' sums
+    // in rank order; four channels' loads from every rank (and their skip
+    // values) in flight at once
+    const int per = p.np / p.cl, cend = min((rank + 1) * per, s.Co);
+    if (warp < 4 && live) {
+      const float *rk[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) rk[q] = cluster.map_shared_rank((float *)sm, q < p.cl ? q : 0);
+      for (int co0 = rank * per; co0 < cend; co0 += 4) {
+        float v[4][8], sk[4];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const int co = co0 + g;
+          const bool valid = co < cend;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v[g][q] = (valid && q < p.cl) ? rk[q][co * 128 + m] : 0.0f;
+          sk[g] = valid ? skip_at(co) : 0.0f;
+        }
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          if (co0 + g >= cend) break;
+          float a = 0.0f;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) a += v[g][q];
+          emit(co0 + g, a, sk[g]);
+        }
       }
+    }
     cluster.sync();  // no CTA leaves while the others read its sums
   }
   __syncthreads();
@@ -789,6 +855,27 @@ hps_status hps_nn_conv_forward(const int32_t dims[7], const void *x, const void 
   if (!shape_ok(dims) || !x || !w || !bias || !y) return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_forward: bad argument");
   nn_conv_forward(dims, x, w, bias, relu, skip, y, (cudaStream_t)stream);
   return nn_status("nn_conv_forward");
+}
+
+hps_status hps_nn_conv_tc_tile_bytes(const int32_t dims[7], uint64_t *bytes) {
+  if (!shape_ok(dims) || !bytes) return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_tc_tile_bytes: bad argument");
+  *bytes = conv_tc_tile_bytes(dims);
+  return HPS_OK;
+}
+
+hps_status hps_nn_conv_tc_prepare(const int32_t dims[7], const void *w, void *tiles, void *stream) {
+  if (!shape_ok(dims) || !w || !tiles || !conv_tc_tile_bytes(dims))
+    return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_tc_prepare: bad argument or shape");
+  conv_tc_prepare(dims, w, tiles, (cudaStream_t)stream);
+  return nn_status("nn_conv_tc_prepare");
+}
+
+hps_status hps_nn_conv_forward_tiles(const int32_t dims[7], const void *x, const void *tiles, const float *bias,
+                                     int relu, const void *skip, void *y, unsigned int *err, void *stream) {
+  if (!shape_ok(dims) || !x || !tiles || !bias || !y || !err || !conv_tc_tile_bytes(dims))
+    return (hps_status)set_error(HPS_ERR_INVALID, "nn_conv_forward_tiles: bad argument or shape");
+  nn_conv_forward_tc(dims, x, tiles, bias, relu, skip, y, err, (cudaStream_t)stream);
+  return nn_status("nn_conv_forward_tiles");
 }
 
 hps_status hps_nn_conv_forward_tc(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,

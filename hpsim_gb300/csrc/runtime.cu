@@ -100,7 +100,8 @@ struct hps_scheff_s {
   ScState *d = nullptr;
   ScTables t{};
   uint64_t version = 0;
-  SurNet *sur = nullptr;  // field surrogate (FP64 beams), owned
+  SurNet *sur = nullptr;  // field surrogate, owned
+  int sur_kernel = 1;     // its layers: 0 tensor cores where the layer allows, 1 CUDA cores (faster at batch 1)
   int contraction = 0;    // FP32 beams: 0 tensor cores where the mesh allows, 1 CUDA cores
 };
 
@@ -876,6 +877,16 @@ hps_status hps_scheff_set(hps_scheff_t s, int param, double v) {
       if (st) return st;
       break;
     }
+    case 13: {
+      if (v != 0.0 && v != 1.0) return fail(HPS_ERR_INVALID, "scheff_set: surrogate layer kernel is 0 or 1");
+      s->sur_kernel = (int)v;
+      if (s->sur) {
+        CK(cudaDeviceSynchronize());
+        s->sur->use_tc = s->sur_kernel == 0;
+      }
+      s->version++;
+      break;
+    }
     default: return fail(HPS_ERR_INVALID, "scheff_set: unknown or read-only parameter");
   }
   return scheff_upload(s);
@@ -902,6 +913,15 @@ hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
     }
     case 10: *v = s->contraction; break;
     case 11: *v = s->t.tcg != nullptr; break;
+    case 13: *v = s->sur_kernel; break;
+    case 14:
+    case 15: {
+      int k = 0;
+      unsigned int err = 0;
+      if (s->sur && sur_conv_state(*s->sur, &k, &err)) return fail(HPS_ERR_CUDA, "scheff_get: reading the surrogate state failed");
+      *v = param == 14 ? (double)k : (double)err;
+      break;
+    }
     default: return fail(HPS_ERR_INVALID, "scheff_get: unknown parameter");
   }
   return HPS_OK;
@@ -958,6 +978,7 @@ hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int3
     delete n;
     return fail(r == 1 ? HPS_ERR_INVALID : HPS_ERR_CUDA, ("scheff_set_surrogate: " + err).c_str());
   }
+  n->use_tc = s->sur_kernel == 0;
   delete s->sur;
   s->sur = n;
   s->version++;

@@ -45,6 +45,7 @@ struct SurDev {
   double residual;     // relative residual of the last check
   double cf[6];        // field = output * (cf0 + cf1 z + cf2 r) for E_r, cf3.. for E_z
   uint32_t n_accepted, n_rejected;
+  unsigned int conv_err;  // a tensor-core layer's bounded wait gave up
 };
 
 // a fixed-point charge bin as FP32 through two 32-bit conversions (a 64-bit
@@ -329,6 +330,7 @@ __global__ void __launch_bounds__(kSurBlock) k_sur_write(const ScState *sc, ScTa
 
 SurNet::~SurNet() {
   for (void *p : w) cudaFree(p);
+  for (void *p : wt) cudaFree(p);
   for (float *p : b) cudaFree(p);
   for (void *p : act) cudaFree(p);
   if (x) cudaFree(x);
@@ -345,7 +347,10 @@ void sur_solve(const DevBeam &bm, ScState *sc, const ScTables &t, const ScKickAr
   for (size_t l = 0; l < n.arch.size(); ++l) {
     const int32_t *dims = n.dims.data() + 7 * l;
     const void *skip = n.skip[l] >= 0 ? n.act[n.skip[l]] : nullptr;
-    nn_conv_forward(dims, cur, n.w[l], n.b[l], n.arch[l][4], skip, n.act[l], st);
+    if (n.use_tc && n.wt[l])
+      nn_conv_forward_tc(dims, cur, n.wt[l], n.b[l], n.arch[l][4], skip, n.act[l], &sd->conv_err, st);
+    else
+      nn_conv_forward(dims, cur, n.w[l], n.b[l], n.arch[l][4], skip, n.act[l], st);
     if ((int)l == n.gmean_after) nn_gmean_forward(n.act[l], dims[2], n.hw[l], st);
     cur = n.act[l];
   }
@@ -412,12 +417,38 @@ int sur_build(SurNet &n, int n_layers, const int32_t *arch, int gmean_after, con
       err = "weight upload failed";
       return 2;
     }
+    // the tensor-core kernel's weight tiles, laid out once
+    void *tp = nullptr;
+    const size_t tb = conv_tc_tile_bytes(n.dims.data() + 7 * l);
+    if (tb) {
+      if (!dm(&tp, tb)) {
+        err = "device allocation failed";
+        return 2;
+      }
+      conv_tc_prepare(n.dims.data() + 7 * l, wp, tp, nullptr);
+    }
+    n.wt.push_back(tp);
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    err = "weight tile layout failed";
+    return 2;
   }
   if (!dm(&n.x, (size_t)2 * nr * nz * 2) || !dm(&n.spot, (size_t)(nr + 1 + nz + n_samples) * 16) ||
       !dm(&n.d, sizeof(SurDev)) || cudaMemset(n.d, 0, sizeof(SurDev)) != cudaSuccess) {
     err = "device allocation failed";
     return 2;
   }
+  return 0;
+}
+
+int sur_conv_state(const SurNet &n, int *tc_layers, unsigned int *err) {
+  int k = 0;
+  for (void *t : n.wt) k += (n.use_tc && t) ? 1 : 0;
+  if (tc_layers) *tc_layers = k;
+  SurDev h;
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(&h, n.d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return 1;
+  if (err) *err = h.conv_err;
   return 0;
 }
 

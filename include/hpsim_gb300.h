@@ -192,13 +192,20 @@ hps_status hps_scheff_destroy(hps_scheff_t s);
 /* parameter: 0 interval, 1 adj_bunch, 2 adj_bunch_cutoff_w, 3 mesh_size_cutoff_w,
  *            4 remesh_threshold, 5 fraction, 6 nr, 7 nz (6/7 read-only);
  * read-only counters since creation: 8 field solves (remeshes), 9 kicks of an
- * FP32 beam whose statistics took the separate loss-test and moments sweeps
- * (the element map before the kick could not certify them).
+ * FP32 beam whose statistics took the loss-test and moments sweeps (the
+ * element map before the kick could not certify them).
  * No reference counterpart: 10 the contraction kernel of FP32 beams (0, the
  * default: split-BF16 tensor cores where the mesh allows -- nz a power of
  * two in 128..512, nr in 16..64 -- else the FP32 ring convolution; 1: the
  * ring convolution always); read-only: 11 the solver holds the tensor-core
- * buffers, 12 a bounded wait of the tensor-core kernel gave up (1). */
+ * buffers, 12 a bounded wait of the tensor-core kernel gave up (1).
+ * 13 the attached surrogate's layers: 0 on the tensor cores where the
+ * layer's shape allows (c_out <= 128, c_in a power of two, w_in even), 1
+ * (the default) on CUDA cores -- a solver evaluates the network on one plane,
+ * where the CUDA-core layers are slightly faster (the tensor-core ones pay
+ * from a batch of about four planes on); read-only: 14 layers of the
+ * attached network on the tensor cores, 15 a tensor-core layer's bounded
+ * wait gave up (1). */
 hps_status hps_scheff_set(hps_scheff_t s, int param, double value);
 hps_status hps_scheff_get(hps_scheff_t s, int param, double *value);
 /* the solver's tables after its last kick (no reference counterpart): charge
@@ -362,6 +369,14 @@ hps_status hps_nn_conv_forward(const int32_t dims[7], const void *x, const void 
  * HPS_ERR_INVALID for a shape the kernel does not take. */
 hps_status hps_nn_conv_forward_tc(const int32_t dims[7], const void *x, const void *w, const float *bias, int relu,
                                   const void *skip, void *y, void *stream);
+/* The tensor-core layer with caller-kept weight tiles: the tiles' bytes for
+ * the layer (0: shape not taken), their layout from BF16 weights w (again
+ * after the weights change), and the layer (asynchronous on stream; *err, a
+ * device word, is set when a pipeline wait gave up). */
+hps_status hps_nn_conv_tc_tile_bytes(const int32_t dims[7], uint64_t *bytes);
+hps_status hps_nn_conv_tc_prepare(const int32_t dims[7], const void *w, void *tiles, void *stream);
+hps_status hps_nn_conv_forward_tiles(const int32_t dims[7], const void *x, const void *tiles, const float *bias,
+                                     int relu, const void *skip, void *y, unsigned int *err, void *stream);
 /* dz = dy masked by the ReLU of y; dw, db = weight and bias gradients; dx
  * (may be NULL) = input gradient */
 hps_status hps_nn_conv_backward(const int32_t dims[7], const void *x, const void *w, const void *y, int relu,

@@ -68,3 +68,20 @@ def test_tensor_core_layer_refuses_shapes_it_does_not_take():
         w = rng.normal(size=(d[2], d[1], 3, 3)).astype(np.float32)
         with pytest.raises(Exception):
             run("hps_nn_conv_forward_tc", d, x, w, np.zeros(d[2], np.float32), 1)
+
+
+def test_training_forward_on_tensor_cores_matches_cuda_cores():
+    """Network.forward of a batch runs its layers on the tensor cores; the
+    prediction equals the CUDA-core layers' to the BF16 activations'
+    precision (2% in norm), and no pipeline wait gave up."""
+    from hpsim_gb300 import surrogate as S
+    net = S.Network(seed=7)
+    rng = np.random.default_rng(7)
+    x = torch.tensor(N.bf16_round(rng.normal(size=(4, 2, 128, 32)).astype(np.float32)), dtype=torch.bfloat16,
+                     device="cuda")
+    preds = {}
+    for tc in (True, False):
+        net.tensor_cores = tc
+        preds[tc] = net.predict(x).cpu().numpy()
+    assert net.tensor_core_errors() == 0
+    assert np.linalg.norm(preds[True] - preds[False]) <= 0.02 * np.linalg.norm(preds[False])

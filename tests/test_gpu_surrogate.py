@@ -192,13 +192,43 @@ def test_accepted_surrogate_field_has_the_plain_boundary():
         assert np.allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
 
 
+def test_tensor_core_layers_give_the_cuda_core_field():
+    """The attached network's layers run on the tensor cores (all ten of the
+    shipped network's shapes qualify); the accepted field of a kick equals
+    the CUDA-core layers' field to the BF16 activations' precision."""
+    import os
+    from hpsim_gb300 import HPSim
+    from hpsim_gb300._capi import call
+    path = os.path.join(os.path.dirname(HPSim.__file__), "data", "scheff_surrogate_32x128.npz")
+    if not os.path.exists(path):
+        pytest.skip("no shipped network")
+    state = dict(np.load(path))
+    fields = {}
+    for kernel in ("tensor", "cuda"):
+        beam, sc, sim = _fodo_sim(16384, state, tol=1e30, graph=False)
+        sc.set_surrogate_kernel(kernel)
+        assert sc.get_counter("surrogate_tc_layers") == (10 if kernel == "tensor" else 0)
+        sim.simulate(0, 1)
+        bins, field, mesh = np.empty(32 * 128), np.empty(129 * 33 * 2), np.empty(7)
+        call("hps_scheff_snapshot", sc.handle, 0, bins.ctypes.data_as(C.POINTER(C.c_double)),
+             field.ctypes.data_as(C.POINTER(C.c_double)), mesh.ctypes.data_as(C.POINTER(C.c_double)))
+        assert sc.surrogate_stats()[:2] == (1, 0) and sc.get_counter("surrogate_tc_error") == 0
+        fields[kernel] = field.reshape(129, 33, 2)
+    tc, cc = fields["tensor"], fields["cuda"]
+    for comp in range(2):
+        ref = cc[:, :, comp]
+        assert np.max(np.abs(tc[:, :, comp] - ref)) <= 2e-2 * np.max(np.abs(ref)), comp
+
+
 @pytest.fixture(scope="module")
 def shipped_runs():
     """The shipped network (hpsim_gb300/data) inside FP64 small-FODO tracking
     at 65,536 particles, against the plain solver on the same beam: the
     per-element monitor records, the median time of a pass and the
     surrogate's counters for the plain path (key None), the residual
-    tolerance 0.02 and every field accepted (1e30)."""
+    tolerance 0.02 and every field accepted (1e30), the layers on the tensor
+    cores, and every field accepted with the layers on CUDA cores
+    ("cuda")."""
     import os
     from hpsim_gb300 import HPSim, lattices as L
     path = os.path.join(os.path.dirname(HPSim.__file__), "data", "scheff_surrogate_32x128.npz")
@@ -206,7 +236,7 @@ def shipped_runs():
         pytest.skip("no shipped network")
     state = dict(np.load(path))
     res = {}
-    for tol in (None, 0.02, 1e30):
+    for tol in (None, 0.02, 1e30, "cuda"):
         beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=65536, precision="fp64")
         beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 777)
         beam.set_ref_w(0.75)
@@ -214,7 +244,10 @@ def shipped_runs():
         beam.save_initial_beam()
         sc = HPSim.SpaceCharge(32, 128, 0.10, 0)
         sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()), sc)
-        if tol is not None:
+        if tol == "cuda":  # every field accepted, the layers on CUDA cores
+            sc.set_surrogate(state, tol=1e30)
+            sc.set_surrogate_kernel("cuda")
+        elif tol is not None:
             sc.set_surrogate(state, tol=tol)
         sim.enable_monitor(True)
         sim.simulate()
@@ -249,7 +282,7 @@ def test_shipped_network_against_the_plain_solver(oracle, shipped_runs):
     assert np.array_equal(plain[:, 0], mon_o[:, 0])
     for i in (6, 11, 16):
         assert np.max(np.abs(plain[:, i] / mon_o[:, i] - 1.0)) <= 1e-6
-    for tol in (0.02, 1e30):
+    for tol in (0.02, 1e30, "cuda"):
         mon, t, st = res[tol]
         msg = f"tol {tol}: accepted/fell back {st[:2]}, {t:.2f} ms vs plain {t_plain:.2f} ms (gain {t_plain / t:.3f})"
         assert st[0] >= 0.8 * (st[0] + st[1]), msg
