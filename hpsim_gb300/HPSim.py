@@ -656,7 +656,7 @@ class Simulator:
         call("hps_sim_last_time_ms", self._h, C.byref(v))
         return v.value
 
-    SHAPE_KEYS = ("contraction", "deposit_blocks_per_sm", "sweep_blocks_per_sm")
+    SHAPE_KEYS = ("contraction", "deposit_blocks_per_sm", "sweep_blocks_per_sm", "deposit_aggregate")
 
     def autotune(self, start=None, end=None, reps=3):
         """Pick the launch shape of this simulation by timing candidates on
@@ -667,19 +667,19 @@ class Simulator:
         return _autotune("hps_sim_autotune", self._h, self.beamline, start, end, reps)
 
     def get_shape(self):
-        sh = np.zeros(3, np.int32)
+        sh = np.zeros(len(self.SHAPE_KEYS), np.int32)
         call("hps_sim_get_shape", self._h, sh.ctypes.data_as(C.POINTER(C.c_int)))
         return dict(zip(self.SHAPE_KEYS, (int(v) for v in sh)))
 
     def set_shape(self, shape):
-        sh = np.array([int(shape[k]) for k in self.SHAPE_KEYS], np.int32)
+        sh = np.array([int(shape.get(k, 0)) for k in self.SHAPE_KEYS], np.int32)
         call("hps_sim_set_shape", self._h, sh.ctypes.data_as(C.POINTER(C.c_int)))
 
 
 def _autotune(fn, handle, bl, start, end, reps):
     s = -1 if start is None else (bl.index(start) if isinstance(start, str) else int(start))
     e = -1 if end is None else (bl.index(end) if isinstance(end, str) else int(end))
-    sh = np.zeros(3, np.int32)
+    sh = np.zeros(len(Simulator.SHAPE_KEYS), np.int32)
     ms = np.zeros(64)
     n = C.c_uint32()
     call(fn, handle, s, e, int(reps), sh.ctypes.data_as(C.POINTER(C.c_int)), dptr(ms), len(ms), C.byref(n))

@@ -96,6 +96,7 @@ struct ScKickArgs {
   int adj_possible;         // adjacent bunches configured (else r_max never sizes the mesh)
   bool mesh_fixed;          // the kick's mesh is the largest one (no mesh-size cut-off energy)
   uint32_t dep_per_sm;      // FP32 deposit: blocks per SM (launch shape)
+  uint32_t dep_agg;         // FP32 deposit: warp-aggregated histogram adds (launch shape)
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);

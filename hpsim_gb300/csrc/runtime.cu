@@ -146,6 +146,7 @@ struct hps_sim_s {
   // launch shapes of the FP32 kernels (hps_sim_autotune picks them)
   uint32_t sweep_cap = 0;   // particle sweeps: blocks per SM (0: all the SM holds)
   uint32_t dep_per_sm = 3;  // deposit: blocks per SM
+  uint32_t dep_agg = 0;     // deposit: warp-aggregated histogram adds
 };
 
 // Many simulators run as one graph launch: each simulator's captured range
@@ -1061,6 +1062,7 @@ ScKickArgs kick_args(Ctx &c, double length) {
   a.adj_possible = c.sc->adj_bunch != 0;
   a.mesh_fixed = c.sc->mesh_w == 0.0 && c.sc->nx == c.sc->nx_max && c.sc->nz == c.sc->nz_max;
   a.dep_per_sm = c.s->dep_per_sm;
+  a.dep_agg = c.s->dep_agg;
   return a;
 }
 
@@ -1414,6 +1416,7 @@ hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
     // launch shapes
     key = mix(key, (uint64_t)s->sweep_cap);
     key = mix(key, (uint64_t)s->dep_per_sm);
+    key = mix(key, (uint64_t)s->dep_agg);
     key = mix(key, c.sc ? (uint64_t)c.sc->contraction : 0);
     p->key = key | 1ull;
   }
@@ -1954,15 +1957,17 @@ hps_status snap_put(const Snapshot &z) {
 }
 
 // one launch shape: contraction kernel of FP32 beams (solver parameter 10),
-// deposit blocks per SM, sweep blocks per SM (0: all the SM holds)
+// deposit blocks per SM, sweep blocks per SM (0: all the SM holds), the
+// deposit's warp-aggregated histogram adds
 struct Shape {
   int contraction;
-  uint32_t dep_per_sm, sweep_cap;
+  uint32_t dep_per_sm, sweep_cap, dep_agg;
 };
 
 hps_status shape_apply(hps_sim_t s, const Shape &sh) {
   s->dep_per_sm = sh.dep_per_sm;
   s->sweep_cap = sh.sweep_cap;
+  s->dep_agg = sh.dep_agg;
   if (s->sc && s->sc->contraction != sh.contraction) {
     hps_status e = hps_scheff_set(s->sc, 10, (double)sh.contraction);
     if (e) return e;
@@ -1987,15 +1992,17 @@ std::string tune_key(hps_sim_t s, const char *what) {
   return buf;
 }
 
-// The search: coordinate descent over the three knobs (contraction kernel,
-// then deposit blocks per SM, then sweep blocks per SM), each candidate
+// The search: coordinate descent over the four knobs (contraction kernel,
+// then deposit blocks per SM, then sweep blocks per SM, then aggregated
+// deposit adds), each candidate
 // timed as the median of `reps` runs after one untimed run (which captures
 // its graph), every run from the snapshot.  run() simulates and returns the
 // device time in ms.
 template <class Run, class Restore>
 hps_status tune_search(const std::vector<hps_sim_t> &sims, bool fp32, bool tc_ok, int reps, Run run,
                        Restore restore, Shape *best_out, std::vector<double> *times) {
-  Shape best{sims[0]->sc ? sims[0]->sc->contraction : 0, sims[0]->dep_per_sm, sims[0]->sweep_cap};
+  Shape best{sims[0]->sc ? sims[0]->sc->contraction : 0, sims[0]->dep_per_sm, sims[0]->sweep_cap,
+             sims[0]->dep_agg};
   if (!fp32) { *best_out = best; return HPS_OK; }
   auto measure = [&](const Shape &sh, double *ms) -> hps_status {
     for (hps_sim_t s : sims) {
@@ -2020,14 +2027,16 @@ hps_status tune_search(const std::vector<hps_sim_t> &sims, bool fp32, bool tc_ok
   hps_status e = measure(best, &best_ms);
   if (e) return e;
   std::vector<Shape> cands;
-  if (tc_ok) cands.push_back({1 - best.contraction, best.dep_per_sm, best.sweep_cap});
-  for (int stage = 0; stage < 3; ++stage) {
+  if (tc_ok) cands.push_back({1 - best.contraction, best.dep_per_sm, best.sweep_cap, best.dep_agg});
+  for (int stage = 0; stage < 4; ++stage) {
     if (stage == 1) {
       for (uint32_t d : {2u, 3u, 4u})
-        if (d != best.dep_per_sm) cands.push_back({best.contraction, d, best.sweep_cap});
+        if (d != best.dep_per_sm) cands.push_back({best.contraction, d, best.sweep_cap, best.dep_agg});
     } else if (stage == 2) {
       for (uint32_t c : {0u, 2u})
-        if (c != best.sweep_cap) cands.push_back({best.contraction, best.dep_per_sm, c});
+        if (c != best.sweep_cap) cands.push_back({best.contraction, best.dep_per_sm, c, best.dep_agg});
+    } else if (stage == 3) {
+      cands.push_back({best.contraction, best.dep_per_sm, best.sweep_cap, 1u - best.dep_agg});
     }
     for (const Shape &sh : cands) {
       double ms = 0.0;
@@ -2042,7 +2051,12 @@ hps_status tune_search(const std::vector<hps_sim_t> &sims, bool fp32, bool tc_ok
 
 void report(const Shape &b, const std::vector<double> &t, int32_t *shape_out, double *ms_out, uint32_t ms_cap,
             uint32_t *n_out) {
-  if (shape_out) { shape_out[0] = b.contraction; shape_out[1] = (int32_t)b.dep_per_sm; shape_out[2] = (int32_t)b.sweep_cap; }
+  if (shape_out) {
+    shape_out[0] = b.contraction;
+    shape_out[1] = (int32_t)b.dep_per_sm;
+    shape_out[2] = (int32_t)b.sweep_cap;
+    shape_out[3] = (int32_t)b.dep_agg;
+  }
   if (ms_out)
     for (size_t k = 0; k < t.size() && k < ms_cap; ++k) ms_out[k] = t[k];
   if (n_out) *n_out = (uint32_t)t.size();
@@ -2152,13 +2166,15 @@ hps_status hps_sim_get_shape(hps_sim_t s, int32_t *shape_out) {
   shape_out[0] = s->sc ? s->sc->contraction : 0;
   shape_out[1] = (int32_t)s->dep_per_sm;
   shape_out[2] = (int32_t)s->sweep_cap;
+  shape_out[3] = (int32_t)s->dep_agg;
   return HPS_OK;
 }
 
 hps_status hps_sim_set_shape(hps_sim_t s, const int32_t *shape) {
-  if (!s || !shape || shape[0] < 0 || shape[0] > 1 || shape[1] < 1 || shape[1] > 8 || shape[2] < 0 || shape[2] > 16)
+  if (!s || !shape || shape[0] < 0 || shape[0] > 1 || shape[1] < 1 || shape[1] > 8 || shape[2] < 0 || shape[2] > 16 ||
+      shape[3] < 0 || shape[3] > 1)
     return fail(HPS_ERR_INVALID, "sim_set_shape: bad argument");
-  return shape_apply(s, Shape{shape[0], (uint32_t)shape[1], (uint32_t)shape[2]});
+  return shape_apply(s, Shape{shape[0], (uint32_t)shape[1], (uint32_t)shape[2], (uint32_t)shape[3]});
 }
 
 }  // extern "C"

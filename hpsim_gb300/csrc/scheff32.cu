@@ -246,7 +246,24 @@ struct DepQ {
   float scale;   // 2^s: fixed-point scale of the per-block histogram
   int shift;     // 36 - s: to the global table's 2^36 scale
   int smem;      // per-block histogram in shared memory (else global atomics)
+  int agg;       // warp-aggregated shared-memory adds (a launch-shape choice)
 };
+
+// Add w to bin k of the block's histogram.  Aggregated: the warp's lanes
+// with the same bin (__match_any_sync) sum their weights (__reduce_add_sync,
+// exact integer sums) and the lowest of them adds the total, one shared-
+// memory atomic per distinct bin per warp instead of one per particle --
+// the beam core's few bins take most particles.  Every lane of the warp
+// calls it (invalid lanes with k = -1 and w = 0).
+__device__ __forceinline__ void hist_add(int *hist32, int k, int w, bool agg) {
+  if (!agg) {
+    if (w) atomicAdd(hist32 + k, w);
+    return;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, k);
+  const int tot = (int)__reduce_add_sync(peers, (unsigned)w);
+  if (k >= 0 && tot && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(hist32 + k, tot);
+}
 
 // Deposit blocks run in clusters of kDepCluster CTAs: each CTA fills its own
 // shared-memory histogram, then CTA r of the cluster sums slice r of the
@@ -281,63 +298,93 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
   const float drdr = dr * dr, inv_drdr = inv_dr * inv_dr;
   const long long m = 1ll << q.shift;
   const uint32_t stride = nblk * blockDim.x;
+  const bool agg = q.smem && q.agg;
   uint32_t cnt = 0;
-  for (uint32_t base = bid * blockDim.x + threadIdx.x; base < bm.n; base += kDepBatch * stride) {
-    DepIn in[kDepBatch];
-#pragma unroll
-    for (int u = 0; u < kDepBatch; ++u) {
-      const uint32_t np = base + u * stride;
-      if (np < bm.n) in[u] = {bm.loss[np], bm.lloss[np], bm.fx[np], bm.fy[np], bm.fphi[np]};
-      else in[u].lo = 1u;
+  // particle in -> its four bins and fixed-point weights; false when it is
+  // not deposited (lost, longitudinally lost, off the mesh)
+  auto weigh = [&](const DepIn &in, int (&k)[4], int (&w)[4]) -> bool {
+    if (in.lo != 0u || in.ll != 0u) return false;
+    const float pz = rel_phase_f(in.ph - pag);
+    const float dx = in.x - xbar, dy = in.y - ybar;
+    const float rsq_sh = dx * dx * inv_epsq + dy * dy * epsq;
+    const int i = (int)(sqrtf(rsq_sh) * inv_dr + 1.0f);
+    const float z = -c2 * wrap_turns(pz - phimc);
+    if (!(i >= 1 && (uint32_t)i <= nx)) return false;
+    if (!(fabsf(z) < hl)) return false;
+    const float zz = z + hl;
+    const int jm1 = (int)(zz * inv_dzg + 1.0f);
+    if (jm1 < 1 || jm1 > (int)nz) return false;
+    int i1 = i + 1;
+    if (rsq_sh < 0.5f * drdr * (float)(i * i + (i - 1) * (i - 1))) i1 = i - 1;
+    i1 = min(max(i1, 1), (int)nx);
+    int j1 = jm1 + 1;
+    if (zz < ((float)jm1 - 0.5f) * dzg) j1 = jm1 - 1;
+    j1 = min(max(j1, 1), (int)nz);
+    // area weights in units of dr^2 (rmax^2 - rmin^2 = sqrtmp dr^2), and the
+    // z weight with (jm1 - j1) dz = +-dz
+    float a = 1.0f;
+    if (i1 != i) {
+      const float sqrtmp = sqrtf(4.0f * rsq_sh * inv_drdr - 1.0f);
+      const float rmin_n = 0.25f * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
+      const float rmax_n = rmin_n + sqrtmp;
+      if (i1 < i) a = __fdividef(rmax_n - (float)((i - 1) * (i - 1)), sqrtmp);
+      else a = __fdividef((float)((i1 - 1) * (i1 - 1)) - rmin_n, sqrtmp);
     }
+    float cc = 1.0f;
+    if (j1 != jm1) cc = (zz - ((float)j1 - 0.5f) * dzg) * (j1 < jm1 ? inv_dzg : -inv_dzg);
+    const float bb = 1.0f - a, d = 1.0f - cc;
+    k[0] = (jm1 - 1) * (int)nx + i - 1;
+    k[1] = k[0] + (i1 - i);
+    k[2] = (j1 - 1) * (int)nx + i - 1;
+    k[3] = k[2] + (i1 - i);
+    w[0] = __float2int_rn(a * cc * q.scale);
+    w[1] = __float2int_rn(bb * cc * q.scale);
+    w[2] = __float2int_rn(a * d * q.scale);
+    w[3] = __float2int_rn(bb * d * q.scale);
+    return true;
+  };
+  if (agg) {
+    // warp-uniform iterations (a lane past the end carries no particle), so
+    // that every lane takes part in the aggregated adds
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t wbase = bid * blockDim.x + (threadIdx.x & ~31u); wbase < bm.n; wbase += kDepBatch * stride) {
+      DepIn in[kDepBatch];
 #pragma unroll
-    for (int u = 0; u < kDepBatch; ++u) {
-      if (in[u].lo != 0u || in[u].ll != 0u) continue;
-      const float pz = rel_phase_f(in[u].ph - pag);
-      float dx = in[u].x - xbar, dy = in[u].y - ybar;
-      float rsq_sh = dx * dx * inv_epsq + dy * dy * epsq;
-      int i = (int)(sqrtf(rsq_sh) * inv_dr + 1.0f);
-      float z = -c2 * wrap_turns(pz - phimc);
-      if (!(i >= 1 && (uint32_t)i <= nx)) continue;
-      if (!(fabsf(z) < hl)) continue;
-      float zz = z + hl;
-      int jm1 = (int)(zz * inv_dzg + 1.0f);
-      if (jm1 < 1 || jm1 > (int)nz) continue;
-      int i1 = i + 1;
-      if (rsq_sh < 0.5f * drdr * (float)(i * i + (i - 1) * (i - 1))) i1 = i - 1;
-      i1 = min(max(i1, 1), (int)nx);
-      int j1 = jm1 + 1;
-      if (zz < ((float)jm1 - 0.5f) * dzg) j1 = jm1 - 1;
-      j1 = min(max(j1, 1), (int)nz);
-      // area weights in units of dr^2 (rmax^2 - rmin^2 = sqrtmp dr^2), and the
-      // z weight with (jm1 - j1) dz = +-dz
-      float a = 1.0f;
-      if (i1 != i) {
-        const float sqrtmp = sqrtf(4.0f * rsq_sh * inv_drdr - 1.0f);
-        const float rmin_n = 0.25f * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
-        const float rmax_n = rmin_n + sqrtmp;
-        if (i1 < i) a = __fdividef(rmax_n - (float)((i - 1) * (i - 1)), sqrtmp);
-        else a = __fdividef((float)((i1 - 1) * (i1 - 1)) - rmin_n, sqrtmp);
+      for (int u = 0; u < kDepBatch; ++u) {
+        const uint32_t np = wbase + lane + u * stride;
+        if (np < bm.n) in[u] = {bm.loss[np], bm.lloss[np], bm.fx[np], bm.fy[np], bm.fphi[np]};
+        else in[u].lo = 1u;
       }
-      float cc = 1.0f;
-      if (j1 != jm1) cc = (zz - ((float)j1 - 0.5f) * dzg) * (j1 < jm1 ? inv_dzg : -inv_dzg);
-      float bb = 1.0f - a, d = 1.0f - cc;
-      int k00 = (jm1 - 1) * (int)nx + i - 1, k01 = k00 + (i1 - i);
-      int k10 = (j1 - 1) * (int)nx + i - 1, k11 = k10 + (i1 - i);
-      int w00 = __float2int_rn(a * cc * q.scale), w01 = __float2int_rn(bb * cc * q.scale);
-      int w10 = __float2int_rn(a * d * q.scale), w11 = __float2int_rn(bb * d * q.scale);
-      if (q.smem) {
-        if (w00) atomicAdd(hist32 + k00, w00);
-        if (w01) atomicAdd(hist32 + k01, w01);
-        if (w10) atomicAdd(hist32 + k10, w10);
-        if (w11) atomicAdd(hist32 + k11, w11);
-      } else {
-        if (w00) atomicAdd(t.bin_fx + k00, (unsigned long long)((long long)w00 * m));
-        if (w01) atomicAdd(t.bin_fx + k01, (unsigned long long)((long long)w01 * m));
-        if (w10) atomicAdd(t.bin_fx + k10, (unsigned long long)((long long)w10 * m));
-        if (w11) atomicAdd(t.bin_fx + k11, (unsigned long long)((long long)w11 * m));
+#pragma unroll
+      for (int u = 0; u < kDepBatch; ++u) {
+        int k[4] = {-1, -1, -1, -1}, w[4] = {0, 0, 0, 0};
+        if (weigh(in[u], k, w)) ++cnt;
+        else k[0] = k[1] = k[2] = k[3] = -1, w[0] = w[1] = w[2] = w[3] = 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) hist_add(hist32, k[e], w[e], true);
       }
-      ++cnt;
+    }
+  } else {
+    for (uint32_t base = bid * blockDim.x + threadIdx.x; base < bm.n; base += kDepBatch * stride) {
+      DepIn in[kDepBatch];
+#pragma unroll
+      for (int u = 0; u < kDepBatch; ++u) {
+        const uint32_t np = base + u * stride;
+        if (np < bm.n) in[u] = {bm.loss[np], bm.lloss[np], bm.fx[np], bm.fy[np], bm.fphi[np]};
+        else in[u].lo = 1u;
+      }
+#pragma unroll
+      for (int u = 0; u < kDepBatch; ++u) {
+        int k[4], w[4];
+        if (!weigh(in[u], k, w)) continue;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (!w[e]) continue;
+          if (q.smem) atomicAdd(hist32 + k[e], w[e]);
+          else atomicAdd(t.bin_fx + k[e], (unsigned long long)((long long)w[e] * m));
+        }
+        ++cnt;
+      }
     }
   }
   for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
@@ -449,7 +496,7 @@ __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc
 }
 
 DepQ dep_quant(uint32_t n, int grid, size_t hist_bytes) {
-  DepQ q;
+  DepQ q{};
   uint32_t per = (uint32_t)grid * kBlock;
   uint32_t iters = (n + per - 1) / per;
   uint64_t p = (uint64_t)iters * kBlock;  // particles one block can deposit
@@ -523,6 +570,7 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
     hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
     if (hb > kMaxHistSmem) hb = 0;
     q = dep_quant(b.n, (int)ndep, hb);
+    q.agg = a.dep_agg ? 1 : 0;
   }
   // Green's table entries of the largest mesh, a few per thread on one block
   // per SM, so that the whole launch is resident at once

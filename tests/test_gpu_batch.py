@@ -131,3 +131,31 @@ def test_batch_autotune():
     for o in objs:
         assert o[2].get_shape() == res["shape"]
     batch.simulate()
+
+
+def test_aggregated_deposit_adds_give_the_same_table():
+    """The deposit's warp-aggregated histogram adds (launch-shape knob
+    deposit_aggregate) sum the same integer weights in another order: the
+    simulation is bit for bit the one with one atomic per particle and bin,
+    on the CUDA-core and the tensor-core contraction."""
+    import numpy as np
+    from hpsim_gb300 import HPSim, lattices as L
+    for contraction in (0, 1):
+        out = []
+        for agg in (0, 1):
+            beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=65536, precision="fp32")
+            beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 21)
+            beam.set_ref_w(0.75)
+            beam.set_ref_phi(0.0)
+            sc = HPSim.SpaceCharge(32, 128)
+            sc.set_remesh_threshold(0.0)
+            sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.dtl_like(n_gaps=10)), sc)
+            sim.set_shape({"contraction": contraction, "deposit_blocks_per_sm": 3, "sweep_blocks_per_sm": 0,
+                           "deposit_aggregate": agg})
+            assert sim.get_shape()["deposit_aggregate"] == agg
+            sim.enable_monitor(True)
+            sim.simulate()
+            out.append((sim.monitor.copy(), [beam._coord(k) for k in ("x", "xp", "y", "yp", "phi", "w")]))
+        assert np.array_equal(out[0][0], out[1][0])
+        for a, b in zip(out[0][1], out[1][1]):
+            assert np.array_equal(a, b)
