@@ -68,8 +68,8 @@ def parse():
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shapes instead of timing candidates before the warm-up")
     p.add_argument("--shape", default=None,
-                   help="contraction,deposit_blocks_per_sm,sweep_blocks_per_sm[,deposit_aggregate]: set this "
-                        "launch shape instead of tuning (reproducible profiling runs)")
+                   help="contraction,deposit_blocks_per_sm,sweep_blocks_per_sm[,deposit_aggregate[,deposit_threads]]: "
+                        "set this launch shape instead of tuning (reproducible profiling runs)")
     p.add_argument("--tune-elements", type=int, default=60,
                    help="the autotuner times runs over the lattice's first N elements")
     p.add_argument("--surrogate-batch", type=int, default=8,

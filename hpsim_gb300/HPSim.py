@@ -656,7 +656,8 @@ class Simulator:
         call("hps_sim_last_time_ms", self._h, C.byref(v))
         return v.value
 
-    SHAPE_KEYS = ("contraction", "deposit_blocks_per_sm", "sweep_blocks_per_sm", "deposit_aggregate")
+    SHAPE_KEYS = ("contraction", "deposit_blocks_per_sm", "sweep_blocks_per_sm", "deposit_aggregate",
+                  "deposit_threads")
 
     def autotune(self, start=None, end=None, reps=3):
         """Pick the launch shape of this simulation by timing candidates on

@@ -97,6 +97,7 @@ struct ScKickArgs {
   bool mesh_fixed;          // the kick's mesh is the largest one (no mesh-size cut-off energy)
   uint32_t dep_per_sm;      // FP32 deposit: blocks per SM (launch shape)
   uint32_t dep_agg;         // FP32 deposit: warp-aggregated histogram adds (launch shape)
+  uint32_t dep_threads;     // FP32 deposit: threads per block, 256 | 512 | 1024 (launch shape)
 };
 // allow the deposit kernel the shared memory of the largest mesh
 void sc_configure(size_t max_deposit_smem);

@@ -147,6 +147,7 @@ struct hps_sim_s {
   uint32_t sweep_cap = 0;   // particle sweeps: blocks per SM (0: all the SM holds)
   uint32_t dep_per_sm = 3;  // deposit: blocks per SM
   uint32_t dep_agg = 0;     // deposit: warp-aggregated histogram adds
+  uint32_t dep_threads = 256;  // deposit: threads per block
 };
 
 // Many simulators run as one graph launch: each simulator's captured range
@@ -1063,6 +1064,7 @@ ScKickArgs kick_args(Ctx &c, double length) {
   a.mesh_fixed = c.sc->mesh_w == 0.0 && c.sc->nx == c.sc->nx_max && c.sc->nz == c.sc->nz_max;
   a.dep_per_sm = c.s->dep_per_sm;
   a.dep_agg = c.s->dep_agg;
+  a.dep_threads = c.s->dep_threads;
   return a;
 }
 
@@ -1417,6 +1419,7 @@ hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
     key = mix(key, (uint64_t)s->sweep_cap);
     key = mix(key, (uint64_t)s->dep_per_sm);
     key = mix(key, (uint64_t)s->dep_agg);
+    key = mix(key, (uint64_t)s->dep_threads);
     key = mix(key, c.sc ? (uint64_t)c.sc->contraction : 0);
     p->key = key | 1ull;
   }
@@ -1958,16 +1961,17 @@ hps_status snap_put(const Snapshot &z) {
 
 // one launch shape: contraction kernel of FP32 beams (solver parameter 10),
 // deposit blocks per SM, sweep blocks per SM (0: all the SM holds), the
-// deposit's warp-aggregated histogram adds
+// deposit's warp-aggregated histogram adds, the deposit's threads per block
 struct Shape {
   int contraction;
-  uint32_t dep_per_sm, sweep_cap, dep_agg;
+  uint32_t dep_per_sm, sweep_cap, dep_agg, dep_threads;
 };
 
 hps_status shape_apply(hps_sim_t s, const Shape &sh) {
   s->dep_per_sm = sh.dep_per_sm;
   s->sweep_cap = sh.sweep_cap;
   s->dep_agg = sh.dep_agg;
+  s->dep_threads = sh.dep_threads;
   if (s->sc && s->sc->contraction != sh.contraction) {
     hps_status e = hps_scheff_set(s->sc, 10, (double)sh.contraction);
     if (e) return e;
@@ -2002,7 +2006,7 @@ template <class Run, class Restore>
 hps_status tune_search(const std::vector<hps_sim_t> &sims, bool fp32, bool tc_ok, int reps, Run run,
                        Restore restore, Shape *best_out, std::vector<double> *times) {
   Shape best{sims[0]->sc ? sims[0]->sc->contraction : 0, sims[0]->dep_per_sm, sims[0]->sweep_cap,
-             sims[0]->dep_agg};
+             sims[0]->dep_agg, sims[0]->dep_threads};
   if (!fp32) { *best_out = best; return HPS_OK; }
   auto measure = [&](const Shape &sh, double *ms) -> hps_status {
     for (hps_sim_t s : sims) {
@@ -2027,16 +2031,21 @@ hps_status tune_search(const std::vector<hps_sim_t> &sims, bool fp32, bool tc_ok
   hps_status e = measure(best, &best_ms);
   if (e) return e;
   std::vector<Shape> cands;
-  if (tc_ok) cands.push_back({1 - best.contraction, best.dep_per_sm, best.sweep_cap, best.dep_agg});
+  if (tc_ok) cands.push_back({1 - best.contraction, best.dep_per_sm, best.sweep_cap, best.dep_agg, best.dep_threads});
   for (int stage = 0; stage < 4; ++stage) {
     if (stage == 1) {
-      for (uint32_t d : {2u, 3u, 4u})
-        if (d != best.dep_per_sm) cands.push_back({best.contraction, d, best.sweep_cap, best.dep_agg});
+      // the deposit's grid: blocks of 256, 512 or 1024 threads, blocks per
+      // SM within the 1024 threads an SM holds at 64 registers a thread
+      const uint32_t grids[6][2] = {{256, 2}, {256, 3}, {256, 4}, {512, 1}, {512, 2}, {1024, 1}};
+      for (const auto &g : grids)
+        if (g[0] != best.dep_threads || g[1] != best.dep_per_sm)
+          cands.push_back({best.contraction, g[1], best.sweep_cap, best.dep_agg, g[0]});
     } else if (stage == 2) {
       for (uint32_t c : {0u, 2u})
-        if (c != best.sweep_cap) cands.push_back({best.contraction, best.dep_per_sm, c, best.dep_agg});
+        if (c != best.sweep_cap)
+          cands.push_back({best.contraction, best.dep_per_sm, c, best.dep_agg, best.dep_threads});
     } else if (stage == 3) {
-      cands.push_back({best.contraction, best.dep_per_sm, best.sweep_cap, 1u - best.dep_agg});
+      cands.push_back({best.contraction, best.dep_per_sm, best.sweep_cap, 1u - best.dep_agg, best.dep_threads});
     }
     for (const Shape &sh : cands) {
       double ms = 0.0;
@@ -2056,6 +2065,7 @@ void report(const Shape &b, const std::vector<double> &t, int32_t *shape_out, do
     shape_out[1] = (int32_t)b.dep_per_sm;
     shape_out[2] = (int32_t)b.sweep_cap;
     shape_out[3] = (int32_t)b.dep_agg;
+    shape_out[4] = (int32_t)b.dep_threads;
   }
   if (ms_out)
     for (size_t k = 0; k < t.size() && k < ms_cap; ++k) ms_out[k] = t[k];
@@ -2167,14 +2177,16 @@ hps_status hps_sim_get_shape(hps_sim_t s, int32_t *shape_out) {
   shape_out[1] = (int32_t)s->dep_per_sm;
   shape_out[2] = (int32_t)s->sweep_cap;
   shape_out[3] = (int32_t)s->dep_agg;
+  shape_out[4] = (int32_t)s->dep_threads;
   return HPS_OK;
 }
 
 hps_status hps_sim_set_shape(hps_sim_t s, const int32_t *shape) {
   if (!s || !shape || shape[0] < 0 || shape[0] > 1 || shape[1] < 1 || shape[1] > 8 || shape[2] < 0 || shape[2] > 16 ||
-      shape[3] < 0 || shape[3] > 1)
+      shape[3] < 0 || shape[3] > 1 || (shape[4] != 0 && shape[4] != 256 && shape[4] != 512 && shape[4] != 1024))
     return fail(HPS_ERR_INVALID, "sim_set_shape: bad argument");
-  return shape_apply(s, Shape{shape[0], (uint32_t)shape[1], (uint32_t)shape[2], (uint32_t)shape[3]});
+  return shape_apply(s, Shape{shape[0], (uint32_t)shape[1], (uint32_t)shape[2], (uint32_t)shape[3],
+                              shape[4] ? (uint32_t)shape[4] : 256u});
 }
 
 }  // extern "C"

@@ -270,6 +270,9 @@ __device__ __forceinline__ void hist_add(int *hist32, int k, int w, bool agg) {
 // cluster's histograms through distributed shared memory and adds it to the
 // global table, so a bin takes one global atomic per cluster, not per block.
 constexpr int kDepCluster = 8;
+// deposit threads per block: 256, 512 or 1024 (a launch-shape choice; the
+// kernels take up to 1024, at most 64 registers a thread)
+constexpr int kDepBlockMax = 1024;
 constexpr int kDepBatch = 4;  // particles a thread loads before it deposits them
 
 struct DepIn {
@@ -430,7 +433,7 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
 // The deposit and the Green's table are independent: one launch, blocks
 // [0, ndep) deposit, blocks [ndep, ndep + ngreen) evaluate the table (both
 // multiples of the cluster size, so no cluster mixes the two).
-__global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
+__global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kDepBlockMax)
     k32_green_deposit(DevBeam bm, ScState *sc, ScTables t, DepQ q, uint32_t ndep, uint32_t ngreen) {
   if (!sc->remesh) return;
   if (blockIdx.x < ndep) deposit_blocks(bm, sc, t, q, blockIdx.x, ndep);
@@ -445,9 +448,10 @@ struct DepSeg {
   ScTables t;
   DepQ q;
   size_t hb;  // shared-memory histogram bytes (the same for every beam of a batch)
+  uint32_t threads;  // block size (the same for every beam of a merged launch)
 };
 template <int B>
-__global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kBlock)
+__global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kDepBlockMax)
     k32_deposit_seg(const __grid_constant__ SegArgs<DepSeg, B> a) {
   uint32_t bid, nblk;
   const DepSeg &p = a.p[seg_find(a, blockIdx.x, bid, nblk)];
@@ -475,7 +479,7 @@ void deposit_merge(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t 
     if (d.q.smem) hb = std::max(hb, d.hb);
   }
   seg_chunks<DepSeg>(recs, [&](const auto &g, uint32_t blocks) {
-    launch_k(k32_deposit_seg<std::decay_t<decltype(g)>::kB>, dim3(blocks), dim3(kBlock), hb, st, g);
+    launch_k(k32_deposit_seg<std::decay_t<decltype(g)>::kB>, dim3(blocks), dim3(g.p[0].threads), hb, st, g);
   });
   cudaStreamWaitEvent(st, a.ev_join, 0);
 }
@@ -495,11 +499,11 @@ __global__ void __launch_bounds__(kBlock) k32_kick(DevBeam bm, const ScState *sc
   }
 }
 
-DepQ dep_quant(uint32_t n, int grid, size_t hist_bytes) {
+DepQ dep_quant(uint32_t n, int grid, uint32_t threads, size_t hist_bytes) {
   DepQ q{};
-  uint32_t per = (uint32_t)grid * kBlock;
+  uint32_t per = (uint32_t)grid * threads;
   uint32_t iters = (n + per - 1) / per;
-  uint64_t p = (uint64_t)iters * kBlock;  // particles one block can deposit
+  uint64_t p = (uint64_t)iters * threads;  // particles one block can deposit
   int bits = 0;
   while ((1ull << bits) <= p) ++bits;
   int s = 30 - bits;
@@ -563,13 +567,14 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
   uint32_t ndep = 0;
   size_t hb = 0;
   DepQ q{};
+  const uint32_t dthreads = a.dep_threads ? a.dep_threads : 256u;  // deposit block size
   if (a.deposit_ok) {
     // dep_per_sm blocks per SM at most (three unless tuned), in whole clusters
-    ndep = std::min<uint32_t>((b.n + kBlock - 1) / kBlock, (a.dep_per_sm ? a.dep_per_sm : 3u) * 152u);
+    ndep = std::min<uint32_t>((b.n + dthreads - 1) / dthreads, (a.dep_per_sm ? a.dep_per_sm : 3u) * 152u);
     ndep = (ndep + kDepCluster - 1) / kDepCluster * kDepCluster;
     hb = (size_t)a.nx_max * a.nz_max * sizeof(int);
     if (hb > kMaxHistSmem) hb = 0;
-    q = dep_quant(b.n, (int)ndep, hb);
+    q = dep_quant(b.n, (int)ndep, dthreads, hb);
     q.agg = a.dep_agg ? 1 : 0;
   }
   // Green's table entries of the largest mesh, a few per thread on one block
@@ -583,7 +588,7 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
       return;
     }
     record("green", &green_merge, 4u * ngreen, MeshSeg{sc, u});
-    record("deposit", &deposit_merge, ndep, DepSeg{b, sc, u, q, hb});
+    record("deposit", &deposit_merge, ndep, DepSeg{b, sc, u, q, hb, dthreads}, dthreads);
     contract32(sc, u, a.nx_max, a.nz_max, a.mesh_fixed, st);
     return;
   }
@@ -592,7 +597,7 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
     // the Green's table and the contraction, which return at once when the
     // network's field was accepted
     if (ndep) {
-      launch_k(k32_green_deposit, dim3(ndep), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, 0u);
+      launch_k(k32_green_deposit, dim3(ndep), dim3(dthreads), q.smem ? hb : 0, st, b, sc, u, q, ndep, 0u);
       note_launch();
     }
     sur_solve(b, sc, u, a, *sur, st, 1);
@@ -608,11 +613,11 @@ void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArg
     cudaStreamWaitEvent(fork->side, fork->ev_fork, 0);
     k32_green<<<ng, kBlock, 0, fork->side>>>(sc, u);
     cudaEventRecord(fork->ev_join, fork->side);
-    launch_k(k32_green_deposit, dim3(ndep), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, 0u);
+    launch_k(k32_green_deposit, dim3(ndep), dim3(dthreads), q.smem ? hb : 0, st, b, sc, u, q, ndep, 0u);
     cudaStreamWaitEvent(st, fork->ev_join, 0);
     note_launch(2);
   } else {
-    launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(kBlock), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
+    launch_k(k32_green_deposit, dim3(ndep + ngreen), dim3(dthreads), q.smem ? hb : 0, st, b, sc, u, q, ndep, ngreen);
     note_launch();
   }
   contract32(sc, u, a.nx_max, a.nz_max, a.mesh_fixed, st);

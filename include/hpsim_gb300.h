@@ -329,14 +329,16 @@ hps_status hps_batch_last_mode(hps_batch_t batch, int *lockstep, char *why, size
 /* ---- autotuner (no reference counterpart; it replaces the reference's fixed
  * launch geometry, e.g. the 64-block cap of src/beam/src/beam.cu:419 and the
  * contraction grid of src/simulation/src/space_charge.cu:189-200).  A launch
- * shape of an FP32 beam's simulation is shape[4] = {contraction kernel (0
+ * shape of an FP32 beam's simulation is shape[5] = {contraction kernel (0
  * split-BF16 tensor cores where the mesh allows, 1 FP32 CUDA cores),
  * deposit blocks per SM (1..8), particle-sweep blocks per SM (0: as many as
  * an SM holds, else a cap 1..16), deposit histogram adds (0 one shared-
  * memory atomic per particle and bin, 1 warp-aggregated: lanes with the
- * same bin sum their weights first)}.  hps_sim_autotune times candidate
- * shapes on the simulator's own simulate(start, end) with CUDA events
- * (coordinate descent over the four knobs; each candidate the median of `reps` runs
+ * same bin sum their weights first), deposit threads per block (256, 512 or
+ * 1024; 0 reads as 256)}.  hps_sim_autotune times candidate shapes on the
+ * simulator's own simulate(start, end) with CUDA events (coordinate descent
+ * over the knobs, the deposit's block size and blocks per SM together; each
+ * candidate the median of `reps` runs
  * after an untimed one that captures its graph; every run starts from a
  * snapshot of the beam, solver and engine state, which is restored at the
  * end), keeps the fastest and caches it per (device, mesh, power-of-two
@@ -351,8 +353,8 @@ hps_status hps_sim_autotune(hps_sim_t sim, int32_t start, int32_t end, int32_t r
                             double *ms_out, uint32_t ms_cap, uint32_t *n_timed);
 hps_status hps_batch_autotune(hps_batch_t batch, int32_t start, int32_t end, int32_t reps, int32_t *shape_out,
                               double *ms_out, uint32_t ms_cap, uint32_t *n_timed);
-hps_status hps_sim_get_shape(hps_sim_t sim, int32_t *shape_out /* 4 */);
-hps_status hps_sim_set_shape(hps_sim_t sim, const int32_t *shape /* 4 */);
+hps_status hps_sim_get_shape(hps_sim_t sim, int32_t *shape_out /* 5 */);
+hps_status hps_sim_set_shape(hps_sim_t sim, const int32_t *shape /* 5 */);
 
 /* ---- SCHEFF field surrogate: network layers (no reference counterpart).
  * Device pointers; tensors [batch][channel][z][r]; x, w, y BF16, bias, dy,

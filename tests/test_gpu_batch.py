@@ -101,7 +101,8 @@ def test_autotune_leaves_no_trace_and_its_shape_reproduces():
     res = sim.autotune(reps=2)
     assert len(res["ms"]) >= 4 and all(t > 0 for t in res["ms"])
     assert sim.get_shape() == res["shape"]
-    assert res["shape"]["contraction"] in (0, 1) and 2 <= res["shape"]["deposit_blocks_per_sm"] <= 4
+    assert res["shape"]["contraction"] in (0, 1) and 1 <= res["shape"]["deposit_blocks_per_sm"] <= 4
+    assert res["shape"]["deposit_threads"] * res["shape"]["deposit_blocks_per_sm"] <= 1024
     sim.enable_monitor(True)
     sim.simulate()
     tuned = sim.monitor.copy(), beam._coord("xp")
