@@ -129,7 +129,6 @@ struct OpPushScStats {
   static constexpr int K = 14;
   static constexpr int kMaxFrom = 12;
   static constexpr int kBatch = 4;
-  static constexpr int kMinBlocks = 3;
   static constexpr bool kFast = true;
   using Comb = SumComb;
   struct Ctx { float s; };

@@ -152,13 +152,6 @@ struct op_max_from : std::integral_constant<int, Op::K> {};
 template <class Op>
 struct op_max_from<Op, std::void_t<decltype(Op::kMaxFrom)>> : std::integral_constant<int, Op::kMaxFrom> {};
 
-// An Op with `static constexpr int kMinBlocks = b` asks the compiler for b
-// resident blocks per SM (a register budget); default 1.
-template <class Op, class = void>
-struct op_min_blocks : std::integral_constant<int, 1> {};
-template <class Op>
-struct op_min_blocks<Op, std::void_t<decltype(Op::kMinBlocks)>> : std::integral_constant<int, Op::kMinBlocks> {};
-
 template <class C, int MF>
 __device__ inline float comb_k(int k, float a, float b) {
   return k >= MF ? fmaxf(a, b) : C::comb(a, b);
@@ -263,7 +256,7 @@ __device__ __forceinline__ void pass_body_f(const Op &op, uint32_t n, PassScratc
 }
 
 template <class Op>
-__global__ void __launch_bounds__(kBlock, op_min_blocks<Op>::value) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
+__global__ void __launch_bounds__(kBlock) pass_kernel_f(Op op, uint32_t n, PassScratch scr) {
   pass_body_f(op, n, scr, blockIdx.x, gridDim.x);
 }
 
