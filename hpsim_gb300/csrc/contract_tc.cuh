@@ -83,9 +83,6 @@ struct TcDims {
   uint32_t S;        // pipeline stages
   uint32_t L;        // elements of one shifted copy of the padded charge column
   uint32_t tiles;    // nz / 128
-  uint32_t KS;       // CTAs splitting a tile's chunks (more CTAs for meshes with few tiles x radii)
-  uint32_t CPS;      // chunks per split
-  uint32_t G;        // partials per tile and field column: nr x KS, (source radius, split) radius-major
   size_t smem;       // dynamic shared memory of k_contract_tc
 };
 
@@ -99,12 +96,6 @@ inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
   const size_t fixed = 1024 + (size_t)16 * d.L * 2 + (size_t)nz * 4 + 256;
   d.S = fixed + 3 * tc_stage_bytes(d.BT) <= kTcSmemMax ? 3 : 2;
   d.smem = fixed + d.S * tc_stage_bytes(d.BT);
-  // a tile's chunks split over KS CTAs while tiles x radii x KS stays within
-  // the SMs (one CTA per SM), no split left empty
-  const uint32_t ks0 = std::max(1u, std::min(d.CPT, 152u / (d.tiles * nr)));
-  d.CPS = (d.CPT + ks0 - 1) / ks0;
-  d.KS = (d.CPT + d.CPS - 1) / d.CPS;
-  d.G = nr * d.KS;
   return d;
 }
 
@@ -112,8 +103,7 @@ inline TcDims tc_dims(uint32_t nr, uint32_t nz) {
 // last row's per-radius partials)
 inline size_t tc_table_bytes(uint32_t nr, uint32_t nz) { return (size_t)nr * (2 * nz / kTcKC) * 2 * tc_n(nr) * 128; }
 inline size_t tc_partial_bytes(uint32_t nr, uint32_t nz) {
-  const TcDims d = tc_dims(nr, nz);
-  return ((size_t)d.tiles * d.G * d.N * kTcM + (size_t)d.G * d.N) * 4;
+  return ((size_t)(nz / kTcM) * nr * tc_n(nr) * kTcM + (size_t)nr * tc_n(nr)) * 4;
 }
 
 // the tensor-core path runs this kick: FP32 tables sized for this mesh
@@ -153,10 +143,9 @@ __device__ __forceinline__ float tc_charge(unsigned long long v) {
 }
 
 // ---- the product ------------------------------------------------------------
-// the CTA of field-row tile bx / KS, chunk split bx % KS and source radius rs
+// the CTA of field-row tile `tile` and source radius `rs`
 __device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTables &t, const TcDims &d,
-                                                 uint32_t bx, uint32_t rs) {
-  const uint32_t tile = bx / d.KS, ks = bx % d.KS, g = rs * d.KS + ks;
+                                                 uint32_t tile, uint32_t rs) {
   if (!tc_go(sc, t)) return;
   extern __shared__ unsigned char tc_raw[];
   __shared__ uint64_t full[3], empty[3], done;
@@ -193,8 +182,7 @@ __device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTabl
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  // this CTA's chunks of the folded range: the tile's chunks [cl, cl + nch)
-  const uint32_t cl = ks * d.CPS, c0 = 2 * tile + cl, nch = std::min(d.CPT, cl + d.CPS) - cl;
+  const uint32_t c0 = 2 * tile, nch = d.CPT;  // this tile's chunks of the folded range
   bool issued_mma = false;
 
   if (warp < 4) {
@@ -243,8 +231,8 @@ __device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTabl
         bulk_g2s(st + 2 * 16384, src, BT, &full[s]);
         bulk_g2s(st + 2 * 16384 + BT, src + BT, BT, &full[s]);
       }
-      // row m of the tile's chunk cl + i: R(W .. W + 63), W = 64 (cl + i) - m (+128 into the copies)
-      const int wp = 64 * (int)(cl + i) - (int)m + 128;
+      // row m of the chunk: R(W .. W + 63), W = 64 i - m (+128 into the copies)
+      const int wp = 64 * (int)i - (int)m + 128;
       const int sh = wp & 7, base = wp - sh;
       const uint4 *hi = (const uint4 *)(cp + sh * L + base);
       const uint4 *lo = (const uint4 *)(cp + (8 + sh) * L + base);
@@ -289,7 +277,7 @@ __device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTabl
     if (last_row && !*abort) {
       // rows n < N only: a thread beyond them would write into the next
       // radius's partials
-      float *pl = t.tcp + (size_t)d.tiles * d.G * N * kTcM + (size_t)g * N;
+      float *pl = t.tcp + (size_t)d.tiles * nr * N * kTcM + (size_t)rs * N;
       if (tid < N) pl[tid] = lr0;
       if (tid + 128 < N) pl[tid + 128] = lr1;
     }
@@ -320,7 +308,7 @@ __device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTabl
     const bool ok = !*abort && mbar_wait(&done, 0, abort);
     if (ok) {
       tc_fence_after();
-      float *out = t.tcp + ((size_t)(tile * d.G + g) * N) * kTcM + 32 * warp + lane;
+      float *out = t.tcp + ((size_t)(tile * nr + rs) * N) * kTcM + 32 * warp + lane;
       const uint32_t tl = tmem + ((32 * warp) << 16);
       for (uint32_t c = 0; c < N; c += 16) {
         float v[16];
@@ -353,7 +341,7 @@ __device__ __forceinline__ void contract_tc_body(const ScState *sc, const ScTabl
   }
 }
 
-// grid (tiles x KS, nr): tile and chunk split blockIdx.x, source radius blockIdx.y
+// grid (tiles, nr): tile blockIdx.x of field rows, source radius blockIdx.y
 __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc(const ScState *sc, ScTables t, TcDims d) {
   contract_tc_body(sc, t, d, blockIdx.x, blockIdx.y);
 }
@@ -365,13 +353,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_contract_tc_seg(const __grid_
   contract_tc_body(p.sc, p.t, d, blockIdx.x, blockIdx.y);
 }
 
-// The partials summed over the source radii and chunk splits: a block takes
-// 64 consecutive field rows of one field radius (blockIdx.y), its four
-// thread quarters a quarter of the G = nr x KS partials each (rows adjacent
-// in memory, so every load of a warp is coalesced), summed in (radius,
-// split) order within a quarter and the quarters in order: deterministic.
-// Tile partials for the rows zp < nz, the last tile's last-row partials for
-// zp = nz.
+// The partials summed over the source radii: a block takes 64 consecutive
+// field rows of one field radius (blockIdx.y), its four thread quarters a
+// quarter of the source radii each (rows adjacent in memory, so every load
+// of a warp is coalesced), summed in radius order within a quarter and the
+// quarters in order: deterministic.  Tile partials for the rows zp < nz, the
+// last tile's last-row partials for zp = nz.
 __device__ __forceinline__ void tc_reduce_body(const ScState *sc, const ScTables &t, const TcDims &d, uint32_t bx,
                                                uint32_t by) {
   if (!tc_go(sc, t)) return;
@@ -384,15 +371,15 @@ __device__ __forceinline__ void tc_reduce_body(const ScState *sc, const ScTables
     const float *p;
     size_t stride, comp;
     if (zp < nz) {
-      p = t.tcp + ((size_t)(zp / kTcM) * d.G * N + 2 * rp) * kTcM + zp % kTcM;
+      p = t.tcp + ((size_t)(zp / kTcM) * nr * N + 2 * rp) * kTcM + zp % kTcM;
       stride = (size_t)N * kTcM;
       comp = kTcM;
     } else {
-      p = t.tcp + (size_t)d.tiles * d.G * N * kTcM + 2 * rp;
+      p = t.tcp + (size_t)d.tiles * nr * N * kTcM + 2 * rp;
       stride = N;
       comp = 1;
     }
-    const uint32_t per = d.G / 4, g0 = q * per;  // G >= 16: a multiple of 4 partials per quarter
+    const uint32_t per = nr / 4, g0 = q * per;  // nr >= 16: a multiple of 4 radii per quarter
     for (uint32_t g = g0; g < g0 + per; g += 4) {
       float vx[4], vz[4];
 #pragma unroll
@@ -453,7 +440,7 @@ inline void contract_tc_merge(const std::vector<const Rec *> &recs, Arena &, cud
   }
   seg_chunks<MeshSeg>(hp, [&](const auto &a, uint32_t) {
     constexpr int B = std::decay_t<decltype(a)>::kB;
-    k_contract_tc_seg<B><<<dim3(d.tiles * d.KS, nr, a.nb), kTcThreads, d.smem, st>>>(a, d);
+    k_contract_tc_seg<B><<<dim3(d.tiles, nr, a.nb), kTcThreads, d.smem, st>>>(a, d);
     k_tc_reduce_seg<B><<<dim3((nz + 1 + 63) / 64, nr + 1, a.nb), 256, 0, st>>>(a, d);
   });
 }
@@ -466,7 +453,7 @@ inline void contract_tc_launch(const ScState *sc, const ScTables &t, uint32_t nr
     return;
   }
   const TcDims d = tc_dims(nr, nz);
-  k_contract_tc<<<dim3(d.tiles * d.KS, nr), kTcThreads, d.smem, st>>>(sc, t, d);
+  k_contract_tc<<<dim3(d.tiles, nr), kTcThreads, d.smem, st>>>(sc, t, d);
   k_tc_reduce<<<dim3((nz + 1 + 63) / 64, nr + 1), 256, 0, st>>>(sc, t, d);
 }
 
