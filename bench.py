@@ -254,8 +254,8 @@ STEP_BYTES = {"fp32": 56, "fp64": 104}
 PHASE_KERNELS = {
     "fp32": {"quad": "pass_kernel_f<OpPushScStats<QuadMap>>", "gap1": "pass_kernel_f<OpPushScStats<Gap1Map>>",
              "drift": "pass_kernel_f<OpPushScStats<DriftMap>>",
-             "sc_stats": "none at a fused kick (the statistics are in the sweep before it); "
-                         "pass_kernel_f<Op32ScStats> elsewhere",
+             "sc_stats": "pass_kernel_f<Op32LlossScStats> (returns at once when the sweep before the kick "
+                         "certified its statistics)",
              "sc_mesh": "k32_green + k32_green_deposit + k_contract_m | k_contract_tc + k_tc_reduce", "sc_kick": "k32_kick_push<QuadMap|Gap2Map|DriftMap>"},
     "fp64": {},
 }

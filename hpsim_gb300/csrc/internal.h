@@ -159,11 +159,17 @@ int sur_read(const SurNet &n, double *accepted, double *rejected, double *residu
 int sur_conv_state(const SurNet &n, int *tc_layers, unsigned int *err);
 
 // ---- FP32 beams (push32.cu, beam32.cu, scheff32.cu) ----------------------
+// the statistics after a PUSH_SCSTATS map that could not certify its own:
+// the longitudinal-loss test and the SCHEFF moments in one sweep, repeated
+// only when the test flagged a particle (the good set, hence <phi>_good,
+// changed).  Both sweeps return at once when they are not needed.
+void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+                           PassScratch s, cudaStream_t st);
 // An element map fused with the space-charge sweep next to it:
 //  PUSH_SCSTATS     the map, then every statistic of the kick after it from
-//                   the new state, the decision and the kick's constants
-//                   (when the sweep cannot certify its statistics, its
-//                   finalising block runs the loss test and the moments);
+//                   the new state, the decision and the kick's constants,
+//                   when the sweep can certify them (else sc_redo = 2 and
+//                   sc32_stats_after_push completes them);
 //  PUSH_AFTER_KICK  the SCHEFF kick, then the map, in one sweep.
 enum { PUSH_SCSTATS = 1, PUSH_AFTER_KICK = 2 };
 struct PushFuse {

@@ -107,8 +107,7 @@ __global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m, Shift sh) {
 // state (UpdateStatForSpaceCharge and the longitudinal-loss test of
 // Scheff::Start, space_charge.cpp:86-101; beam.cpp:776-852, 1008-1009) in
 // the same sweep, and in the finaliser the decision and the kick's
-// constants (so that a kick takes no statistics launch of its own).  Phase
-// sums are taken about s, the offset of <phi>_good from
+// constants.  Phase sums are taken about s, the offset of <phi>_good from
 // the synchronous particle at the last kick of this simulation call (zero at
 // its first), an estimate of the new one: <phi>_good from the raw offsets,
 // sigma_phi and the mean relative phase of the live particles from the
@@ -116,10 +115,11 @@ __global__ void __launch_bounds__(kBlock) k32_push(DevBeam b, Map m, Shift sh) {
 // separate sweeps' answers: no particle lies above <phi>_good + 3 pi (the
 // loss test flags none) and no relative phase lies within |<phi>_good - s|
 // of a wrap boundary (it wraps about <phi>_good as about s).  Without the
-// certificate the finalising block records the counts and <phi>_good and
-// runs the loss-test and moments sweeps itself (sc32_fallback_block); so it
-// does when s lies more than 4 sigma_phi from <phi>_good, where sigma_phi^2
-// as a difference of FP32 moments about s would lose precision.
+// certificate the finaliser records the counts and <phi>_good and sets
+// sc_redo = 2 for the loss-test and moments sweeps (one grid-wide launch
+// after this one, sc32_stats_after_push); so it does when s lies more than 4
+// sigma_phi from <phi>_good, where sigma_phi^2 as a difference of FP32
+// moments about s would lose precision.
 template <class Map>
 struct OpPushScStats {
   // 0 good count, 1 sum d (raw, for <phi>_good), 2-3 sum f, f^2 (wrapped, for
@@ -193,11 +193,12 @@ struct OpPushScStats {
         for (int k = 1; k < 8; ++k) sm[k] = t[k + 1];
         st.sc_redo = 0u;
         sc_moments_finish(b, sm, sc, tb, freq, frac, h);
+      } else {
+        st.sc_redo = 2u;
       }
     }
     __syncthreads();
-    if (!ok) sc32_fallback_block(b, sc, tb, freq, frac, h, tid, nth);
-    zero_mesh_tables(sc, tb, tid, nth);
+    if (ok) zero_mesh_tables(sc, tb, tid, nth);
   }
 };
 

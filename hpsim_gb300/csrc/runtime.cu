@@ -1117,7 +1117,7 @@ void sc_apply(Ctx &c, double length, bool fused = false) {
   if (f32(b)) {
     sc32_configure();
     if (fused) {
-      // the fused sweep before the kick took every statistic (sc32_stats.cuh)
+      PHASE(HPS_PROF_SC_STATS, sc32_stats_after_push(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream));
       PHASE(HPS_PROF_SC_MESH, sc32_mesh(b->d, c.sc->d, c.sc->t, a, b->scr, b->stream, c.sc->sur, &b->fork));
       return;
     }

@@ -169,105 +169,5 @@ __device__ inline void sc_moments_add(float (&a)[12], float pr, uint32_t lo, uin
   a[7] += gd * w;
 }
 
-// totals of k per-thread values over the block, in a fixed order: each warp
-// by a shuffle tree, then the warps in order (every thread gets them in tot)
-template <int K>
-__device__ inline void block_sums(double (&v)[K], double *red /* [32][K] */, double *tot /* [K] */, int tid,
-                                  int nth) {
-  const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double x = v[k];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-    if (lane == 0) red[warp * K + k] = x;
-  }
-  __syncthreads();
-  if (tid < K) {
-    double x = 0.0;
-    for (int w = 0; w < nth / 32; ++w) x += red[w * K + tid];
-    tot[tid] = x;
-  }
-  __syncthreads();
-}
-
-// The statistics of a kick whose fused sweep could not certify them, by the
-// one block that finalised that sweep: the longitudinal-loss test about the
-// recorded <phi>_good (Scheff::Start, space_charge.cpp:86-101) with the
-// relative phases and the SCHEFF moments in the same pass, and, if the test
-// flagged particles of the good set, the moments again about the new
-// <phi>_good; then the decision and the kick's constants.  A rare path, so
-// it takes no launch of its own: each thread sums runs of 64 particles in
-// FP32 and the runs in FP64.
-__device__ __noinline__ void sc32_fallback_block(const DevBeam &b, ScState *sc, const ScTables &t, double freq, double frac,
-                                    const Sc32Host &h, int tid, int nth) {
-  __shared__ double red[32 * 12];
-  __shared__ double tot[12];
-  const double pag0 = b.st->st[PHI_AVG_GOOD] - b.phi_ref;
-  const float lim = (float)(pag0 + TWOPI + PI), pag = (float)pag0;
-  double v[12];
-#pragma unroll
-  for (int k = 0; k < 12; ++k) v[k] = 0.0;
-  for (uint32_t i0 = (uint32_t)tid; i0 < b.n; i0 += 64u * (uint32_t)nth) {
-    float a[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) a[k] = 0.0f;
-    for (uint32_t i = i0, r = 0; r < 64u && i < b.n; ++r, i += (uint32_t)nth) {
-      const uint32_t lo = b.loss[i];
-      uint32_t ll = b.lloss[i];
-      const float ph = b.fphi[i];
-      if (ph > lim && ll != 1u) {
-        if (lo == 0u && ll == 0u) a[11] += 1.0f;
-        ll = 1u;
-        b.lloss[i] = 1u;
-      }
-      const float pr = rel_phase_f(ph - pag);
-      b.fphi_r[i] = pr;
-      sc_moments_add(a, pr, lo, ll, b.fx[i], b.fy[i], b.fw[i]);
-      const bool g = (lo | ll) == 0u;
-      a[8] += ll != 0u ? 1.0f : 0.0f;
-      a[9] += g ? 1.0f : 0.0f;
-      a[10] += g ? ph : 0.0f;
-    }
-#pragma unroll
-    for (int k = 0; k < 12; ++k) v[k] += (double)a[k];
-  }
-  block_sums<12>(v, red, tot, tid, nth);
-  const uint32_t ng = (uint32_t)tot[9];
-  const bool redo = tot[11] != 0.0;
-  if (tid == 0) {
-    sc->n_stat_sweeps += 1;
-    BeamStats &st = *b.st;
-    st.num_lloss = (uint32_t)tot[8];
-    st.num_good = ng;
-    if (redo) st.st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)tot[10] / (float)ng) + b.phi_ref : -99999;
-  }
-  __syncthreads();
-  if (redo) {  // the good set changed: the moments again about the new <phi>_good
-    const float pag1 = (float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref);
-    double u[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) u[k] = 0.0;
-    for (uint32_t i0 = (uint32_t)tid; i0 < b.n; i0 += 64u * (uint32_t)nth) {
-      float a[12];
-#pragma unroll
-      for (int k = 0; k < 12; ++k) a[k] = 0.0f;
-      for (uint32_t i = i0, r = 0; r < 64u && i < b.n; ++r, i += (uint32_t)nth) {
-        const float pr = rel_phase_f(b.fphi[i] - pag1);
-        b.fphi_r[i] = pr;
-        sc_moments_add(a, pr, b.loss[i], b.lloss[i], b.fx[i], b.fy[i], b.fw[i]);
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) u[k] += (double)a[k];
-    }
-    block_sums<8>(u, red, tot, tid, nth);
-  }
-  if (tid == 0) {
-    sc_moments_finish(b, tot, sc, t, freq, frac, h);
-    b.st->sc_redo = 0u;
-  }
-  __syncthreads();
-}
-
 }  // namespace
 }  // namespace hps

@@ -13,10 +13,10 @@
 //  * ahead of a kick on four or more particles, the element half before it
 //    takes every statistics sweep in its own sweep (push32.cu,
 //    OpPushScStats) and certifies that the loss test flags no particle
-//    and that no relative phase wraps; only when it cannot, the block that
-//    finalises that sweep runs the loss test and the moments itself
-//    (sc32_fallback_block in sc32_stats.cuh).  The kick runs inside the
-//    element half after it;
+//    and that no relative phase wraps; only when it cannot, the loss test
+//    and the moments run here in one small launch (Op32LlossScStats, whose
+//    last block sweeps the moments again when the good set changed).  The
+//    kick runs inside the element half after it;
 //  * relative phases are not stored: the deposit and the kick form
 //    wrap(phi - <phi>_good) from the phase offset and Sc32Consts::pag;
 //  * the deposit keeps a 32-bit fixed-point histogram per block in shared
@@ -147,6 +147,112 @@ struct Op32ScStats {
     }
     if (!sc) return;
     __syncthreads();
+    zero_mesh_tables(sc, t, tid, nth);
+  }
+};
+
+// The longitudinal-loss test (UpdateLongitudinalLossCoordinateKernel with the
+// lloss and good counts and <phi>_good, beam.cpp:780-781, 1008-1009) and the
+// SCHEFF moments in one sweep, when the element map before the kick could
+// not certify its own statistics (sc_redo == 2).  The relative phases are
+// taken about the <phi>_good that sweep recorded; when the test flags no
+// particle of the good set, that is the <phi>_good the separate sweeps would
+// have used, and the totals are the same ones in the same order.  Otherwise
+// the sweep records the new <phi>_good and asks for the moments sweep again
+// (sc_redo = 1).
+struct Op32LlossScStats {
+  static constexpr int K = 12;
+  static constexpr bool kFast = true;
+  using Comb = SumComb;
+  struct Ctx { float lim, pag; };
+  DevBeam b;
+  ScState *sc;
+  ScTables t;
+  double freq, frac;
+  Sc32Host h;
+  __device__ bool enabled() const { return b.st->sc_redo == 2u; }
+  __device__ Ctx setup() const {
+    const double pag = b.st->st[PHI_AVG_GOOD] - b.phi_ref;
+    return {(float)(pag + TWOPI + PI), (float)pag};
+  }
+  struct P { uint32_t lo, ll; float ph, x, y, w; };
+  __device__ P load(uint32_t i) const { return {b.loss[i], b.lloss[i], b.fphi[i], b.fx[i], b.fy[i], b.fw[i]}; }
+  __device__ void use(uint32_t i, const P &p, float (&a)[K], const Ctx &c) const {
+    uint32_t ll = p.ll;
+    float newly = 0.0f;
+    if (p.ph > c.lim && ll != 1u) {
+      if (p.lo == 0u && ll == 0u) newly = 1.0f;
+      ll = 1u;
+      b.lloss[i] = 1u;
+    }
+    const float pr = rel_phase_f(p.ph - c.pag);
+    b.fphi_r[i] = pr;
+    sc_moments_add(a, pr, p.lo, ll, p.x, p.y, p.w);
+    const bool g = (uint32_t)(p.lo + ll) == 0u;
+    a[8] += ll != 0u ? 1.0f : 0.0f;
+    a[9] += g ? 1.0f : 0.0f;
+    a[10] += g ? p.ph : 0.0f;
+    a[11] += newly;
+  }
+  __device__ void finalize(const double *s, int tid, int nth) const {
+    __shared__ int redo;
+    __shared__ float red[kBlock / 32][8];
+    __shared__ double mom[8];
+    if (tid == 0) {
+      sc->n_stat_sweeps += 1;
+      BeamStats &st = *b.st;
+      const uint32_t ng = (uint32_t)s[9];
+      st.num_lloss = (uint32_t)s[8];
+      st.num_good = ng;
+      redo = s[11] != 0.0;
+      if (redo) {
+        st.st[PHI_AVG_GOOD] = ng > 0 ? (double)((float)s[10] / (float)ng) + b.phi_ref : -99999;
+      } else {
+        sc_moments_finish(b, s, sc, t, freq, frac, h);
+        st.sc_redo = 0u;
+      }
+    }
+    __syncthreads();
+    if (redo) {
+      // the loss test changed the good set: the moments again about the new
+      // <phi>_good (Op32ScStats), swept by this last block alone -- a rare
+      // path, kept out of a launch of its own; thread order, then a fixed
+      // shuffle tree and the warps in order
+      const float pag = (float)(b.st->st[PHI_AVG_GOOD] - b.phi_ref);
+      float a[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) a[k] = 0.0f;
+      for (uint32_t i = tid; i < b.n; i += nth) {
+        const float pr = rel_phase_f(b.fphi[i] - pag);
+        b.fphi_r[i] = pr;
+        float a12[12];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a12[k] = a[k];
+        sc_moments_add(a12, pr, b.loss[i], b.lloss[i], b.fx[i], b.fy[i], b.fw[i]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = a12[k];
+      }
+      const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        float v = a[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][k] = v;
+      }
+      __syncthreads();
+      if (tid < 8) {
+        double v = 0.0;
+        for (int w = 0; w < nth / 32; ++w) v += (double)red[w][tid];
+        mom[tid] = v;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        sc_moments_finish(b, mom, sc, t, freq, frac, h);
+        b.st->sc_redo = 0u;
+      }
+      __syncthreads();
+    }
     zero_mesh_tables(sc, t, tid, nth);
   }
 };
@@ -555,6 +661,18 @@ void sc32_stats(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickAr
     launch_k(k32_decide_only, dim3(1), dim3(kBlock), 0, st, b, sc, u, a.freq, a.frac, h);
     note_launch();
   }
+}
+
+// one launch of one block per SM: it returns at once when the element map
+// before the kick certified its statistics (every kick of the bench
+// workloads), so its cost there is the launch alone
+void sc32_stats_after_push(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a,
+                           PassScratch s, cudaStream_t st) {
+  ScTables u = tables32(t);
+  const Sc32Host h = sc32_host(b, a);
+  launch_pass_f_grid(Op32LlossScStats{b, sc, u, a.freq, a.frac, h}, b.n, s, st, (uint32_t)pass_blocks_f(b.n, 1),
+                     "stats_fallback");
+  if (!recorder()) note_launch();
 }
 
 void sc32_mesh(const DevBeam &b, ScState *sc, const ScTables &t, const ScKickArgs &a, PassScratch s,
