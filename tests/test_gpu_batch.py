@@ -160,3 +160,33 @@ def test_aggregated_deposit_adds_give_the_same_table():
         assert np.array_equal(out[0][0], out[1][0])
         for a, b in zip(out[0][1], out[1][1]):
             assert np.array_equal(a, b)
+
+
+def test_deposit_block_sizes_agree():
+    """The deposit's block size (launch-shape knob deposit_threads: 256, 512,
+    1024 threads) changes the fixed-point scale of the per-block histograms,
+    not the physics: the same transmission and loss flags, emittances within
+    1e-4 relative at every element."""
+    import numpy as np
+    from hpsim_gb300 import HPSim, lattices as L
+    runs = {}
+    for threads, per_sm in ((256, 3), (512, 1), (1024, 1)):
+        beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=65536, precision="fp32")
+        beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 33)
+        beam.set_ref_w(0.75)
+        beam.set_ref_phi(0.0)
+        sc = HPSim.SpaceCharge(64, 256)
+        sc.set_remesh_threshold(0.0)
+        sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.dtl_like(n_gaps=8)), sc)
+        sim.set_shape({"contraction": 0, "deposit_blocks_per_sm": per_sm, "sweep_blocks_per_sm": 0,
+                       "deposit_aggregate": 0, "deposit_threads": threads})
+        sim.enable_monitor(True)
+        sim.simulate()
+        runs[threads] = (sim.monitor.copy(), beam._loss(0), beam._loss(1))
+    ref = runs[256]
+    for threads in (512, 1024):
+        mon, loss, lloss = runs[threads]
+        assert np.array_equal(loss, ref[1]) and np.array_equal(lloss, ref[2])
+        assert np.array_equal(mon[:, 0], ref[0][:, 0])
+        for i in (6, 11, 16):
+            assert np.max(np.abs(mon[:, i] / ref[0][:, i] - 1.0)) <= 1e-4, (threads, i)
