@@ -49,12 +49,14 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--workload", default="dtl_like",
-                   choices=["dtl_like", "small_fodo", "ccl_large", "batched", "ccl_batch"],
+                   choices=["dtl_like", "small_fodo", "ccl_large", "batched", "ccl_batch", "surrogate_net"],
                    help="dtl_like: one 1M-particle beam through 165 DTL gaps (the headline); small_fodo: "
                         "65,536 particles in FP64 through buncher + 40 FODO elements; ccl_large: 16,777,216 "
                         "particles through 1024 CCL gaps, SCHEFF 64x256; batched: 256 beams of the "
                         "small-FODO topology in one graph launch; ccl_batch: 16 beams of 1,048,576 particles "
-                        "through the CCL lattice with perturbed set points in one graph launch")
+                        "through the CCL lattice with perturbed set points in one graph launch; surrogate_net: "
+                        "the learned field surrogate's forward pass at batches of 1, 8 and 32 planes, its "
+                        "layers on CUDA cores and on the tensor cores")
     p.add_argument("--beams", type=int, default=None, help="batched: 256, ccl_batch: 16")
     p.add_argument("--lockstep", action="store_true",
                    help="batches run in lockstep (one launch per kernel for all beams) instead of as per-simulator "
@@ -545,6 +547,95 @@ def surrogate_accuracy(args, check):
     return accuracy(mon, sim.mon.copy(), loss, b.arr("loss").copy(), lloss, b.arr("lloss").copy())
 
 
+def run_surrogate_net(args):
+    """The surrogate network's forward pass (ten layers, random weights of the
+    shipped architecture, 128 x 32 planes) at batches of 1, 8 and 32 planes,
+    captured as one CUDA graph per variant and timed with CUDA events over
+    max(--steps, 20) replays after --warmup: the layers on CUDA cores
+    (hps_nn_conv_forward) and on the tensor cores (hps_nn_conv_forward_tiles,
+    weight tiles laid out once).  value = the tensor-core forward time at
+    batch 32 (ms, lower is better); the table is under "forward_ms"."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from hpsim_gb300 import HPSim, build, surrogate as S  # noqa: F401
+    from hpsim_gb300._capi import call
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    build.build()
+    HPSim.set_gpu(local)
+
+    def ptr(t):
+        return C.c_void_p(t.data_ptr())
+
+    rng = np.random.default_rng(0)
+    table = {}
+    for B in (1, 8, 32):
+        shapes = S.layer_shapes(B)
+        wts = [torch.tensor(rng.normal(size=(co, ci, 3, 3)) / np.sqrt(9 * ci), dtype=torch.bfloat16, device="cuda")
+               for ci, co, *_ in S.ARCH]
+        bias = [torch.zeros(co, device="cuda") for _, co, *_ in S.ARCH]
+        x = torch.randn(B, 2, S.NZ, S.NR, device="cuda").to(torch.bfloat16)
+        acts, tiles = [], []
+        for d, w in zip(shapes, wts):
+            b_, ci, co, h, wd, s, u = (int(v) for v in d)
+            acts.append(torch.empty(b_, co, (h * u - 1) // s + 1, (wd * u - 1) // s + 1, dtype=torch.bfloat16,
+                                    device="cuda"))
+            nb = C.c_uint64()
+            call("hps_nn_conv_tc_tile_bytes", d.ctypes.data_as(C.POINTER(C.c_int)), C.byref(nb))
+            t = torch.empty(int(nb.value), dtype=torch.uint8, device="cuda")
+            call("hps_nn_conv_tc_prepare", d.ctypes.data_as(C.POINTER(C.c_int)), ptr(w), ptr(t), None)
+            tiles.append(t)
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        cs = torch.cuda.Stream()
+
+        def net(tc):
+            st = C.c_void_p(cs.cuda_stream)
+            cur = x
+            for l, (d, w, b, a, t) in enumerate(zip(shapes, wts, bias, acts, tiles)):
+                skip = acts[S.SKIP[l]] if l in S.SKIP else None
+                dp = d.ctypes.data_as(C.POINTER(C.c_int))
+                if tc:
+                    call("hps_nn_conv_forward_tiles", dp, ptr(cur), ptr(t), ptr(b), int(S.ARCH[l][4]),
+                         None if skip is None else ptr(skip), ptr(a), ptr(err), st)
+                else:
+                    call("hps_nn_conv_forward", dp, ptr(cur), ptr(w), ptr(b), int(S.ARCH[l][4]),
+                         None if skip is None else ptr(skip), ptr(a), st)
+                cur = a
+
+        for tc in (False, True):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(cs):
+                net(tc)  # untimed run outside the capture (kernel attributes, lazy loading)
+                with torch.cuda.graph(g, stream=cs):
+                    net(tc)
+            for _ in range(max(3, args.warmup)):
+                g.replay()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = max(args.steps, 20)
+            e0.record()
+            for _ in range(reps):
+                g.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            table[f"{'tensor' if tc else 'cuda'}_b{B}"] = e0.elapsed_time(e1) / reps
+        if int(err.item()):
+            raise SystemExit("surrogate_net: a tensor-core layer's pipeline wait timed out")
+    if rank != 0:
+        return
+    line = {"metric": "surrogate network forward time, batch 32, tensor-core layers", "value": table["tensor_b32"],
+            "unit": "ms", "n_gpus": 1, "steps": max(args.steps, 20), "warmup": args.warmup,
+            "ms_per_step": table["tensor_b32"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16", "data": "synthetic (random weights of the shipped architecture, random planes)",
+            "config": {"workload": "surrogate_net: ten 3x3 conv layers (32-64-128-128-128 down, 128-128-64-32 up, "
+                                   "2 out) on 128 x 32 planes, one CUDA graph per variant",
+                       "forward_ms": {k: round(v, 4) for k, v in table.items()}},
+            "e2e": None, "gpu_launches": 10}
+    print(json.dumps(line), flush=True)
+
+
 def run_batched(args):
     """Independent beams advanced by one graph launch per step; value = all
     beams' particle-element steps / step time.  batched: beams of uneven
@@ -687,6 +778,9 @@ def main():
         return
     if args.workload in ("batched", "ccl_batch"):
         run_batched(args)
+        return
+    if args.workload == "surrogate_net":
+        run_surrogate_net(args)
         return
     ws, rank, local = dist_env()
     import numpy as np
