@@ -298,7 +298,7 @@ inline int contract_slabs(uint32_t nz_max) { return sizeof(T) == 4 && nz_max >= 
 
 // the launch: the layout and slab count for the largest mesh the solver takes
 template <class T>
-inline void contract_m_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+inline void contract_m_merge(const std::vector<const Rec *> &recs, SegFork &, cudaStream_t st, cudaStream_t) {
   uint32_t dims[2];
   std::memcpy(dims, recs[0]->p.data() + sizeof(MeshSeg), sizeof(dims));
   const uint32_t nx_max = dims[0], nz_max = dims[1];

@@ -427,7 +427,7 @@ inline cudaError_t contract_tc_configure() {
   return e;
 }
 
-inline void contract_tc_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+inline void contract_tc_merge(const std::vector<const Rec *> &recs, SegFork &, cudaStream_t st, cudaStream_t) {
   uint32_t dims[2];
   std::memcpy(dims, recs[0]->p.data() + sizeof(MeshSeg), sizeof(dims));
   const uint32_t nr = dims[0], nz = dims[1];

@@ -27,13 +27,13 @@
 
 namespace hps {
 
-struct Arena;
+struct SegFork;
 
 // one recorded launch of one beam
 struct Rec {
   const char *site = nullptr;   // launch site: merged launches need equal sites
   // issue the merged launch of recs (one per beam, same site) on st
-  void (*merge)(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t main, cudaStream_t side) = nullptr;
+  void (*merge)(const std::vector<const Rec *> &recs, SegFork &a, cudaStream_t main, cudaStream_t side) = nullptr;
   uint32_t blocks = 0;          // this beam's grid blocks (flat launches)
   uint64_t shape = 0;           // launch shape every beam of a merged launch must share
   std::vector<unsigned char> p; // the launch's parameters (trivially copyable bytes)
@@ -50,7 +50,7 @@ struct Recorder {
 Recorder *&recorder();
 
 template <class P>
-inline void record(const char *site, void (*merge)(const std::vector<const Rec *> &, Arena &, cudaStream_t, cudaStream_t),
+inline void record(const char *site, void (*merge)(const std::vector<const Rec *> &, SegFork &, cudaStream_t, cudaStream_t),
                    uint32_t blocks, const P &p, uint64_t shape = 0) {
   Rec r;
   r.site = site;
@@ -62,9 +62,9 @@ inline void record(const char *site, void (*merge)(const std::vector<const Rec *
   recorder()->recs.push_back(std::move(r));
 }
 
-// The streams and events of one merged range: a side-stream branch forks
-// from the main stream and joins it again.
-struct Arena {
+// The events of a merged range's side-stream branch (the Green's tables):
+// it forks from the main stream and joins it again.
+struct SegFork {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 

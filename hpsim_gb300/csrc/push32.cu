@@ -271,13 +271,13 @@ __global__ void __launch_bounds__(kBlock) k32_kick_push_seg(const __grid_constan
   kick_push_body(p.b, p.sc, p.t, p.rk, p.skip_mask, p.m, p.sh, bid, nblk);
 }
 template <class Map>
-void push_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+void push_merge(const std::vector<const Rec *> &recs, SegFork &, cudaStream_t st, cudaStream_t) {
   seg_chunks<PushSeg<Map>>(recs, [&](const auto &a, uint32_t blocks) {
     k32_push_seg<Map, std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
   });
 }
 template <class Map>
-void kick_push_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+void kick_push_merge(const std::vector<const Rec *> &recs, SegFork &, cudaStream_t st, cudaStream_t) {
   seg_chunks<KickPushSeg<Map>>(recs, [&](const auto &a, uint32_t blocks) {
     k32_kick_push_seg<Map, std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
   });
@@ -346,7 +346,7 @@ __global__ void k32_aperture_seg(const __grid_constant__ SegArgs<AptArgs, B> a) 
   uint32_t bid, nblk;
   aperture_body(a.p[seg_find(a, blockIdx.x, bid, nblk)], bid, nblk);
 }
-void aperture_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+void aperture_merge(const std::vector<const Rec *> &recs, SegFork &, cudaStream_t st, cudaStream_t) {
   seg_chunks<AptArgs>(recs, [&](const auto &a, uint32_t blocks) {
     k32_aperture_seg<std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
   });

@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(kBlock) pass_kernel_f_seg(const __grid_constan
   pass_body_f(p.op, p.n, p.scr, bid, nblk);
 }
 template <class Op>
-inline void pass_merge(const std::vector<const Rec *> &recs, Arena &, cudaStream_t st, cudaStream_t) {
+inline void pass_merge(const std::vector<const Rec *> &recs, SegFork &, cudaStream_t st, cudaStream_t) {
   seg_chunks<PassSeg<Op>>(recs, [&](const auto &a, uint32_t blocks) {
     pass_kernel_f_seg<Op, std::decay_t<decltype(a)>::kB><<<blocks, kBlock, 0, st>>>(a);
   });

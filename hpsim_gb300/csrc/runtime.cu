@@ -174,7 +174,7 @@ struct hps_batch_s {
   cudaGraphExec_t ls_exec = nullptr;
   uint64_t ls_key = 0, ls_nodes = 0;
   std::vector<HostState> ls_after;   // every simulator's host state after the range
-  Arena arena;
+  SegFork segfork;              // the side-stream fork and join events of merged launches
 };
 
 // ---------------------------------------------------------------------------
@@ -1640,8 +1640,8 @@ hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *
   bt->sims = v;
   if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&bt->side, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&bt->arena.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&bt->arena.ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&bt->segfork.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&bt->segfork.ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&bt->ev0) != cudaSuccess || cudaEventCreate(&bt->ev1) != cudaSuccess) {
     hps_batch_destroy(bt);
     return fail(HPS_ERR_CUDA, "batch_create: stream or events");
@@ -1655,8 +1655,8 @@ hps_status hps_batch_destroy(hps_batch_t bt) {
   if (bt->stream) cudaStreamSynchronize(bt->stream);
   if (bt->exec) cudaGraphExecDestroy(bt->exec);
   if (bt->ls_exec) cudaGraphExecDestroy(bt->ls_exec);
-  if (bt->arena.ev_fork) cudaEventDestroy(bt->arena.ev_fork);
-  if (bt->arena.ev_join) cudaEventDestroy(bt->arena.ev_join);
+  if (bt->segfork.ev_fork) cudaEventDestroy(bt->segfork.ev_fork);
+  if (bt->segfork.ev_join) cudaEventDestroy(bt->segfork.ev_join);
   if (bt->side) cudaStreamDestroy(bt->side);
   if (bt->ev0) cudaEventDestroy(bt->ev0);
   if (bt->ev1) cudaEventDestroy(bt->ev1);
@@ -1751,7 +1751,7 @@ hps_status lockstep_prepare(hps_batch_t bt, std::vector<RunPlan> &plans, bool *r
   }
   std::vector<HostState> after(m);
   for (size_t k = 0; k < m; ++k) after[k] = host_get(bt->sims[k]);
-  Arena &a = bt->arena;
+  SegFork &a = bt->segfork;
   auto merge_all = [&]() {
     std::vector<const Rec *> v(m);
     for (size_t j = 0; j < recs[0].recs.size(); ++j) {

@@ -566,7 +566,7 @@ __global__ void __cluster_dims__(kDepCluster, 1, 1) __launch_bounds__(kDepBlockM
 }
 
 // the side-stream branch: fork, the Green's tables of every beam, join
-void green_merge(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t st, cudaStream_t side) {
+void green_merge(const std::vector<const Rec *> &recs, SegFork &a, cudaStream_t st, cudaStream_t side) {
   uint32_t blocks = 0;  // the table entries are independent of the block count
   for (const Rec *r : recs) blocks = std::max(blocks, r->blocks);
   cudaEventRecord(a.ev_fork, st);
@@ -577,7 +577,7 @@ void green_merge(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t st
   cudaEventRecord(a.ev_join, side);
 }
 // the deposit on the main stream, then the join of the Green's branch
-void deposit_merge(const std::vector<const Rec *> &recs, Arena &a, cudaStream_t st, cudaStream_t) {
+void deposit_merge(const std::vector<const Rec *> &recs, SegFork &a, cudaStream_t st, cudaStream_t) {
   size_t hb = 0;  // the largest histogram of the beams that deposit through shared memory
   for (const Rec *r : recs) {
     DepSeg d;
