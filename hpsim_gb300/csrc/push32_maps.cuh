@@ -146,6 +146,14 @@ struct Gap1Map {
   }
 };
 
+// sin and cos of a phase: reduced to [-pi, pi] by whole turns, then the
+// hardware approximation (absolute error about 2^-21 there, below the FP32
+// rounding of the phase offsets it is applied to)
+__device__ __forceinline__ void fast_sincos(float a, float *s, float *c) {
+  const float r = fmaf(-6.28318530717958647692f, rintf(a * 0.15915494309189533577f), a);
+  __sincosf(r, s, c);
+}
+
 // Bessi0c / Bessi1c (simulation_kernel.cu:15-73) in FP32; bessi0c also
 // returns I0 - 1 without cancellation
 __device__ inline float fbessi0c(float x, float *m1) {
@@ -240,14 +248,14 @@ struct Gap2Map {
     const float con5nex2 = -G.con2nex * t * G.inv_fkis;
     const float delta = G.ccl ? dphi - G.ccl_dg * D : dphi;
     float sd, cd;
-    sincosf(delta, &sd, &cd);
+    fast_sincos(delta, &sd, &cd);
     const float sinp1 = G.sinF * cd + G.cosF * sd, cosp1 = G.cosF * cd - G.sinF * sd;
     const float prome1 = -G.con1 * (tp * (sinp1 - G.sinps) + sp * (cosp1 - G.cosps));
     const float eps = delta + (prome1 - G.prome1_r);
     // sin and cos of eps from those of eps/2 (one evaluation instead of two;
     // 2 sin^2(eps/2) = 1 - cos(eps) is the form dcos needs anyway)
     float sh, ch;
-    sincosf(0.5f * eps, &sh, &ch);
+    fast_sincos(0.5f * eps, &sh, &ch);
     const float se = 2.0f * sh * ch, omc = 2.0f * sh * sh, ce = 1.0f - omc;
     const float sinp = G.sinP * ce + G.cosP * se, cosp = G.cosP * ce - G.sinP * se;
     const float dcos = -G.cosP * omc - G.sinP * se;
