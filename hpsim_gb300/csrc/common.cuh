@@ -146,9 +146,12 @@ __device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta, fl
   g = fmaf(dw, r.minv, r.g);
   const float gam = g + 1.0f;
   bg = sqrtf(g * (g + 2.0f));
-  beta = bg / gam;
+  // both quotients by the two-ulp reciprocal-multiply: the denominators are
+  // products of gamma, beta and beta gamma of live particles, far from zero
+  // and from overflow
+  beta = __fdividef(bg, gam);
   const float dg = dw * r.minv;
-  return -(dg * (gam + r.gam)) / (gam * r.gam * r.gam * (beta + r.beta) * bg * r.beta);
+  return -__fdividef(dg * (gam + r.gam), gam * r.gam * r.gam * (beta + r.beta) * bg * r.beta);
 }
 __device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta) {
   float bg;
