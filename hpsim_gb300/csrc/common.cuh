@@ -142,10 +142,18 @@ __host__ __device__ inline RefK make_refk(double w, double mass) {
 //   1/beta_i - 1/beta_r = -(dgamma (gamma_i + gamma_r)) /
 //                          (gamma_i gamma_r^2 (beta_i + beta_r) (beta gamma)_i beta_r)
 // (one division); also returns g_i = W_i/m, beta_i and (beta gamma)_i.
+// square root by the hardware approximation (sqrt.approx.f32: within about
+// an ulp; +0 -> +0, negative -> NaN), for the per-particle sweeps
+__device__ __forceinline__ float sqrt_fast(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 __device__ inline float dinvb(float dw, const RefK &r, float &g, float &beta, float &bg) {
   g = fmaf(dw, r.minv, r.g);
   const float gam = g + 1.0f;
-  bg = sqrtf(g * (g + 2.0f));
+  bg = sqrt_fast(g * (g + 2.0f));
   // both quotients by the two-ulp reciprocal-multiply: the denominators are
   // products of gamma, beta and beta gamma of live particles, far from zero
   // and from overflow

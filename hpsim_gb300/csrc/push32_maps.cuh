@@ -82,7 +82,7 @@ struct QuadMap {
       return m | WR_PH;
     } else {
       const float g = fmaf(p.w, r.minv, r.g);
-      const float bg = sqrtf(g * (g + 2.0f) * (1.0f + xp * xp + yp * yp));
+      const float bg = sqrt_fast(g * (g + 2.0f) * (1.0f + xp * xp + yp * yp));
       const float rb = rsqrtf(bg);
       const float k = sk0 * rb;              // sqrt(kcoef / bg)
       const float inv_k = bg * rb * isk0;    // sqrt(bg / kcoef)
@@ -260,7 +260,7 @@ struct Gap2Map {
     const float sinp = G.sinP * ce + G.cosP * se, cosp = G.cosP * ce - G.sinP * se;
     const float dcos = -G.cosP * omc - G.sinP * se;
     const float rs_p = x * x + y * y, rrp = x * xp + y * yp;
-    const float ris = sqrtf(rs_p), fkrris = G.fkr * ris;
+    const float ris = sqrt_fast(rs_p), fkrris = G.fkr * ris;
     float b0m1;
     const float b0c = fbessi0c(fkrris, &b0m1);
     const float b1c = fbessi1c(fkrris);

@@ -60,12 +60,12 @@ __device__ inline uint32_t kick_particle(Part &p, float phi, const KickEnv &e) {
   const float dw = p.w;
   const float g = fmaf(dw, e.r.minv, e.r.g);
   const float gm = g + 1.0f;
-  const float bgz = sqrtf(g * (g + 2.0f));
+  const float bgz = sqrt_fast(g * (g + 2.0f));
   float bgx = bgz * p.xp, bgy = bgz * p.yp;
   const float dgc = (dw + e.dwc) * e.r.minv;  // gm - gamma_c
   const float s0 = __fdividef(dgc * (gm + e.gmg), e.gmg * (bgz + e.beta * gm));
   const float xxbar = p.x - e.xbar, yybar = p.y - e.ybar;
-  float rr = sqrtf(xxbar * xxbar * e.inv_epsq + yybar * yybar * e.epsq);
+  float rr = sqrt_fast(xxbar * xxbar * e.inv_epsq + yybar * yybar * e.epsq);
   if (rr == 0.0f) rr = 1.0e-8f;
   const float inv_rr = __fdividef(1.0f, rr);
   const float xovr = xxbar * e.xfac * inv_rr, yovr = yybar * e.yfac * inv_rr;

@@ -416,7 +416,7 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
     const float pz = rel_phase_f(in.ph - pag);
     const float dx = in.x - xbar, dy = in.y - ybar;
     const float rsq_sh = dx * dx * inv_epsq + dy * dy * epsq;
-    const int i = (int)(sqrtf(rsq_sh) * inv_dr + 1.0f);
+    const int i = (int)(sqrt_fast(rsq_sh) * inv_dr + 1.0f);
     const float z = -c2 * wrap_turns(pz - phimc);
     if (!(i >= 1 && (uint32_t)i <= nx)) return false;
     if (!(fabsf(z) < hl)) return false;
@@ -433,7 +433,7 @@ __device__ void deposit_blocks(const DevBeam &bm, ScState *sc, const ScTables &t
     // z weight with (jm1 - j1) dz = +-dz
     float a = 1.0f;
     if (i1 != i) {
-      const float sqrtmp = sqrtf(4.0f * rsq_sh * inv_drdr - 1.0f);
+      const float sqrtmp = sqrt_fast(4.0f * rsq_sh * inv_drdr - 1.0f);
       const float rmin_n = 0.25f * (sqrtmp - 1.0f) * (sqrtmp - 1.0f);
       const float rmax_n = rmin_n + sqrtmp;
       if (i1 < i) a = __fdividef(rmax_n - (float)((i - 1) * (i - 1)), sqrtmp);
