@@ -55,7 +55,8 @@ __device__ inline float wrap_turns(float d) {
 // kick particle p (live, not longitudinally lost) whose relative phase is
 // phi; returns the fields changed.  Quotients whose denominators are
 // bounded away from zero and overflow use the two-ulp reciprocal-multiply
-// (__fdividef).
+// (__fdividef), the square roots of the common path the hardware
+// approximation (sqrt_fast).
 __device__ inline uint32_t kick_particle(Part &p, float phi, const KickEnv &e) {
   const float dw = p.w;
   const float g = fmaf(dw, e.r.minv, e.r.g);
@@ -114,7 +115,7 @@ __device__ inline uint32_t kick_particle(Part &p, float phi, const KickEnv &e) {
   // comes straight from the particle's energy
   const float s2 = s0 * s0;
   const float dbgz = e.gmg * (cbgzs + e.beta * (0.5f * cbgzs * (2.0f * s0 + cbgzs) +
-                                                __fdividef(s2 * s2, 4.0f * (1.0f + 0.5f * s2 + sqrtf(1.0f + s2)))));
+                                                __fdividef(s2 * s2, 4.0f * (1.0f + 0.5f * s2 + sqrt_fast(1.0f + s2)))));
   const float bgzf = bgz + dbgz;
   if (bgzf <= 0.0f) {
     p.lo = 9999u;
