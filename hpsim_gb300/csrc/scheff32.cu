@@ -379,7 +379,10 @@ constexpr int kDepCluster = 8;
 // deposit threads per block: 256, 512 or 1024 (a launch-shape choice; the
 // kernels take up to 1024, at most 64 registers a thread)
 constexpr int kDepBlockMax = 1024;
-constexpr int kDepBatch = 4;  // particles a thread loads before it deposits them
+// particles a thread loads before it deposits them.  Measured on the whole
+// step: 2 (51 registers) ties 4 on 1M-particle beams but is 3.5% slower on a
+// 16M-particle beam (fewer loads in flight); 8 is 3% slower on 1M particles
+constexpr int kDepBatch = 4;
 
 struct DepIn {
   uint32_t lo, ll;
