@@ -105,17 +105,22 @@ struct hps_scheff_s {
   int contraction = 0;    // FP32 beams: 0 tensor cores where the mesh allows, 1 CUDA cores
 };
 
+// The host-side state of a simulator that a range advances (engine, beam
+// and solver fields; phi_ref and w_ref are an FP32 beam's synchronous
+// particle): a captured range stores it as it is at the range's end, and a
+// lockstep recording saves and puts it back.
+struct HostState {
+  double design_w, wavelen, beam_freq, beam_current, beam_design_w, phi_ref, w_ref, fraction, interval;
+  uint32_t ccl_cell_num, cur_id;
+};
+
 struct GraphEntry {
   uint64_t key = 0;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;  // the captured graph, kept for batches
   uint64_t serial = 0;          // bumped at every capture
-  // host state after the range
-  double design_w, wavelen, beam_freq, beam_current, beam_design_w, fraction, interval;
-  double phi_ref, w_ref;  // synchronous particle of an FP32 beam
-  uint32_t ccl_cell_num, cur_id;
-  int prev_end;
-  uint64_t nkernels = 0;  // kernels in the captured graph
+  HostState after{};            // host state after the range
+  uint64_t nkernels = 0;        // kernels in the captured graph
 };
 
 struct hps_sim_s {
@@ -152,12 +157,6 @@ struct hps_sim_s {
 
 // Many simulators run as one graph launch: each simulator's captured range
 // is a child graph of one parent graph, with no edges between them.
-// The host-side state of a simulator that a range advances (engine, beam
-// and solver fields), saved and put back around a lockstep recording.
-struct HostState {
-  double design_w, wavelen, beam_freq, beam_current, beam_design_w, phi_ref, w_ref, fraction, interval;
-  uint32_t ccl_cell_num, cur_id;
-};
 
 struct hps_batch_s {
   std::vector<hps_sim_t> sims;
@@ -1426,6 +1425,24 @@ hps_status plan_run(hps_sim_t s, int32_t start, int32_t end, RunPlan *p) {
   return HPS_OK;
 }
 
+HostState host_get(hps_sim_t s) {
+  HostState h;
+  hps_beam_t b = s->beam;
+  h.design_w = s->design_w; h.wavelen = s->wavelen; h.ccl_cell_num = s->ccl_cell_num; h.cur_id = s->cur_id;
+  h.beam_freq = b->freq; h.beam_current = b->current; h.beam_design_w = b->design_w;
+  h.phi_ref = b->d.phi_ref; h.w_ref = b->d.w_ref;
+  h.fraction = s->sc ? s->sc->fraction : 0.0;
+  h.interval = s->sc ? s->sc->interval : 0.0;
+  return h;
+}
+void host_put(hps_sim_t s, const HostState &h) {
+  hps_beam_t b = s->beam;
+  s->design_w = h.design_w; s->wavelen = h.wavelen; s->ccl_cell_num = h.ccl_cell_num; s->cur_id = h.cur_id;
+  b->freq = h.beam_freq; b->current = h.beam_current; b->design_w = h.beam_design_w;
+  b->d.phi_ref = h.phi_ref; b->d.w_ref = h.w_ref;
+  if (s->sc) { s->sc->fraction = h.fraction; s->sc->interval = h.interval; }
+}
+
 // The simulator's graph for the plan: the cached one when the host state
 // matches (the host state then moves to the end of the range, as a replay
 // does), else a new capture (which moves it while recording).  The graph is
@@ -1437,34 +1454,38 @@ hps_status prepare_graph(RunPlan &p) {
   cudaStream_t st = b->stream;
   GraphEntry &g = s->graph;
   if (g.exec && g.key == p.key) {
-    s->design_w = g.design_w; s->wavelen = g.wavelen; s->ccl_cell_num = g.ccl_cell_num; s->cur_id = g.cur_id;
-    b->freq = g.beam_freq; b->current = g.beam_current; b->design_w = g.beam_design_w;
-    b->d.phi_ref = g.phi_ref; b->d.w_ref = g.w_ref;
-    if (c.sc) { c.sc->fraction = g.fraction; c.sc->interval = g.interval; }
+    host_put(s, g.after);
     note_launch((int)g.nkernels);  // a replay launches the captured kernels again
     return HPS_OK;
   }
-  cudaGraph_t gr;
+  // a capture that fails leaves the host state as it was before the range
+  const HostState before = host_get(s);
+  cudaGraph_t gr = nullptr;
   uint64_t launches0 = g_launches.load();
-  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
   hps_status e = run_range(c, p.start_index, p.end_index, p.monitor);
   g.nkernels = g_launches.load() - launches0;
-  cudaError_t ce = cudaStreamEndCapture(st, &gr);
-  if (e) { if (ce == cudaSuccess) cudaGraphDestroy(gr); return e; }
-  if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+  ce = cudaStreamEndCapture(st, &gr);
+  if (e || ce != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    host_put(s, before);
+    return e ? e : fail(HPS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+  }
   if (g.exec) cudaGraphExecDestroy(g.exec);
   if (g.graph) cudaGraphDestroy(g.graph);
   g.exec = nullptr;
   g.graph = gr;
   g.serial++;
+  g.key = 0;
   cudaError_t ie = cudaGraphInstantiate(&g.exec, gr, 0);
-  if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+  if (ie != cudaSuccess) {
+    g.exec = nullptr;
+    host_put(s, before);
+    return fail(HPS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+  }
   g.key = p.key;
-  g.design_w = s->design_w; g.wavelen = s->wavelen; g.ccl_cell_num = s->ccl_cell_num; g.cur_id = s->cur_id;
-  g.beam_freq = b->freq; g.beam_current = b->current; g.beam_design_w = b->design_w;
-  g.phi_ref = b->d.phi_ref; g.w_ref = b->d.w_ref;
-  g.fraction = c.sc ? c.sc->fraction : 0.0;
-  g.interval = c.sc ? c.sc->interval : 0.0;
+  g.after = host_get(s);
   return HPS_OK;
 }
 
@@ -1665,30 +1686,9 @@ hps_status hps_batch_destroy(hps_batch_t bt) {
   return HPS_OK;
 }
 
-// Simulator::Simulate(start, end) on every simulator of the batch in one
-// graph launch.  Each simulator must be able to run as a graph (graphs on,
-// profiling off, no mesh-size cut-off energy).
 }  // extern "C"
 
 namespace {
-
-HostState host_get(hps_sim_t s) {
-  HostState h;
-  hps_beam_t b = s->beam;
-  h.design_w = s->design_w; h.wavelen = s->wavelen; h.ccl_cell_num = s->ccl_cell_num; h.cur_id = s->cur_id;
-  h.beam_freq = b->freq; h.beam_current = b->current; h.beam_design_w = b->design_w;
-  h.phi_ref = b->d.phi_ref; h.w_ref = b->d.w_ref;
-  h.fraction = s->sc ? s->sc->fraction : 0.0;
-  h.interval = s->sc ? s->sc->interval : 0.0;
-  return h;
-}
-void host_put(hps_sim_t s, const HostState &h) {
-  hps_beam_t b = s->beam;
-  s->design_w = h.design_w; s->wavelen = h.wavelen; s->ccl_cell_num = h.ccl_cell_num; s->cur_id = h.cur_id;
-  b->freq = h.beam_freq; b->current = h.beam_current; b->design_w = h.beam_design_w;
-  b->d.phi_ref = h.phi_ref; b->d.w_ref = h.w_ref;
-  if (s->sc) { s->sc->fraction = h.fraction; s->sc->interval = h.interval; }
-}
 
 // The batch's range in lockstep (lockstep.cuh): the cached graph when every
 // simulator's plan matches, else each simulator's range recorded (its launches
@@ -1759,17 +1759,27 @@ hps_status lockstep_prepare(hps_batch_t bt, std::vector<RunPlan> &plans, bool *r
       v[0]->merge(v, a, bt->stream, bt->side);
     }
   };
+  // nothing runs when the merged graph cannot be built: the simulators keep
+  // the host state they had before the range
+  auto undo = [&](const char *what, cudaError_t err) {
+    for (size_t k = 0; k < m; ++k) host_put(bt->sims[k], before[k]);
+    return fail(HPS_ERR_CUDA, std::string(what) + cudaGetErrorString(err));
+  };
   cudaGraph_t gr = nullptr;
-  CK(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t be = cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal);
+  if (be != cudaSuccess) return undo("lockstep capture: ", be);
   merge_all();
   const cudaError_t ce = cudaStreamEndCapture(bt->stream, &gr);
-  if (ce != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("lockstep capture: ") + cudaGetErrorString(ce));
+  if (ce != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    return undo("lockstep capture: ", ce);
+  }
   size_t nodes = 0;
   cudaGraphGetNodes(gr, nullptr, &nodes);
   cudaGraphExec_t ex = nullptr;
   const cudaError_t ie = cudaGraphInstantiate(&ex, gr, 0);
   cudaGraphDestroy(gr);
-  if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("lockstep instantiate: ") + cudaGetErrorString(ie));
+  if (ie != cudaSuccess) return undo("lockstep instantiate: ", ie);
   if (bt->ls_exec) cudaGraphExecDestroy(bt->ls_exec);
   bt->ls_exec = ex;
   bt->ls_key = key;
@@ -1800,6 +1810,11 @@ hps_status hps_batch_last_mode(hps_batch_t bt, int *lockstep, char *why, size_t 
   return HPS_OK;
 }
 
+// Simulator::Simulate(start, end) on every simulator of the batch in one
+// graph launch: the lockstep graph when the batch is in lockstep and its
+// launches merge, else a parent graph of the simulators' captured ranges.
+// Each simulator must be able to run as a graph (graphs on, profiling off,
+// no mesh-size cut-off energy).
 hps_status hps_batch_simulate(hps_batch_t bt, int32_t start, int32_t end) {
   if (!bt) return fail(HPS_ERR_INVALID, "bad batch handle");
   const size_t m = bt->sims.size();
@@ -1837,30 +1852,42 @@ hps_status hps_batch_simulate(hps_batch_t bt, int32_t start, int32_t end) {
       return HPS_OK;
     }
   }
+  // nothing runs when the batch graph cannot be built: every simulator
+  // keeps the host state it had before the range
+  std::vector<HostState> before(m);
+  for (size_t k = 0; k < m; ++k) before[k] = host_get(bt->sims[k]);
+  auto undo = [&](hps_status e) {
+    for (size_t k = 0; k < m; ++k) host_put(bt->sims[k], before[k]);
+    return e;
+  };
   std::vector<uint64_t> serials(m, 0);
   for (size_t k = 0; k < m; ++k) {
     if (plans[k].empty) continue;
     hps_status e = prepare_graph(plans[k]);
-    if (e) return e;
+    if (e) return undo(e);
     serials[k] = bt->sims[k]->graph.serial;
   }
   if (!bt->exec || serials != bt->serials) {
     if (bt->exec) cudaGraphExecDestroy(bt->exec);
     bt->exec = nullptr;
     cudaGraph_t parent;
-    CK(cudaGraphCreate(&parent, 0));
+    const cudaError_t ge = cudaGraphCreate(&parent, 0);
+    if (ge != cudaSuccess) return undo(fail(HPS_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ge)));
     for (size_t k = 0; k < m; ++k) {
       if (plans[k].empty) continue;
       cudaGraphNode_t node;
       cudaError_t ce = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, bt->sims[k]->graph.graph);
       if (ce != cudaSuccess) {
         cudaGraphDestroy(parent);
-        return fail(HPS_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ce));
+        return undo(fail(HPS_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ce)));
       }
     }
     cudaError_t ie = cudaGraphInstantiate(&bt->exec, parent, 0);
     cudaGraphDestroy(parent);
-    if (ie != cudaSuccess) return fail(HPS_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(ie));
+    if (ie != cudaSuccess) {
+      bt->exec = nullptr;
+      return undo(fail(HPS_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(ie)));
+    }
     bt->serials = serials;
   }
   CK(cudaEventRecord(bt->ev0, bt->stream));
