@@ -95,6 +95,7 @@ struct SegArgs {
 // args a SegArgs<P, 4 | 16 | SegCap<P>> and blocks the chunk's flat grid.
 template <class P, int B, class F>
 inline void seg_chunk(const std::vector<const Rec *> &recs, size_t k0, size_t k1, F &f) {
+  static_assert(sizeof(SegArgs<P, B>) <= 32764, "a merged launch's parameters exceed the kernel parameter limit");
   std::vector<unsigned char> buf(sizeof(SegArgs<P, B>), 0);  // up to 32 KB: not on the stack
   SegArgs<P, B> &a = *reinterpret_cast<SegArgs<P, B> *>(buf.data());
   a.nb = (uint32_t)(k1 - k0);
@@ -119,11 +120,15 @@ inline void seg_chunks(const std::vector<const Rec *> &recs, F &&f) {
 }
 
 #ifdef __CUDACC__
+#define HPS_SEG_FN __host__ __device__ __forceinline__
+#else
+#define HPS_SEG_FN inline
+#endif
 // the beam of flat block blk, its block index within the beam and the beam's
 // block count (uniform over the block: a binary search of the constant-bank
 // table with the block index)
 template <class P, int B>
-__device__ __forceinline__ uint32_t seg_find(const SegArgs<P, B> &a, uint32_t blk, uint32_t &bid, uint32_t &nblk) {
+HPS_SEG_FN uint32_t seg_find(const SegArgs<P, B> &a, uint32_t blk, uint32_t &bid, uint32_t &nblk) {
   uint32_t lo = 0, hi = a.nb;  // first[lo] <= blk < first[hi]
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
@@ -134,6 +139,6 @@ __device__ __forceinline__ uint32_t seg_find(const SegArgs<P, B> &a, uint32_t bl
   nblk = a.first[lo + 1] - a.first[lo];
   return lo;
 }
-#endif
+#undef HPS_SEG_FN
 
 }  // namespace hps
