@@ -1,8 +1,8 @@
 /*
  * hps_oracle.h -- FP64 CPU restatement of HPSim's per-element tracking path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
- * implementation in hpsim_gb300/: it is loaded by tests/, by
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the CUDA
+ * implementation in hpsim_gb300/ is tested against: it is loaded by tests/, by
  * __graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by the
  * product.  Every routine cites the reference file:line it restates.
  *

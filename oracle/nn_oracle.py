@@ -1,6 +1,6 @@
 """Test infrastructure: numpy restatement (FP64 arithmetic) of the field
-surrogate's layers (hpsim_gb300/csrc/nn.cu) -- the checker of their forward
-values and gradients.  Never used by the library.
+surrogate's layers (hpsim_gb300/csrc/nn.cu) -- the oracle their forward
+values and gradients are tested against.  Never used by the library.
 
 Layouts as the kernels: tensors [batch][channel][z][r], weights
 [c_out][c_in][3][3]; a layer upsamples its input by `up` (nearest), pads by

@@ -1,11 +1,11 @@
 """Test infrastructure: numpy restatement of the reference's plot-data
-kernels (src/graphics/inc/graphics_kernel.cu), the checker for
+kernels (src/graphics/inc/graphics_kernel.cu), the oracle for
 hpsim_gb300's headless plot kernels (csrc/plot.cu).  Never used by the
 library.
 
 Parity of this restatement is pinned to the kernels' source, not to runs of
-them: their only caller is the reference's OpenGL online mode (unavailable
-on this machine), and a host build of the kernels would change the
+them: their only caller is the reference's OpenGL online mode (it needs a
+graphics stack, which this project does not use), and a host build of the kernels would change the
 float-to-unsigned conversion they rely on (the GPU's saturates; a host
 conversion of a negative float is undefined).
 """
