@@ -186,7 +186,12 @@ hps_status hps_beamline_set_param(hps_beamline_t bl, uint32_t index, int slot, d
 
 /* ---- SCHEFF (src/simulation/inc/space_charge.h) ------------------------- */
 /* Scheff(nr, nz, adj_bunch), space_charge.cpp:31-40.  nr and nz must be
- * powers of two, nz <= 512 (the reference's launch geometry requires it). */
+ * powers of two, nz <= 512 (the reference's launch geometry requires it).
+ * The charge table holds signed 64-bit integers in units of 2^-36 of a
+ * particle (exact and order-independent), so one bin holds the charge of
+ * fewer than 2^27 particles: beams of fewer than 2^27 (134,217,728)
+ * particles cannot overflow it; a larger beam overflows only if 2^27 of
+ * its particles fall into one bin. */
 hps_status hps_scheff_create(uint32_t nr, uint32_t nz, uint32_t adj_bunch, hps_scheff_t *out);
 hps_status hps_scheff_destroy(hps_scheff_t s);
 /* parameter: 0 interval, 1 adj_bunch, 2 adj_bunch_cutoff_w, 3 mesh_size_cutoff_w,
