@@ -182,6 +182,10 @@ __host__ __device__ inline uint32_t next_pow2(uint32_t x) {
   return ++x;
 }
 
+// particles a beam may hold: next_pow2 of the count and the sweeps'
+// 32-bit particle indices (index + grid stride) stay in range
+constexpr uint32_t kMaxParticles = 1u << 31;
+
 // Beam::SetNumThreadsPerBlock, src/beam/src/beam.cpp:148-168
 __host__ __device__ inline void ref_launch(uint32_t n, uint32_t *grid, uint32_t *blck) {
   uint32_t nt = next_pow2(n);

@@ -290,6 +290,10 @@ hps_status hps_beam_create(uint32_t num, double mass, double charge, double curr
   *out = nullptr;
   if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32)
     return fail(HPS_ERR_UNSUPPORTED, "hps_beam_create: unknown precision");
+  // the reference's launch geometry (next power of two of the count,
+  // beam.cpp:148-168) and the 32-bit particle indices of the sweeps hold
+  // up to 2^31 particles
+  if (num > kMaxParticles) return fail(HPS_ERR_INVALID, "hps_beam_create: a beam holds at most 2^31 particles");
   hps_beam_t b = new hps_beam_s();
   b->n = num; b->mass = mass; b->charge = charge; b->current = current; b->prec = precision;
   ref_launch(num, &b->grid_size, &b->blck_size);

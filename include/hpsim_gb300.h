@@ -71,7 +71,9 @@ hps_status hps_set_gpu(int device);
 uint64_t hps_kernel_launch_count(void);
 
 /* ---- Beam (src/beam/inc/beam.h:35-312) ---------------------------------- */
-/* Beam(num, mass, charge, current): beam.cpp:69-75 + AllocateBeam :124-134 */
+/* Beam(num, mass, charge, current): beam.cpp:69-75 + AllocateBeam :124-134.
+ * num <= 2^31 (HPS_ERR_INVALID above: the reference's launch geometry, the
+ * next power of two of num, and 32-bit particle indices). */
 hps_status hps_beam_create(uint32_t num, double mass, double charge, double current,
                            int precision, hps_beam_t *out);
 hps_status hps_beam_destroy(hps_beam_t beam);

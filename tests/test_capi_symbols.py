@@ -75,3 +75,15 @@ def test_invalid_handles_are_rejected(capi):
     assert lib.hps_beam_get_coord(None, 0, None) == 1
     bad = C.c_void_p()
     assert lib.hps_scheff_create(48, 128, 0, C.byref(bad)) == 1  # not a power of two
+
+
+def test_beam_particle_count_limit(capi):
+    """A beam holds at most 2^31 particles (the reference's next-power-of-two
+    launch geometry and 32-bit particle indices); the check runs before any
+    device work."""
+    lib = capi.lib()
+    out = C.c_void_p()
+    for prec in (0, 1):
+        assert lib.hps_beam_create((1 << 31) + 1, 939.294, -1.0, 0.0, prec, C.byref(out)) == 1
+        assert not out.value
+        assert b"2^31" in lib.hps_last_error()
