@@ -65,6 +65,7 @@ using namespace hps;
 // ---------------------------------------------------------------------------
 struct hps_beam_s {
   uint32_t n = 0;
+  int dev = -1;  // the device its memory lives on
   int prec = HPS_PREC_FP64;
   double mass = 0, charge = 0, current = 0, freq = 0, design_w = 0;
   uint32_t grid_size = 1, blck_size = 1;
@@ -92,6 +93,7 @@ struct hps_beamline_s {
 };
 
 struct hps_scheff_s {
+  int dev = -1;  // the device its memory lives on
   // host mirror of SpaceCharge's members (space_charge.h:88-125)
   uint32_t nx, nz, nx_init, nz_init, adj_bunch;
   double fraction = 1.0, interval = 0.01, interval_init = 0.01, adj_bunch_w = 0.0, mesh_w = 0.0,
@@ -182,6 +184,23 @@ struct hps_batch_s {
 namespace {
 
 bool valid(hps_beam_t b) { return b != nullptr && b->d.loss != nullptr; }
+// An object's kernels and copies run on the calling thread's current
+// device, which must be the one its memory was allocated on (set_gpu
+// selects it): a call from another device is refused.
+hps_status device_check(int dev, const char *what) {
+  int cur = -1;
+  const cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return fail(HPS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  if (dev >= 0 && cur != dev)
+    return fail(HPS_ERR_STATE, std::string(what) + ": the object lives on device " + std::to_string(dev) +
+                                   ", the current device is " + std::to_string(cur) + " (call set_gpu first)");
+  return HPS_OK;
+}
+#define ON_DEVICE(obj, what)                          \
+  do {                                                \
+    const hps_status dev_e_ = device_check((obj)->dev, what); \
+    if (dev_e_) return dev_e_;                        \
+  } while (0)
 bool f32(hps_beam_t b) { return b->prec == HPS_PREC_FP32; }
 size_t esize(hps_beam_t b) { return f32(b) ? sizeof(float) : sizeof(double); }
 // the six coordinate arrays of the beam's own precision
@@ -296,6 +315,7 @@ hps_status hps_beam_create(uint32_t num, double mass, double charge, double curr
   if (num > kMaxParticles) return fail(HPS_ERR_INVALID, "hps_beam_create: a beam holds at most 2^31 particles");
   hps_beam_t b = new hps_beam_s();
   b->n = num; b->mass = mass; b->charge = charge; b->current = current; b->prec = precision;
+  cudaGetDevice(&b->dev);
   ref_launch(num, &b->grid_size, &b->blck_size);
   hps_status s = HPS_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
@@ -359,6 +379,7 @@ hps_status hps_beam_set_distribution(hps_beam_t b, const double *x, const double
                                      const double *yp, const double *phi, const double *w,
                                      const uint32_t *loss, const uint32_t *lloss) {
   if (!valid(b) || !x || !xp || !y || !yp || !phi || !w) return fail(HPS_ERR_INVALID, "set_distribution: null array");
+  ON_DEVICE(b, __func__);
   hps_status s = upload(b, x, xp, y, yp, phi, w, loss, lloss);
   if (s) return s;
   // the reference particle sits on axis (beam.cpp:344-358)
@@ -379,6 +400,7 @@ hps_status hps_beam_set_distribution(hps_beam_t b, const double *x, const double
 hps_status hps_beam_set_waterbag(hps_beam_t b, const double t[9], double r_sync_phi, double r_sync_w,
                                  double r_freq, uint32_t r_seed) {
   if (!valid(b) || !t) return fail(HPS_ERR_INVALID, "set_waterbag: bad argument");
+  ON_DEVICE(b, __func__);
   uint32_t n = b->n;
   std::vector<double> xh(n), xph(n), yh(n), yph(n), phih(n), wh(n);
   if (r_seed == 0) std::srand((unsigned)std::time(nullptr));
@@ -424,6 +446,7 @@ hps_status hps_beam_set_waterbag(hps_beam_t b, const double t[9], double r_sync_
 hps_status hps_beam_set_dc(hps_beam_t b, const double t[6], double r_dphi, double r_sync_phi,
                            double r_sync_w, uint32_t r_seed) {
   if (!valid(b) || !t) return fail(HPS_ERR_INVALID, "set_dc: bad argument");
+  ON_DEVICE(b, __func__);
   uint32_t n = b->n;
   std::vector<double> xh(n), xph(n), yh(n), yph(n), phih(n), wh(n);
   if (r_seed == 0) std::srand((unsigned)std::time(nullptr));
@@ -460,6 +483,7 @@ hps_status hps_beam_set_dc(hps_beam_t b, const double t[6], double r_dphi, doubl
 
 hps_status hps_beam_get_coord(hps_beam_t b, int coord, double *out) {
   if (!valid(b) || !out || coord < 0 || coord > HPS_COORD_PHI_R) return fail(HPS_ERR_INVALID, "get_coord: bad argument");
+  ON_DEVICE(b, __func__);
   if (f32(b)) {
     hps_status e = stage_alloc(b);
     if (e) return e;
@@ -473,6 +497,7 @@ hps_status hps_beam_get_coord(hps_beam_t b, int coord, double *out) {
 
 hps_status hps_beam_get_loss(hps_beam_t b, int longitudinal, uint32_t *out) {
   if (!valid(b) || !out) return fail(HPS_ERR_INVALID, "get_loss: bad argument");
+  ON_DEVICE(b, __func__);
   CK(cudaMemcpyAsync(out, longitudinal ? b->d.lloss : b->d.loss, (size_t)b->n * 4, cudaMemcpyDeviceToHost,
                      b->stream));
   return sync(b);
@@ -480,6 +505,7 @@ hps_status hps_beam_get_loss(hps_beam_t b, int longitudinal, uint32_t *out) {
 
 hps_status hps_beam_save(hps_beam_t b, int slot) {
   if (!valid(b) || slot < 0 || slot > 1) return fail(HPS_ERR_INVALID, "save: bad argument");
+  ON_DEVICE(b, __func__);
   size_t nd = (size_t)b->n * esize(b), nu = (size_t)b->n * 4;
   hps_status s;
   for (int k = 0; k < 6; ++k) {
@@ -507,6 +533,7 @@ hps_status hps_beam_save(hps_beam_t b, int slot) {
 // UpdateRelativePhi(true)
 hps_status hps_beam_restore(hps_beam_t b, int slot) {
   if (!valid(b) || slot < 0 || slot > 1) return fail(HPS_ERR_INVALID, "restore: bad argument");
+  ON_DEVICE(b, __func__);
   if (!b->saved[slot]) return fail(HPS_ERR_STATE, "restore: no beam has been saved in this slot");
   size_t nd = (size_t)b->n * esize(b), nu = (size_t)b->n * 4;
   for (int k = 0; k < 6; ++k)
@@ -532,6 +559,7 @@ hps_status hps_beam_restore(hps_beam_t b, int slot) {
 
 hps_status hps_beam_set_ref_w(hps_beam_t b, double w) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  ON_DEVICE(b, __func__);
   if (f32(b)) beam32_set_ref(b->d, HPS_COORD_W, w, b->stream);
   else beam_set_ref(b->d, HPS_COORD_W, w, b->stream);
   b->design_w = w;
@@ -539,12 +567,14 @@ hps_status hps_beam_set_ref_w(hps_beam_t b, double w) {
 }
 hps_status hps_beam_set_ref_phi(hps_beam_t b, double phi) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  ON_DEVICE(b, __func__);
   if (f32(b)) beam32_set_ref(b->d, HPS_COORD_PHI, phi, b->stream);
   else beam_set_ref(b->d, HPS_COORD_PHI, phi, b->stream);
   return sync(b);
 }
 hps_status hps_beam_get_ref(hps_beam_t b, double *w, double *phi) {
   if (!valid(b) || b->n == 0) return fail(HPS_ERR_INVALID, "bad beam handle");
+  ON_DEVICE(b, __func__);
   if (f32(b)) {
     float fw = 0.f, fp = 0.f;
     CK(cudaMemcpyAsync(&fw, b->d.fw, 4, cudaMemcpyDeviceToHost, b->stream));
@@ -579,6 +609,7 @@ hps_status hps_beam_get_scalar(hps_beam_t b, int which, double *out) {
 
 hps_status hps_beam_update(hps_beam_t b, int op, int coord, int good) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  ON_DEVICE(b, __func__);
   const DevBeam &d = b->d;
   if ((op == 3 || op == 4) && (coord < 0 || coord > HPS_COORD_PHI_R))
     return fail(HPS_ERR_INVALID, "beam_update: bad coordinate");
@@ -606,6 +637,7 @@ hps_status hps_beam_update(hps_beam_t b, int op, int coord, int good) {
 
 hps_status hps_beam_get_stat(hps_beam_t b, int stat, double *out) {
   if (!valid(b) || !out || stat < 0 || stat >= HPS_NST) return fail(HPS_ERR_INVALID, "get_stat: bad argument");
+  ON_DEVICE(b, __func__);
   BeamStats h;
   CK(cudaMemcpyAsync(&h, b->d.st, sizeof(h), cudaMemcpyDeviceToHost, b->stream));
   hps_status s = sync(b);
@@ -619,6 +651,7 @@ hps_status hps_beam_get_stat(hps_beam_t b, int stat, double *out) {
 
 hps_status hps_beam_apply_cut(hps_beam_t b, char coord, double lo, double hi) {
   if (!valid(b)) return fail(HPS_ERR_INVALID, "bad beam handle");
+  ON_DEVICE(b, __func__);
   char c = (char)std::tolower((unsigned char)coord);
   int k = c == 'x' ? HPS_COORD_X : c == 'y' ? HPS_COORD_Y : c == 'w' ? HPS_COORD_W : c == 'p' ? HPS_COORD_PHI : -1;
   if (k < 0) return HPS_OK;  // the reference leaves the beam untouched
@@ -631,6 +664,7 @@ hps_status hps_beam_apply_cut(hps_beam_t b, char coord, double lo, double hi) {
 
 hps_status hps_beam_translate(hps_beam_t b, int coord, double v) {
   if (!valid(b) || coord < 0 || coord > HPS_COORD_W) return fail(HPS_ERR_INVALID, "translate: bad argument");
+  ON_DEVICE(b, __func__);
   if (f32(b)) beam32_shift(b->d, coord, v, b->stream);
   else beam_shift(b->d, coord, v, b->stream);
   if (coord == HPS_COORD_PHI) {  // Beam::ShiftPhi re-initialises <phi>_good
@@ -644,6 +678,7 @@ hps_status hps_beam_translate(hps_beam_t b, int coord, double v) {
 
 hps_status hps_beam_monitor(hps_beam_t b, double *out) {
   if (!valid(b) || !out) return fail(HPS_ERR_INVALID, "monitor: bad argument");
+  ON_DEVICE(b, __func__);
   double *dm = nullptr;
   CK(cudaMalloc((void **)&dm, HPS_NMON * sizeof(double)));
   if (f32(b)) beam32_monitor(b->d, nullptr, dm, 0, b->scr, b->stream);
@@ -683,6 +718,7 @@ static hps_status plot_finish(hps_beam_t b, void *user, void *dev, size_t bytes,
 
 hps_status hps_plot_points(hps_beam_t b, int cx, int cy, float *xy, int on_device) {
   if (!valid(b) || !xy || !plot_coord_ok(cx) || !plot_coord_ok(cy)) return fail(HPS_ERR_INVALID, "plot_points: bad argument");
+  ON_DEVICE(b, __func__);
   const size_t bytes = (size_t)b->n * sizeof(float2);
   void *dev = nullptr;
   hps_status s = plot_out(xy, bytes, on_device, &dev);
@@ -693,6 +729,7 @@ hps_status hps_plot_points(hps_beam_t b, int cx, int cy, float *xy, int on_devic
 
 hps_status hps_plot_maxmin(hps_beam_t b, int cx, int cy, int live_only, double out[4]) {
   if (!valid(b) || !out || !plot_coord_ok(cx) || !plot_coord_ok(cy)) return fail(HPS_ERR_INVALID, "plot_maxmin: bad argument");
+  ON_DEVICE(b, __func__);
   void *dev = nullptr;
   hps_status s = plot_out(out, 4 * sizeof(double), 0, &dev);
   if (s) return s;
@@ -705,6 +742,7 @@ hps_status hps_plot_histogram(hps_beam_t b, int coord, uint32_t nbins, double mn
                               int on_device) {
   if (!valid(b) || !hist || !plot_coord_ok(coord) || nbins < 1 || nbins > HPS_PLOT_MAX_BINS || !(mx > mn))
     return fail(HPS_ERR_INVALID, "plot_histogram: bad argument (1 <= nbins <= 12288, max > min)");
+  ON_DEVICE(b, __func__);
   const size_t bytes = (size_t)nbins * sizeof(uint32_t);
   void *dev = nullptr;
   hps_status s = plot_out(hist, bytes, on_device, &dev);
@@ -718,6 +756,7 @@ hps_status hps_plot_histogram2d(hps_beam_t b, int cx, int cy, uint32_t nx, uint3
   if (!valid(b) || !hist || !maxmin || !plot_coord_ok(cx) || !plot_coord_ok(cy) || nx < 1 || ny < 1 ||
       (uint64_t)nx * ny > (1ull << 26))
     return fail(HPS_ERR_INVALID, "plot_histogram2d: bad argument");
+  ON_DEVICE(b, __func__);
   const size_t bytes = (size_t)nx * ny * sizeof(uint32_t);
   void *dev = nullptr;
   hps_status s = plot_out(hist, bytes, on_device, &dev);
@@ -842,6 +881,7 @@ hps_status hps_scheff_create(uint32_t nr, uint32_t nz, uint32_t adj_bunch, hps_s
   if (!pow2(nr) || !pow2(nz) || nz > 512 || nr > 256)
     return fail(HPS_ERR_INVALID, "SCHEFF mesh: nr and nz must be powers of two, nz <= 512, nr <= 256");
   hps_scheff_t s = new hps_scheff_s();
+  cudaGetDevice(&s->dev);
   s->nx = s->nx_init = nr; s->nz = s->nz_init = nz; s->adj_bunch = adj_bunch;
   s->nx_max = nr; s->nz_max = nz;
   hps_status st;
@@ -866,6 +906,7 @@ hps_status hps_scheff_destroy(hps_scheff_t s) {
 // SpaceCharge setters, space_charge.h:43-87
 hps_status hps_scheff_set(hps_scheff_t s, int param, double v) {
   if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  ON_DEVICE(s, __func__);
   switch (param) {
     case 0: s->interval = v; s->interval_init = v; break;
     case 1: s->adj_bunch = (uint32_t)v; break;
@@ -898,6 +939,7 @@ hps_status hps_scheff_set(hps_scheff_t s, int param, double v) {
 }
 hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
   if (!s || !v) return fail(HPS_ERR_INVALID, "bad argument");
+  ON_DEVICE(s, __func__);
   switch (param) {
     case 0: *v = s->interval; break;
     case 1: *v = s->adj_bunch; break;
@@ -937,6 +979,7 @@ hps_status hps_scheff_get(hps_scheff_t s, int param, double *v) {
 // largest mesh.
 hps_status hps_scheff_snapshot(hps_scheff_t s, int fp32, double *bins, double *field, double *mesh) {
   if (!s || !bins || !field || !mesh) return fail(HPS_ERR_INVALID, "scheff_snapshot: bad argument");
+  ON_DEVICE(s, __func__);
   CK(cudaDeviceSynchronize());
   ScState h;
   CK(cudaMemcpy(&h, s->d, sizeof(h), cudaMemcpyDeviceToHost));
@@ -959,6 +1002,7 @@ hps_status hps_scheff_snapshot(hps_scheff_t s, int fp32, double *bins, double *f
 // Scheff::SetMeshSize, space_charge.cpp:61-73 (tables reallocated and zeroed)
 hps_status hps_scheff_set_mesh_size(hps_scheff_t s, uint32_t nr, uint32_t nz) {
   if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  ON_DEVICE(s, __func__);
   if (!pow2(nr) || !pow2(nz) || nz > 512 || nr > 256)
     return fail(HPS_ERR_INVALID, "SCHEFF mesh: nr and nz must be powers of two, nz <= 512, nr <= 256");
   if (nr == s->nx && nz == s->nz) return HPS_OK;
@@ -974,6 +1018,7 @@ hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int3
                                     const int32_t *skip, const uint16_t *const *weights, const float *const *biases,
                                     uint32_t nr, uint32_t nz, double out_scale, double tol, uint32_t n_samples) {
   if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  ON_DEVICE(s, __func__);
   CK(cudaDeviceSynchronize());
   SurNet *n = new SurNet();
   std::string err;
@@ -992,6 +1037,7 @@ hps_status hps_scheff_set_surrogate(hps_scheff_t s, int32_t n_layers, const int3
 
 hps_status hps_scheff_clear_surrogate(hps_scheff_t s) {
   if (!s) return fail(HPS_ERR_INVALID, "bad scheff handle");
+  ON_DEVICE(s, __func__);
   if (!s->sur) return HPS_OK;
   CK(cudaDeviceSynchronize());
   delete s->sur;
@@ -1002,6 +1048,7 @@ hps_status hps_scheff_clear_surrogate(hps_scheff_t s) {
 
 hps_status hps_scheff_surrogate_stats(hps_scheff_t s, double *accepted, double *rejected, double *residual) {
   if (!s || !s->sur) return fail(HPS_ERR_INVALID, "scheff_surrogate_stats: no surrogate attached");
+  ON_DEVICE(s, __func__);
   if (sur_read(*s->sur, accepted, rejected, residual)) return fail(HPS_ERR_CUDA, "scheff_surrogate_stats: read failed");
   return HPS_OK;
 }
@@ -1513,6 +1560,9 @@ extern "C" {
 
 hps_status hps_sim_create(hps_beam_t beam, hps_beamline_t bl, hps_scheff_t scheff, hps_sim_t *out) {
   if (!out || !valid(beam) || !bl) return fail(HPS_ERR_INVALID, "sim_create: bad argument");
+  ON_DEVICE(beam, __func__);
+  if (scheff && scheff->dev != beam->dev)
+    return fail(HPS_ERR_INVALID, "sim_create: the beam and the SpaceCharge live on different devices");
   hps_sim_t s = new hps_sim_s();
   s->beam = beam; s->bl = bl; s->sc = scheff;
   s->sc_on = scheff != nullptr;
@@ -1596,6 +1646,8 @@ hps_status hps_sim_last_time_ms(hps_sim_t s, double *ms) {
 }
 
 hps_status hps_sim_simulate(hps_sim_t s, int32_t start, int32_t end) {
+  if (!s) return fail(HPS_ERR_INVALID, "bad sim handle");
+  ON_DEVICE(s->beam, __func__);
   RunPlan p;
   hps_status e = plan_run(s, start, end, &p);
   if (e || p.empty) return e;
@@ -1660,7 +1712,10 @@ hps_status hps_batch_create(const hps_sim_t *sims, uint32_t count, hps_batch_t *
       if (v[i]->sc && v[j]->sc == v[i]->sc)
         return fail(HPS_ERR_INVALID, "batch_create: every simulator of a batch needs its own SpaceCharge");
     }
+    if (v[i]->beam->dev != v[0]->beam->dev)
+      return fail(HPS_ERR_INVALID, "batch_create: the simulators live on different devices");
   }
+  ON_DEVICE(v[0]->beam, __func__);  // the batch's streams and events are made on it
   hps_batch_t bt = new hps_batch_s();
   bt->sims = v;
   if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1821,6 +1876,7 @@ hps_status hps_batch_last_mode(hps_batch_t bt, int *lockstep, char *why, size_t 
 // no mesh-size cut-off energy).
 hps_status hps_batch_simulate(hps_batch_t bt, int32_t start, int32_t end) {
   if (!bt) return fail(HPS_ERR_INVALID, "bad batch handle");
+  ON_DEVICE(bt->sims[0]->beam, __func__);
   const size_t m = bt->sims.size();
   std::vector<RunPlan> plans(m);
   for (size_t k = 0; k < m; ++k) {
@@ -2110,6 +2166,7 @@ extern "C" {
 hps_status hps_sim_autotune(hps_sim_t s, int32_t start, int32_t end, int32_t reps, int32_t *shape_out, double *ms_out,
                             uint32_t ms_cap, uint32_t *n_timed) {
   if (!s || reps < 1 || reps > 64) return fail(HPS_ERR_INVALID, "sim_autotune: bad argument");
+  ON_DEVICE(s->beam, __func__);
   const std::string key = tune_key(s, "sim");
   std::vector<double> times;
   Shape best{};
@@ -2151,6 +2208,7 @@ hps_status hps_sim_autotune(hps_sim_t s, int32_t start, int32_t end, int32_t rep
 hps_status hps_batch_autotune(hps_batch_t bt, int32_t start, int32_t end, int32_t reps, int32_t *shape_out,
                               double *ms_out, uint32_t ms_cap, uint32_t *n_timed) {
   if (!bt || bt->sims.empty() || reps < 1 || reps > 64) return fail(HPS_ERR_INVALID, "batch_autotune: bad argument");
+  ON_DEVICE(bt->sims[0]->beam, __func__);
   const std::string key = tune_key(bt->sims[0], bt->lockstep ? "batch-lockstep" : "batch") + "|" +
                           std::to_string(bt->sims.size());
   std::vector<double> times;

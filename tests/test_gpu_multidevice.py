@@ -47,3 +47,36 @@ def test_switching_devices_in_one_process():
     assert np.array_equal(fields[0], fields[1])
     HPSim.set_gpu(0)
     torch.cuda.set_device(0)
+
+
+def test_objects_refuse_calls_from_another_device():
+    """A beam, solver, simulator or batch runs on the device it was made on:
+    while another device is current its calls return HPS_ERR_STATE (no
+    kernel touches another device's memory), and a simulator cannot join a
+    beam and a solver of different devices."""
+    import torch
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two visible GPUs")
+    from hpsim_gb300 import HPSim, lattices as L
+    from hpsim_gb300._capi import dptr, lib
+    HPSim.set_gpu(0)
+    beam = HPSim.Beam(mass=939.294, charge=-1.0, current=0.015, num=4096, precision="fp32")
+    beam.set_waterbag(*L.waterbag_twiss(), 0.0, 0.75, 201.25, 7)
+    beam.set_ref_w(0.75)
+    sc0 = HPSim.SpaceCharge(32, 128, 0.10, 0)
+    sim = HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()[:5]), sc0)
+    try:
+        HPSim.set_gpu(1)
+        out = np.zeros(4096)
+        assert lib().hps_beam_get_coord(beam.handle, 0, dptr(out)) == 5  # HPS_ERR_STATE
+        assert b"device 0" in lib().hps_last_error()
+        with pytest.raises(Exception):
+            sim.simulate()
+        sc1 = HPSim.SpaceCharge(32, 128, 0.10, 0)  # made on device 1
+        HPSim.set_gpu(0)
+        with pytest.raises(Exception):
+            HPSim.Simulator(beam, HPSim.BeamLine(elements=L.small_fodo()[:5]), sc1)
+        sim.simulate()  # back on its own device
+        assert beam.get_loss_num() == 0
+    finally:
+        HPSim.set_gpu(0)
