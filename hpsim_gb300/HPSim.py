@@ -369,6 +369,49 @@ class DBConnection:
         return epics_channels(self)
 
 
+def _db_args(dbconnection, beamline=None, what=""):
+    if not isinstance(dbconnection, DBConnection):
+        raise TypeError(f"{what}: needs a DBConnection")
+    if beamline is not None and not isinstance(beamline, BeamLine):
+        raise TypeError(f"{what}: needs a BeamLine")
+
+
+def get_db_model(record_name, field_name, dbconnection):
+    """get_db_model(record_name, field_name, DBConnection) -> the model
+    parameter's value in the database as text, or None (hpsim_module.cpp:
+    307-360)."""
+    from .dbloader import get_db_model as _get
+    _db_args(dbconnection, what="get_db_model")
+    return _get(str(record_name), str(field_name), dbconnection)
+
+
+def set_db_model(record_name, field_name, value, dbconnection, beamline):
+    """set_db_model(record_name, field_name, value, DBConnection, BeamLine):
+    set a model parameter in the database and hand the recomputed model
+    values to the beamline's elements (hpsim_module.cpp:86-267; the lattice
+    loader's dbloader.set_db_model)."""
+    from .dbloader import set_db_model as _set
+    _db_args(dbconnection, beamline, "set_db_model")
+    _set(str(record_name), str(field_name), value, dbconnection, beamline)
+
+
+def get_db_epics(pv_name, dbconnection):
+    """get_db_epics(pv_name, DBConnection) -> the channel's value in the
+    database as text, or None (hpsim_module.cpp:269-305)."""
+    from .dbloader import get_db_epics as _get
+    _db_args(dbconnection, what="get_db_epics")
+    return _get(str(pv_name), dbconnection)
+
+
+def set_db_epics(pv_name, value, dbconnection, beamline):
+    """set_db_epics(pv_name, value, DBConnection, BeamLine)
+    (hpsim_module.cpp:52-84) drives the EPICS server's PV observers
+    (src/server), which this package does not include: it raises.  Model
+    parameters are set with set_db_model."""
+    raise NotImplementedError("set_db_epics: the EPICS server's PV observers are not part of this package; "
+                              "set model parameters with set_db_model")
+
+
 class BeamLine:
     """BeamLine(DBConnection) (wrap_beamline.cpp:24-41).
 

@@ -34,12 +34,40 @@ KINDS = {
 }
 
 
+def _math_functions(conn):
+    """The databases' triggers call pi(), power(), cos(), acos() and their
+    kin; SQLite builds without its math functions get them from Python's
+    math module."""
+    try:
+        conn.execute("select pi(), power(2, 2), cos(0), acos(1), radians(0)").fetchone()
+        return
+    except sqlite3.OperationalError:
+        pass
+    import math
+
+    def safe(f):
+        def g(*a):
+            try:
+                return None if any(x is None for x in a) else f(*(float(x) for x in a))
+            except (ValueError, OverflowError):
+                return None  # NULL, as SQLite's own functions give for a domain error
+        return g
+    fns = {"pi": (0, lambda: math.pi), "power": (2, math.pow), "pow": (2, math.pow), "sqrt": (1, math.sqrt),
+           "cos": (1, math.cos), "sin": (1, math.sin), "tan": (1, math.tan), "acos": (1, math.acos),
+           "asin": (1, math.asin), "atan": (1, math.atan), "atan2": (2, math.atan2), "exp": (1, math.exp),
+           "ln": (1, math.log), "log10": (1, math.log10), "radians": (1, math.radians),
+           "degrees": (1, math.degrees)}
+    for name, (n, f) in fns.items():
+        conn.create_function(name, n, safe(f), deterministic=True)
+
+
 def open_connection(db_addr):
     """DBConnection(db_addr): the connection and its database list
     [("main", path)]."""
     if not os.path.exists(db_addr):
         raise ValueError(f"DBConnection: no database at {db_addr}")
     conn = sqlite3.connect(db_addr)
+    _math_functions(conn)
     return conn, [("main", db_addr)]
 
 
@@ -192,3 +220,153 @@ def epics_channels(dbc):
     for db, _ in dbc.dbs:
         out += [r[0] for r in dbc._conn.execute(f"select lcs_name from {_ident(db)}.epics_channel")]
     return out
+
+
+# ---- model and channel values by record name (hpsim_module.cpp:86-360) ----
+
+def _tables(conn, db):
+    return [r[0] for r in conn.execute(f"select name from {_ident(db)}.sqlite_master where type = 'table'")]
+
+
+def _columns(conn, db, tbl):
+    return [r[1] for r in conn.execute(f"pragma {_ident(db)}.table_info({_ident(tbl)})")]
+
+
+def _text(conn, sql, args):
+    """GetDataFromDB: the first row's first column as SQLite renders it as
+    text; '' for no row, NULL, or a table without the queried columns."""
+    try:
+        row = conn.execute(sql, args).fetchone()
+    except sqlite3.OperationalError:
+        return ""
+    return "" if row is None or row[0] is None else str(row[0])
+
+
+def get_db_model(record_name, field_name, dbc):
+    """GetDbModel (hpsim_module.cpp:307-360): the value of ``field_name`` of
+    the record called ``record_name``, from the first table (every database
+    of the connection in order, ``epics_channel`` excluded) that has the
+    column and a non-NULL value there, as text; None when none has."""
+    conn = dbc._conn
+    for db, _ in dbc.dbs:
+        for tbl in _tables(conn, db):
+            if tbl == "epics_channel" or field_name not in _columns(conn, db, tbl):
+                continue
+            v = _text(conn, f"select cast({field_name} as text) from {db}.{tbl} where name = ?", (record_name,))
+            if v != "":
+                return v
+    return None
+
+
+def get_db_epics(pv_name, dbc):
+    """GetDbEPICS (hpsim_module.cpp:269-305): the ``value`` of the
+    ``epics_channel`` row whose ``lcs_name`` is ``pv_name`` (first database
+    that has one), as text; None when no database has a value for it."""
+    conn = dbc._conn
+    for db, _ in dbc.dbs:
+        v = _text(conn, f"select cast(value as text) from {_ident(db)}.epics_channel where lcs_name = ?",
+                  (pv_name,))
+        if v != "":
+            return v
+    return None
+
+
+def _sql_number(value):
+    """The reference pastes ``value`` into the UPDATE statement as an SQL
+    literal: an integer literal stays an integer, anything else numeric is a
+    real; here it is bound as a parameter of that type."""
+    s = str(value).strip()
+    try:
+        return int(s) if s.lstrip("+-").isdigit() else float(s)
+    except ValueError:
+        raise ValueError(f"set_db_model: {value!r} is not a number") from None
+
+
+# tables set_db_model changes, and for each the fields whose new model value
+# it also hands to the beamline's element: (field changed, model column read
+# back after the database's triggers ran, element parameter)
+_MODEL_PUSH = {
+    "spch_comp": {"fraction_model": ("fraction_model", "fraction")},
+    "buncher": {"phase_offset_cal": ("phase_model", "phase")},
+    "raperture": {f: (f, p) for f, p in (("aperture_xl_model", "xl"), ("aperture_xr_model", "xr"),
+                                         ("aperture_yt_model", "yt"), ("aperture_yb_model", "yb"),
+                                         ("in_out_model", "in"))},
+    "caperture": {"aperture_model": ("aperture_model", "aperture"), "in_out_model": ("in_out_model", "in")},
+    "rf_module": {},
+}
+# rf_module fields and the rf_gap columns -> element parameters they reach
+_RF_PUSH = {
+    "phase_offset_cal": (("beam_phase_shift_model", "phase_shift"),),
+    "amplitude_scale_cal": (("amplitude_model", "amplitude"), ("ref_phase_model", "phase_ref")),
+    "amplitude_tilt_cal": (("amplitude_model", "amplitude"), ("ref_phase_model", "phase_ref")),
+    "voltage_cal": (("amplitude_model", "amplitude"), ("ref_phase_model", "phase_ref")),
+}
+
+
+def _model_index(dbc, db, tbl, where, args):
+    """The beamline index of a record: the connection's own record of it
+    (kept for every database, writable or not), else the table's
+    model_index column."""
+    conn = dbc._conn
+    row = conn.execute(f"select view_index, model_index from {db}.{tbl} where {where}", args).fetchone()
+    if row is None:
+        return None
+    mi = dbc.model_index.get((db, tbl, row[0]))
+    if mi is None and row[1] is not None:
+        mi = int(row[1])
+    return mi
+
+
+def _push(beamline, index, key, text):
+    if index is None or beamline is None:
+        return
+    v = _f(text)
+    if key == "in":
+        v = 1.0 if _on(text) else 0.0
+    beamline.set_param(int(index), key, v)
+
+
+def set_db_model(record_name, field_name, value, dbc, beamline):
+    """SetDbModel (hpsim_module.cpp:86-267): set ``field_name`` of the record
+    ``record_name`` in the first of the tables buncher, rf_module, spch_comp,
+    raperture and caperture (every database of the connection in order) that
+    has the column and the record, let the database's triggers recompute the
+    model columns, and hand the new model values to the beamline's elements:
+    a space-charge compensation's fraction, a buncher's phase (after
+    ``phase_offset_cal``), an aperture's sizes and in/out flag, and for an RF
+    module every gap of the module (``phase_offset_cal``: the beam phase
+    shift; ``amplitude_scale_cal``, ``amplitude_tilt_cal``, ``voltage_cal``:
+    amplitude and reference phase).  Returns True when a table took the
+    change, False (with a message on stderr, as the reference prints) when
+    none had the record and field."""
+    import sys
+    conn = dbc._conn
+    num = _sql_number(value)
+    for db, _ in dbc.dbs:
+        for tbl in _tables(conn, db):
+            if tbl not in _MODEL_PUSH or field_name not in _columns(conn, db, tbl):
+                continue
+            if conn.execute(f"select 1 from {db}.{tbl} where name = ? limit 1", (record_name,)).fetchone() is None:
+                continue
+            try:
+                with conn:
+                    conn.execute(f"update {db}.{tbl} set {field_name} = ? where name = ?", (num, record_name))
+            except sqlite3.Error as e:
+                raise RuntimeError(f"set_db_model: {record_name}:{field_name}: {e}") from None
+            if tbl == "rf_module":
+                cols = _RF_PUSH.get(field_name, ())
+                if cols:
+                    gaps = conn.execute(
+                        f"select view_index, model_index, {', '.join(c for c, _ in cols)} from {db}.rf_gap "
+                        f"where module_id = (select id from {db}.rf_module where name = ?)", (record_name,)).fetchall()
+                    for vi, mi_col, *vals in gaps:
+                        mi = dbc.model_index.get((db, "rf_gap", vi), mi_col)
+                        for (_, key), v in zip(cols, vals):
+                            _push(beamline, mi, key, v)
+            elif field_name in _MODEL_PUSH[tbl]:
+                col, key = _MODEL_PUSH[tbl][field_name]
+                text = _text(conn, f"select cast({col} as text) from {db}.{tbl} where name = ?", (record_name,))
+                _push(beamline, _model_index(dbc, db, tbl, "name = ?", (record_name,)), key, text)
+            return True
+    print(f"Error in set_db_model: can't make the change for {record_name}:{field_name}", file=sys.stderr)
+    return False
