@@ -229,7 +229,11 @@ def _tables(conn, db):
 
 
 def _columns(conn, db, tbl):
-    return [r[1] for r in conn.execute(f"pragma {_ident(db)}.table_info({_ident(tbl)})")]
+    """The table's column names; none for a table whose name is not a plain
+    identifier (no element table has such a name)."""
+    if not tbl.replace("_", "").isalnum():
+        return []
+    return [r[1] for r in conn.execute(f"pragma {_ident(db)}.table_info({tbl})")]
 
 
 def _text(conn, sql, args):
