@@ -1,8 +1,6 @@
 """Run a lattice through the CUDA path (hpsim_gb300.HPSim over the C ABI)."""
 from __future__ import annotations
 
-import numpy as np
-
 COORDS = ("x", "xp", "y", "yp", "phi", "w")
 
 
