@@ -64,7 +64,9 @@ def parse():
     p.add_argument("--surrogate", nargs="?", const=SURROGATE_NET, default=None,
                    help="small_fodo (FP64): time the plain path, then with the learned field surrogate attached "
                         "(a network file; default the shipped 32x128 network), and report both")
-    p.add_argument("--surrogate-tol", type=float, default=0.02)
+    p.add_argument("--surrogate-tol", type=float, default=None,
+                   help="the network's spot-check tolerance: default 0.015 for the DTL-like batch (the largest "
+                        "measured that meets the 1e-3 emittance gate there), 0.02 for the small_fodo ablation")
     p.add_argument("--surrogate-kernel", choices=["tensor", "cuda"], default="cuda",
                    help="the surrogate's layers on CUDA cores (default: faster at one plane) or on the tensor cores")
     p.add_argument("--no-autotune", action="store_true",
@@ -841,9 +843,10 @@ def main():
                                    device=f"cuda:{local}")
         mon_plain = monitored()
         net = np.load(args.surrogate)
-        sc.set_surrogate(net, tol=args.surrogate_tol)
+        tol = 0.02 if args.surrogate_tol is None else args.surrogate_tol
+        sc.set_surrogate(net, tol=tol)
         sc.set_surrogate_kernel(args.surrogate_kernel)
-        sur = {"network": os.path.relpath(args.surrogate, ROOT), "tol": args.surrogate_tol, "layers": args.surrogate_kernel,
+        sur = {"network": os.path.relpath(args.surrogate, ROOT), "tol": tol, "layers": args.surrogate_kernel,
                "plain_value": plain_value, "plain_ms_per_step": sum(plain_ms) / len(plain_ms),
                "network_val_field_err_median": float(net["meta_val_median"]) if "meta_val_median" in net else None}
 
@@ -938,7 +941,8 @@ def main():
     # the headline comparison: surrogate + batched against the plain path
     sb_rec = sb_check = None
     if args.workload == "dtl_like" and args.surrogate_batch > 0 and ws == 1 and not args.surrogate:
-        sb_rec, sb_check = surrogate_batched(args, value, local, flush, SURROGATE_NET, args.surrogate_tol)
+        sb_tol = 0.015 if args.surrogate_tol is None else args.surrogate_tol
+        sb_rec, sb_check = surrogate_batched(args, value, local, flush, SURROGATE_NET, sb_tol)
 
     if rank != 0:
         return
